@@ -1,0 +1,339 @@
+"""The reference's native world API over the GB300 engine.
+
+Mirrors ``createSolverPipeline({backend})`` (``src/native/pipeline.js:14-92``) with a
+``"gb300"`` backend, the world object's stepping, reads and writes (``src/native/scenes.d.ts:
+317-454``, ``src/native/runtime.js:46-272``) and, as an addition the reference does not have,
+batches of worlds stepped together. Every method validates its arguments before calling the
+engine and raises ``ValueError`` (the reference throws synchronously); engine failures raise
+``AvbdError``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+
+import numpy as np
+
+from . import _lib as L
+from .scene import AvbdScene3D, SceneArrays
+
+
+def _arrays(scene) -> SceneArrays:
+    if isinstance(scene, AvbdScene3D):
+        scene.created = True
+        return scene.arrays()
+    if isinstance(scene, SceneArrays):
+        return scene
+    raise ValueError("expected an AvbdScene3D or SceneArrays")
+
+
+class SolverPipeline:
+    """A device context owning worlds and batches; ``destroy()`` releases all of them."""
+
+    backend = "gb300"
+
+    def __init__(self, device: int = 0):
+        h = C.c_void_p()
+        L.check(L.lib().avbd_ctx_create(int(device), C.byref(h)))
+        self._h = h
+        self._children = []
+
+    def _live(self):
+        if self._h is None:
+            raise RuntimeError("The pipeline has been destroyed")
+
+    @property
+    def stream(self) -> int:
+        """The engine's cudaStream_t (as an integer handle)."""
+        self._live()
+        h = C.c_void_p()
+        L.check(L.lib().avbd_ctx_stream(self._h, C.byref(h)))
+        return int(h.value or 0)
+
+    def synchronize(self):
+        self._live()
+        L.check(L.lib().avbd_ctx_synchronize(self._h))
+
+    def createSolver(self, scene, options=None) -> "World":
+        self._live()
+        if options:
+            unknown = set(options) - {"spatialSort"}
+            if unknown:
+                raise ValueError(f"unsupported solver options {sorted(unknown)}")
+        w = World(self, _arrays(scene))
+        self._children.append(w)
+        return w
+
+    def createBatch(self, scenes) -> "Batch":
+        self._live()
+        b = Batch(self, [_arrays(s) for s in scenes])
+        self._children.append(b)
+        return b
+
+    def destroy(self):
+        if self._h is None:
+            return
+        for c in self._children:
+            c._h = None  # freed with the context
+        self._children.clear()
+        L.check(L.lib().avbd_ctx_destroy(self._h))
+        self._h = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+
+def createSolverPipeline(backend: str = "gb300", device: int = 0) -> SolverPipeline:
+    """``createSolverPipeline({backend: "gb300"})``; the reference's "webgpu" and "cpu"
+    backends are not part of this engine."""
+    if backend != "gb300":
+        raise ValueError('backend must be "gb300"')
+    return SolverPipeline(device)
+
+
+def _indices(indices, n):
+    idx = np.ascontiguousarray(np.asarray(indices, dtype=np.int64).reshape(-1))
+    if idx.size and (idx.min() < 0 or idx.max() >= n):
+        raise ValueError("body index out of range")
+    return idx.astype(np.uint32)
+
+
+class World:
+    """One world (``pipeline.createSolver(scene)``)."""
+
+    def __init__(self, pipe: SolverPipeline, arrays: SceneArrays):
+        self._pipe = pipe
+        self._packed = L.PackedScene(arrays)
+        h = C.c_void_p()
+        L.check(L.lib().avbd_world_create(pipe._h, C.byref(self._packed.desc), C.byref(self._packed.params), C.byref(h)))
+        self._h = h
+        self.bodyCount = arrays.n_bodies
+        self.jointCount = self._packed.n_joints
+        self.dt = float(arrays.params.dt)
+        self.timeAccumulator = 0.0
+
+    def _live(self):
+        if self._h is None:
+            raise RuntimeError("The solver has been destroyed")
+
+    # stepping ---------------------------------------------------------------
+    def step(self, steps: int = 1):
+        self._live()
+        if int(steps) != steps or steps < 0:
+            raise ValueError("steps must be a non-negative integer")
+        L.check(L.lib().avbd_world_step(self._h, int(steps)))
+        return self
+
+    def advance(self, elapsed: float, maxSubSteps: int = 8, maxFrameTime: float = 0.25) -> int:
+        """Fixed-step accumulator (``src/native/runtime.js:255-272``); returns steps taken."""
+        self._live()
+        if not math.isfinite(elapsed) or elapsed < 0:
+            raise ValueError("elapsed must be finite nonnegative seconds")
+        if int(maxSubSteps) != maxSubSteps or maxSubSteps < 1 or not math.isfinite(maxFrameTime) or maxFrameTime <= 0:
+            raise ValueError("Stepping limits must be positive")
+        dt = self.dt
+        self.timeAccumulator = min(maxSubSteps * dt, self.timeAccumulator + min(maxFrameTime, elapsed))
+        count = 0
+        while self.timeAccumulator + 1e-12 >= dt and count < maxSubSteps:
+            count += 1
+            self.timeAccumulator = max(0.0, self.timeAccumulator - dt)
+        if count:
+            self.step(count)
+        return count
+
+    # reads --------------------------------------------------------------------
+    def readBodyState(self) -> dict:
+        """Positions, rotations, velocities, angular and previous velocities (float32)."""
+        self._live()
+        n = self.bodyCount
+        out = {k: np.zeros((n, 4 if k == "rotation" else 3), dtype=np.float32)
+               for k in ("position", "rotation", "velocity", "angular", "prev_velocity")}
+        L.check(L.lib().avbd_world_read_state(self._h, *(L.fptr(out[k]) for k in
+                                                         ("position", "rotation", "velocity", "angular", "prev_velocity"))))
+        return out
+
+    def readSelectedBodies(self, indices, posesOnly: bool = False) -> np.ndarray:
+        """8 floats per body (pos, friction, quat) or the 40-float body record."""
+        self._live()
+        idx = _indices(indices, self.bodyCount)
+        stride = 8 if posesOnly else 40
+        out = np.zeros(idx.size * stride, dtype=np.float32)
+        L.check(L.lib().avbd_world_read_selected(self._h, L.uptr(idx), idx.size, int(bool(posesOnly)), L.fptr(out)))
+        return out
+
+    def readBodies(self) -> np.ndarray:
+        return self.readSelectedBodies(np.arange(self.bodyCount))
+
+    def readCounters(self) -> dict:
+        self._live()
+        c = L.Counters()
+        L.check(L.lib().avbd_world_counters(self._h, C.byref(c)))
+        return {k: getattr(c, k) for k, _ in L.Counters._fields_}
+
+    # writes -------------------------------------------------------------------
+    def setPoses(self, indices, positions, rotations=None):
+        self._live()
+        idx = _indices(indices, self.bodyCount)
+        p = np.ascontiguousarray(np.asarray(positions, dtype=np.float32).reshape(idx.size, 3))
+        r = None if rotations is None else np.ascontiguousarray(np.asarray(rotations, dtype=np.float32).reshape(idx.size, 4))
+        if not np.isfinite(p).all() or (r is not None and (not np.isfinite(r).all() or (np.abs(r).sum(1) == 0).any())):
+            raise ValueError("poses must be finite and rotations nonzero")
+        L.check(L.lib().avbd_world_set_poses(self._h, L.uptr(idx), idx.size, L.fptr(p), L.fptr(r)))
+
+    def setVelocities(self, indices, linear=None, angular=None):
+        self._live()
+        idx = _indices(indices, self.bodyCount)
+        v = None if linear is None else np.ascontiguousarray(np.asarray(linear, dtype=np.float32).reshape(idx.size, 3))
+        a = None if angular is None else np.ascontiguousarray(np.asarray(angular, dtype=np.float32).reshape(idx.size, 3))
+        for x in (v, a):
+            if x is not None and not np.isfinite(x).all():
+                raise ValueError("velocities must be finite")
+        L.check(L.lib().avbd_world_set_velocities(self._h, L.uptr(idx), idx.size, L.fptr(v), L.fptr(a)))
+
+    def setLinearVelocities(self, indices, linear):
+        self.setVelocities(indices, linear=linear)
+
+    def setAngularVelocities(self, indices, angular):
+        self.setVelocities(indices, angular=angular)
+
+    # parity dumps (readPairs / readContactList) ------------------------------------
+    def readPairs(self) -> np.ndarray:
+        self._live()
+        n = C.c_int64()
+        L.check(L.lib().avbd_world_pairs(self._h, None, 0, C.byref(n)))
+        out = np.zeros((n.value, 2), dtype=np.uint32)
+        L.check(L.lib().avbd_world_pairs(self._h, L.uptr(out), n.value, C.byref(n)))
+        return out
+
+    def readPairContacts(self) -> np.ndarray:
+        self._live()
+        n = C.c_int64()
+        L.check(L.lib().avbd_world_pair_contacts(self._h, None, 0, C.byref(n)))
+        out = np.zeros(n.value, dtype=np.int32)
+        L.check(L.lib().avbd_world_pair_contacts(self._h, L.iptr(out), n.value, C.byref(n)))
+        return out
+
+    def readColors(self) -> np.ndarray:
+        self._live()
+        out = np.zeros(self.bodyCount, dtype=np.int32)
+        L.check(L.lib().avbd_world_colors(self._h, L.iptr(out)))
+        return out
+
+    def exportState(self) -> dict:
+        """Full solver state (bodies, joints, manifolds with their contacts, colours)."""
+        self._live()
+        nj, nm, nc = C.c_int32(), C.c_int64(), C.c_int64()
+        L.check(L.lib().avbd_world_state_sizes(self._h, C.byref(nj), C.byref(nm), C.byref(nc)))
+        j, m, c = nj.value, nm.value, nc.value
+        st = {k: np.zeros((j, 3), dtype=np.float32) for k in ("jpen_lin", "jpen_ang", "jlam_lin", "jlam_ang")}
+        st["jbroken"] = np.zeros(j, dtype=np.int32)
+        st["mpairs"] = np.zeros((m, 2), dtype=np.uint32)
+        st["mcount"] = np.zeros(m, dtype=np.int32)
+        st["cfeature"] = np.zeros(c, dtype=np.uint32)
+        for k in ("cra", "crb", "cpen", "clam"):
+            st[k] = np.zeros((c, 3), dtype=np.float32)
+        st["cstick"] = np.zeros(c, dtype=np.int32)
+        L.check(L.lib().avbd_world_export_state(
+            self._h, L.fptr(st["jpen_lin"]), L.fptr(st["jpen_ang"]), L.fptr(st["jlam_lin"]), L.fptr(st["jlam_ang"]),
+            L.iptr(st["jbroken"]), L.uptr(st["mpairs"]), L.iptr(st["mcount"]), L.uptr(st["cfeature"]),
+            L.fptr(st["cra"]), L.fptr(st["crb"]), L.fptr(st["cpen"]), L.fptr(st["clam"]), L.iptr(st["cstick"])))
+        b = self.readBodyState()
+        st.update(pos=b["position"], quat=b["rotation"], vel=b["velocity"], angvel=b["angular"],
+                  prev_vel=b["prev_velocity"], colors=self.readColors())
+        return st
+
+    def profile(self, enable: bool = True):
+        """Start (and reset) or stop per-kernel-class timing and traffic accounting."""
+        self._live()
+        L.check(L.lib().avbd_world_profile(self._h, int(bool(enable))))
+
+    def profileRead(self) -> dict:
+        self._live()
+        p = L.Profile()
+        L.check(L.lib().avbd_world_profile_read(self._h, C.byref(p)))
+        return {k: getattr(p, k) for k, _ in L.Profile._fields_ if k != "pad"}
+
+    def destroy(self):
+        if self._h is None:
+            return
+        L.check(L.lib().avbd_world_destroy(self._h))
+        self._h = None
+        if self in self._pipe._children:
+            self._pipe._children.remove(self)
+
+
+class Batch:
+    """Many independent worlds stepped together in one launch sequence per step."""
+
+    def __init__(self, pipe: SolverPipeline, arrays_list):
+        if not arrays_list:
+            raise ValueError("a batch needs at least one world")
+        self._pipe = pipe
+        self._packed = [L.PackedScene(a) for a in arrays_list]
+        descs = (L.SceneDesc * len(arrays_list))(*[p.desc for p in self._packed])
+        params = (L.Params * len(arrays_list))(*[p.params for p in self._packed])
+        h = C.c_void_p()
+        L.check(L.lib().avbd_batch_create(pipe._h, descs, params, len(arrays_list), C.byref(h)))
+        self._h = h
+        self.worldCount = len(arrays_list)
+        self.bodyCounts = [a.n_bodies for a in arrays_list]
+        self.bodyCount = int(sum(self.bodyCounts))
+
+    def step(self, steps: int = 1):
+        if self._h is None:
+            raise RuntimeError("The batch has been destroyed")
+        L.check(L.lib().avbd_batch_step(self._h, int(steps)))
+        return self
+
+    def readBodyState(self, world: int) -> dict:
+        if not 0 <= world < self.worldCount:
+            raise ValueError("world index out of range")
+        n = self.bodyCounts[world]
+        out = {k: np.zeros((n, 4 if k == "rotation" else 3), dtype=np.float32)
+               for k in ("position", "rotation", "velocity", "angular", "prev_velocity")}
+        L.check(L.lib().avbd_batch_read_state(self._h, int(world), *(L.fptr(out[k]) for k in
+                                                                     ("position", "rotation", "velocity", "angular", "prev_velocity"))))
+        return out
+
+    def readCounters(self) -> dict:
+        c = L.Counters()
+        L.check(L.lib().avbd_batch_counters(self._h, C.byref(c)))
+        return {k: getattr(c, k) for k, _ in L.Counters._fields_}
+
+    def readPoses(self, out: np.ndarray | None = None) -> np.ndarray:
+        """Poses of all bodies of all worlds, (bodyCount, 8) float32: pos, friction, quat."""
+        if out is None:
+            out = np.zeros((self.bodyCount, 8), dtype=np.float32)
+        if out.dtype != np.float32 or out.size != self.bodyCount * 8 or not out.flags["C_CONTIGUOUS"]:
+            raise ValueError("out must be a contiguous float32 array of bodyCount x 8")
+        L.check(L.lib().avbd_batch_read_poses(self._h, L.fptr(out)))
+        return out
+
+    def setVelocities(self, indices, linear=None, angular=None):
+        """Batch-global body indices (world offset + body index)."""
+        idx = _indices(indices, self.bodyCount)
+        v = None if linear is None else np.ascontiguousarray(np.asarray(linear, dtype=np.float32).reshape(idx.size, 3))
+        a = None if angular is None else np.ascontiguousarray(np.asarray(angular, dtype=np.float32).reshape(idx.size, 3))
+        for x in (v, a):
+            if x is not None and not np.isfinite(x).all():
+                raise ValueError("velocities must be finite")
+        L.check(L.lib().avbd_batch_set_velocities(self._h, L.uptr(idx), idx.size, L.fptr(v), L.fptr(a)))
+
+    def profile(self, enable: bool = True):
+        L.check(L.lib().avbd_batch_profile(self._h, int(bool(enable))))
+
+    def profileRead(self) -> dict:
+        p = L.Profile()
+        L.check(L.lib().avbd_batch_profile_read(self._h, C.byref(p)))
+        return {k: getattr(p, k) for k, _ in L.Profile._fields_ if k != "pad"}
+
+    def destroy(self):
+        if self._h is None:
+            return
+        L.check(L.lib().avbd_batch_destroy(self._h))
+        self._h = None
+        if self in self._pipe._children:
+            self._pipe._children.remove(self)

@@ -1,0 +1,767 @@
+// Collision stage: hashed-grid broadphase and narrowphase with warm-start matching.
+//
+// Compiled with -fmad=false: every product and sum is rounded separately, in the order of
+// the reference's arithmetic, so pair sets and contact counts match its float32 results
+// exactly.
+//
+// Broadphase. The pair predicate is the reference CPU's (src/native/cpu/cpuPhysics3D.js:319-343):
+// A = the higher body index, B = the lower; bounding spheres overlap (|xA - xB|^2 <= (rA + rB)^2),
+// not both static, collision masks agree, and no live joint/spring/ignore links the two. A hashed
+// grid only narrows the candidates: per world, bodies with radius <= largeR go into cells of size
+// cell >= 2 * max small radius keyed by (world, cell); each small body scans the 27 cells around
+// its own for lower-index partners, every body scans its world's large-body list, and large
+// bodies scan their world's lower-index small bodies. Two passes (count, then write after a
+// prefix sum) give each body a private output range, which it sorts by partner: the pair list
+// comes out sorted by (hi, lo) with no global sort and no atomics on the output.
+//
+// Narrowphase. One thread per candidate pair. Box-box: 15-axis SAT with the faceBias rule,
+// reference-face clipping, up to 8 contacts (src/native/cpu/cpuBoxContacts3D.ts:409-499, the
+// pinned reference/three-avbd/src/avbd3d/ref/collide.ts). Pairs with a sphere: the reference
+// CPU's generic support-function SAT with one contact (src/native/cpu/cpuContacts3D.js:188-296).
+// Warm start: the previous step's manifold of the same pair is found by binary search in the
+// previous (sorted) pair list and its contacts are matched by feature key
+// (src/native/cpu/cpuPhysics3D.js:76-147).
+#include <float.h>
+
+#include "engine.cuh"
+
+namespace avbd {
+
+// ------------------------------------------------------------------ grid
+
+__device__ __forceinline__ uint32_t mix32(uint32_t x) {
+  x ^= x >> 16;
+  x *= 0x7feb352du;
+  x ^= x >> 15;
+  x *= 0x846ca68bu;
+  x ^= x >> 16;
+  return x;
+}
+
+__device__ __forceinline__ uint32_t cell_hash(int world, int cx, int cy, int cz) {
+  uint32_t h = uint32_t(cx) * 73856093u;
+  h ^= uint32_t(cy) * 19349663u;
+  h ^= uint32_t(cz) * 83492791u;
+  h ^= uint32_t(world) * 2654435761u;
+  return mix32(h);
+}
+
+__device__ __forceinline__ int cell_coord(float x, float cell) { return __float2int_rd(x / cell); }
+
+__global__ void k_grid_count(const float4* __restrict__ pos, const int4* __restrict__ meta, const WorldDev* __restrict__ worlds,
+                             int n, uint32_t mask, int* __restrict__ cellCount, int* __restrict__ bodyBucket) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float4 p = pos[i];
+    const int w = meta[i].x;
+    const WorldDev& W = worlds[w];
+    if (p.w > W.largeR) {
+      bodyBucket[i] = -1;
+      continue;
+    }
+    uint32_t b = cell_hash(w, cell_coord(p.x, W.cell), cell_coord(p.y, W.cell), cell_coord(p.z, W.cell)) & mask;
+    bodyBucket[i] = int(b);
+    atomicAdd(&cellCount[b], 1);
+  }
+}
+
+__global__ void k_grid_scatter(const int* __restrict__ bodyBucket, int n, const int* __restrict__ cellStart,
+                               int* __restrict__ cellFill, int* __restrict__ cellBodies) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    int b = bodyBucket[i];
+    if (b < 0) continue;
+    int slot = cellStart[b] + atomicAdd(&cellFill[b], 1);
+    cellBodies[slot] = i;
+  }
+}
+
+void launch_grid_build(const BodyPtrs& b, const WorldDev* worlds, int nBodies, Grid g, void* scanTemp, cudaStream_t s) {
+  const int table = int(g.tableMask) + 1;
+  cudaMemsetAsync(g.cellCount, 0, sizeof(int) * (table + 1), s);
+  cudaMemsetAsync(g.cellFill, 0, sizeof(int) * table, s);
+  if (nBodies == 0) return;
+  k_grid_count<<<grid_blocks(nBodies, 256), 256, 0, s>>>(b.pos, b.meta, worlds, nBodies, g.tableMask, g.cellCount, g.bodyBucket); note_launches(1);
+  scan_exclusive(g.cellCount, table + 1, nullptr, scanTemp, s);
+  k_grid_scatter<<<grid_blocks(nBodies, 256), 256, 0, s>>>(g.bodyBucket, nBodies, g.cellCount, g.cellFill, g.cellBodies); note_launches(1);
+}
+
+// ------------------------------------------------------------------ pair predicate
+
+struct PairCtx {
+  const float4* __restrict__ pos;
+  const float4* __restrict__ mass;
+  const int4* __restrict__ meta;
+  NoCollide nc;
+  const int* __restrict__ jbroken;
+};
+
+__device__ __forceinline__ bool linked(const NoCollide& nc, const int* jbroken, int hi, int lo) {
+  const unsigned long long key = (unsigned long long)(uint32_t)hi << 32 | (uint32_t)lo;
+  int a = 0, b = nc.n;
+  while (a < b) {
+    int m = (a + b) >> 1;
+    if (nc.keys[m] < key) a = m + 1;
+    else b = m;
+  }
+  for (; a < nc.n && nc.keys[a] == key; a++) {
+    int j = nc.jid[a];
+    if (j < 0 || !jbroken[j]) return true;
+  }
+  return false;
+}
+
+// cpuPhysics3D.js:319-343 pair(): A = hi, B = lo
+__device__ __forceinline__ bool pair_test(const PairCtx& c, int hi, int lo, float4 pA, float mA, int4 metaA) {
+  const float4 pB = c.pos[lo];
+  const float mB = c.mass[lo].x;
+  if (mA <= 0.f && mB <= 0.f) return false;
+  const int4 metaB = c.meta[lo];
+  if (!(uint32_t(metaA.z) & uint32_t(metaB.w)) || !(uint32_t(metaB.z) & uint32_t(metaA.w))) return false;
+  const float r = pA.w + pB.w;
+  const V3 d = v3(pA) - v3(pB);
+  if (!(dot(d, d) <= r * r)) return false;
+  if (c.nc.n > 0 && linked(c.nc, c.jbroken, hi, lo)) return false;
+  return true;
+}
+
+// Enumerate the lower-index partners of body i; emit(j) for each pair (i, j).
+template <class Emit>
+__device__ __forceinline__ void for_each_partner(const PairCtx& c, const WorldDev* __restrict__ worlds, const Grid& g, int i, Emit emit) {
+  const float4 pA = c.pos[i];
+  const float mA = c.mass[i].x;
+  const int4 metaA = c.meta[i];
+  const int w = metaA.x;
+  const WorldDev W = worlds[w];
+  const bool small = !(pA.w > W.largeR);
+  if (small) {
+    const int cx = cell_coord(pA.x, W.cell), cy = cell_coord(pA.y, W.cell), cz = cell_coord(pA.z, W.cell);
+    uint32_t seen[27];
+    int nseen = 0;
+    for (int dz = -1; dz <= 1; dz++)
+      for (int dy = -1; dy <= 1; dy++)
+        for (int dx = -1; dx <= 1; dx++) {
+          uint32_t b = cell_hash(w, cx + dx, cy + dy, cz + dz) & g.tableMask;
+          bool dup = false;
+          for (int k = 0; k < nseen; k++) dup |= seen[k] == b;
+          if (dup) continue;
+          seen[nseen++] = b;
+          const int s0 = g.cellCount[b], s1 = g.cellCount[b + 1];
+          for (int s = s0; s < s1; s++) {
+            const int j = g.cellBodies[s];
+            if (j >= i || c.meta[j].x != w) continue;
+            if (pair_test(c, i, j, pA, mA, metaA)) emit(j);
+          }
+        }
+  }
+  for (int k = 0; k < W.largeCount; k++) {
+    const int L = g.large[W.largeOff + k];
+    if (L >= i) break;
+    if (pair_test(c, i, L, pA, mA, metaA)) emit(L);
+  }
+  if (!small) {
+    for (int j = W.bodyOff; j < i; j++) {
+      if (c.pos[j].w > W.largeR) continue;  // large partners came from the list above
+      if (pair_test(c, i, j, pA, mA, metaA)) emit(j);
+    }
+  }
+}
+
+__global__ void k_pair_count(PairCtx c, const WorldDev* __restrict__ worlds, Grid g, int n, int* __restrict__ pairCount) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    int cnt = 0;
+    for_each_partner(c, worlds, g, i, [&](int) { cnt++; });
+    pairCount[i] = cnt;
+  }
+}
+
+__global__ void k_pair_write(PairCtx c, const WorldDev* __restrict__ worlds, Grid g, int n, const int* __restrict__ pairStart,
+                             uint2* __restrict__ out, int capacity) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int start = pairStart[i];
+    int k = 0;
+    for_each_partner(c, worlds, g, i, [&](int j) {
+      const int slot = start + k++;
+      if (slot < capacity) out[slot] = make_uint2(uint32_t(i), uint32_t(j));
+    });
+    // insertion sort of this body's range by partner (a body has a few dozen partners at most)
+    const int end = min(start + k, capacity);
+    for (int a = start + 1; a < end; a++) {
+      const uint2 v = out[a];
+      int b = a;
+      while (b > start && out[b - 1].y > v.y) {
+        out[b] = out[b - 1];
+        b--;
+      }
+      out[b] = v;
+    }
+  }
+}
+
+__global__ void k_pair_finish(Counters* ctr, int capacity) {
+  ctr->npairs = min(ctr->pairsNeeded, capacity);
+}
+
+void launch_pairs(const BodyPtrs& b, const WorldDev* worlds, int nBodies, Grid g, NoCollide nc, const int* jbroken,
+                  int* pairCount, int* pairStart, uint2* pairsOut, int capacity, Counters* ctr, void* scanTemp,
+                  cudaStream_t s) {
+  PairCtx c{b.pos, b.mass, b.meta, nc, jbroken};
+  if (nBodies == 0) {
+    cudaMemsetAsync(&ctr->pairsNeeded, 0, sizeof(int), s);
+    k_pair_finish<<<1, 1, 0, s>>>(ctr, capacity); note_launches(1);
+    return;
+  }
+  k_pair_count<<<grid_blocks(nBodies, 128), 128, 0, s>>>(c, worlds, g, nBodies, pairCount); note_launches(1);
+  cudaMemcpyAsync(pairStart, pairCount, sizeof(int) * nBodies, cudaMemcpyDeviceToDevice, s);
+  scan_exclusive(pairStart, nBodies, &ctr->pairsNeeded, scanTemp, s);
+  k_pair_write<<<grid_blocks(nBodies, 128), 128, 0, s>>>(c, worlds, g, nBodies, pairStart, pairsOut, capacity); note_launches(1);
+  k_pair_finish<<<1, 1, 0, s>>>(ctr, capacity); note_launches(1);
+}
+
+// ------------------------------------------------------------------ box-box (collide.ts)
+
+namespace box {
+
+constexpr float SAT_EPS = 1.0e-6f;
+constexpr float PLANE_EPS = 1.0e-5f;
+constexpr float MERGE_SQ = 1.0e-6f;
+constexpr int MAX_POLY = 16;
+constexpr int AXIS_FACE_A = 0, AXIS_FACE_B = 1, AXIS_EDGE = 2;
+
+struct OBB {
+  V3 c, h, ax[3];
+};
+struct Sat {
+  int type, ia, ib;
+  float sep;
+  V3 n;
+  bool valid;
+};
+
+__device__ __forceinline__ OBB make_obb(float4 p, float4 q, float4 size) {
+  OBB o;
+  o.c = v3(p);
+  o.h = V3{size.x * 0.5f, size.y * 0.5f, size.z * 0.5f};
+  o.ax[0] = rotate(q, V3{1.f, 0.f, 0.f});
+  o.ax[1] = rotate(q, V3{0.f, 1.f, 0.f});
+  o.ax[2] = rotate(q, V3{0.f, 0.f, 1.f});
+  return o;
+}
+
+__device__ __forceinline__ float absdot(V3 a, V3 b) { return fabsf(dot(a, b)); }
+
+__device__ __forceinline__ V3 support_point(const OBB& b, V3 dir) {
+  float sx = dot(dir, b.ax[0]) >= 0 ? 1.f : -1.f;
+  float sy = dot(dir, b.ax[1]) >= 0 ? 1.f : -1.f;
+  float sz = dot(dir, b.ax[2]) >= 0 ? 1.f : -1.f;
+  V3 p = madd(b.c, b.ax[0], b.h.x * sx);
+  p = madd(p, b.ax[1], b.h.y * sy);
+  return madd(p, b.ax[2], b.h.z * sz);
+}
+
+__device__ __forceinline__ bool test_axis(const OBB& A, const OBB& B, V3 delta, V3 axis, int type, int ia, int ib, Sat& best) {
+  float l2 = len2(axis);
+  if (l2 < SAT_EPS) return true;
+  float inv = 1.f / sqrtf(l2);
+  V3 n = axis * inv;
+  if (dot(n, delta) < 0) n = -n;
+  float distance = fabsf(dot(delta, n));
+  float rA = A.h.x * absdot(n, A.ax[0]) + A.h.y * absdot(n, A.ax[1]) + A.h.z * absdot(n, A.ax[2]);
+  float rB = B.h.x * absdot(n, B.ax[0]) + B.h.y * absdot(n, B.ax[1]) + B.h.z * absdot(n, B.ax[2]);
+  float sep = distance - (rA + rB);
+  if (sep > 0) return false;
+  if (!best.valid || sep > best.sep) {
+    best.valid = true;
+    best.type = type;
+    best.ia = ia;
+    best.ib = ib;
+    best.sep = sep;
+    best.n = n;
+  }
+  return true;
+}
+
+__device__ __forceinline__ void face_axes(const OBB& b, int i, V3& u, V3& v, float& eu, float& ev) {
+  if (i == 0) { u = b.ax[1]; v = b.ax[2]; eu = b.h.y; ev = b.h.z; }
+  else if (i == 1) { u = b.ax[0]; v = b.ax[2]; eu = b.h.x; ev = b.h.z; }
+  else { u = b.ax[0]; v = b.ax[1]; eu = b.h.x; ev = b.h.y; }
+}
+
+__device__ __forceinline__ int clip_polygon(const V3* in, int nin, V3* out, V3 n, float off) {
+  int nout = 0;
+  if (nin == 0) return 0;
+  V3 a = in[nin - 1];
+  float da = dot(n, a) - off;
+  for (int k = 0; k < nin; k++) {
+    V3 b = in[k];
+    float db = dot(n, b) - off;
+    bool aIn = da <= PLANE_EPS, bIn = db <= PLANE_EPS;
+    if (aIn != bIn) {
+      float t = 0.f;
+      float denom = da - db;
+      if (fabsf(denom) > SAT_EPS) t = clampr(da / denom, 0.f, 1.f);
+      if (nout < MAX_POLY) out[nout++] = madd(a, b - a, t);
+    }
+    if (bIn && nout < MAX_POLY) out[nout++] = b;
+    a = b;
+    da = db;
+  }
+  return nout;
+}
+
+// ContactBuilder: merges near-duplicate midpoints, at most 8 contacts, anchors body-local.
+struct Builder {
+  V3 mids[MAX_CONTACTS];
+  int n;
+  float4 pA, qA, pB, qB;
+  uint32_t* feat;
+  V3* rA;
+  V3* rB;
+  __device__ __forceinline__ void add(V3 xA, V3 xB, uint32_t feature) {
+    V3 mid = (xA + xB) * 0.5f;
+    for (int k = 0; k < n; k++)
+      if (len2(mid - mids[k]) < MERGE_SQ) return;
+    if (n >= MAX_CONTACTS) return;
+    feat[n] = feature;
+    rA[n] = rotateInv(qA, xA - v3(pA));
+    rB[n] = rotateInv(qB, xB - v3(pB));
+    mids[n] = mid;
+    n++;
+  }
+};
+
+__device__ __forceinline__ void support_edge(const OBB& b, int i, V3 dir, V3& e0, V3& e1) {
+  int a1 = (i + 1) % 3, a2 = (i + 2) % 3;
+  float s1 = dot(dir, b.ax[a1]) >= 0 ? 1.f : -1.f;
+  float s2 = dot(dir, b.ax[a2]) >= 0 ? 1.f : -1.f;
+  V3 c = madd(b.c, b.ax[a1], comp(b.h, a1) * s1);
+  c = madd(c, b.ax[a2], comp(b.h, a2) * s2);
+  V3 e = b.ax[i] * comp(b.h, i);
+  e0 = c - e;
+  e1 = c + e;
+}
+
+__device__ __forceinline__ void closest_segments(V3 p0, V3 p1, V3 q0, V3 q1, V3& xA, V3& xB) {
+  V3 d1 = p1 - p0, d2 = q1 - q0, r = p0 - q0;
+  float a = dot(d1, d1), e = dot(d2, d2), f = dot(d2, r);
+  float s = 0.f, t = 0.f;
+  if (a <= SAT_EPS && e <= SAT_EPS) {
+    xA = p0;
+    xB = q0;
+    return;
+  }
+  if (a <= SAT_EPS) {
+    t = clampr(f / e, 0.f, 1.f);
+  } else {
+    float c = dot(d1, r);
+    if (e <= SAT_EPS) {
+      s = clampr(-c / a, 0.f, 1.f);
+    } else {
+      float b = dot(d1, d2);
+      float denom = a * e - b * b;
+      if (fabsf(denom) > SAT_EPS) s = clampr((b * f - c * e) / denom, 0.f, 1.f);
+      t = (b * s + f) / e;
+      if (t < 0) {
+        t = 0.f;
+        s = clampr(-c / a, 0.f, 1.f);
+      } else if (t > 1) {
+        t = 1.f;
+        s = clampr((b - c) / a, 0.f, 1.f);
+      }
+    }
+  }
+  xA = madd(p0, d1, s);
+  xB = madd(q0, d2, t);
+}
+
+__device__ void face_manifold(Builder& bld, const OBB& A, const OBB& B, bool refIsA, int refAxis, V3 nAB) {
+  const OBB& R = refIsA ? A : B;
+  const OBB& I = refIsA ? B : A;
+  V3 refOut = refIsA ? nAB : -nAB;
+  float sgn = dot(refOut, R.ax[refAxis]) >= 0 ? 1.f : -1.f;
+  V3 rn = R.ax[refAxis] * sgn;
+  V3 rc = madd(R.c, rn, comp(R.h, refAxis));
+  V3 ru, rv;
+  float reu, rev;
+  face_axes(R, refAxis, ru, rv, reu, rev);
+  // incident face: most anti-parallel axis of the other box
+  int incAxis = 0;
+  float best = -FLT_MAX;
+  for (int k = 0; k < 3; k++) {
+    float d = absdot(I.ax[k], rn);
+    if (d > best) {
+      best = d;
+      incAxis = k;
+    }
+  }
+  float isg = dot(I.ax[incAxis], rn) > 0 ? -1.f : 1.f;
+  V3 fn = I.ax[incAxis] * isg;
+  V3 fc = madd(I.c, fn, comp(I.h, incAxis));
+  V3 iu, iv;
+  float ieu, iev;
+  face_axes(I, incAxis, iu, iv, ieu, iev);
+  V3 bufA[MAX_POLY], bufB[MAX_POLY];
+  bufA[0] = madd(madd(fc, iu, 1.f * ieu), iv, 1.f * iev);
+  bufA[1] = madd(madd(fc, iu, -1.f * ieu), iv, 1.f * iev);
+  bufA[2] = madd(madd(fc, iu, -1.f * ieu), iv, -1.f * iev);
+  bufA[3] = madd(madd(fc, iu, 1.f * ieu), iv, -1.f * iev);
+  int np = 4;
+  V3 planes[4] = {ru, -ru, rv, -rv};
+  float ext[4] = {reu, reu, rev, rev};
+  V3* in = bufA;
+  V3* out = bufB;
+  for (int k = 0; k < 4; k++) {
+    np = clip_polygon(in, np, out, planes[k], dot(planes[k], rc) + ext[k]);
+    if (np == 0) return;
+    V3* t = in;
+    in = out;
+    out = t;
+  }
+  const uint32_t prefix = (uint32_t(refIsA ? AXIS_FACE_A : AXIS_FACE_B) << 24) | (uint32_t(refAxis & 0xff) << 16) |
+                          (uint32_t(incAxis & 0xff) << 8);
+  for (int k = 0; k < np && bld.n < MAX_CONTACTS; k++) {
+    V3 pI = in[k];
+    float distance = dot(pI - rc, rn);
+    if (distance > PLANE_EPS) continue;
+    V3 pR = madd(pI, rn, -distance);
+    if (refIsA) bld.add(pR, pI, prefix | uint32_t(k & 0xff));
+    else bld.add(pI, pR, prefix | uint32_t(k & 0xff));
+  }
+  if (bld.n == 0) bld.add(support_point(A, nAB), support_point(B, -nAB), prefix);
+}
+
+__device__ void edge_contact(Builder& bld, const OBB& A, const OBB& B, int axA, int axB, V3 nAB) {
+  V3 a0, a1, b0, b1, xA, xB;
+  support_edge(A, axA, nAB, a0, a1);
+  support_edge(B, axB, -nAB, b0, b1);
+  closest_segments(a0, a1, b0, b1, xA, xB);
+  const uint32_t key = (uint32_t(AXIS_EDGE) << 24) | (uint32_t(axA & 0xff) << 8) | uint32_t(axB & 0xff);
+  bld.add(xA, xB, key);
+  if (bld.n == 0) bld.add(support_point(A, nAB), support_point(B, -nAB), key);
+}
+
+// Returns the contact count (0: separated); basis rows n (B to A), t1, t2.
+__device__ int collide(Builder& bld, float4 pA, float4 qA, float4 sA, float4 pB, float4 qB, float4 sB, bool faceBias, M33& basis) {
+  OBB A = make_obb(pA, qA, sA), B = make_obb(pB, qB, sB);
+  V3 delta = B.c - A.c;
+  Sat bf{AXIS_FACE_A, 0, 0, -FLT_MAX, V3{0, 0, 0}, false};
+  Sat be{AXIS_EDGE, 0, 0, -FLT_MAX, V3{0, 0, 0}, false};
+  for (int i = 0; i < 3; i++)
+    if (!test_axis(A, B, delta, A.ax[i], AXIS_FACE_A, i, -1, bf)) return 0;
+  for (int i = 0; i < 3; i++)
+    if (!test_axis(A, B, delta, B.ax[i], AXIS_FACE_B, -1, i, bf)) return 0;
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++)
+      if (!test_axis(A, B, delta, cross(A.ax[i], B.ax[j]), AXIS_EDGE, i, j, be)) return 0;
+  if (!bf.valid) return 0;
+  Sat best = bf;
+  if (be.valid) {
+    const float rel = 0.95f, absT = 0.01f;
+    bool edgeWins = !faceBias ? rel * be.sep > bf.sep + absT : be.sep > rel * bf.sep + absT;
+    if (edgeWins) best = be;
+  }
+  basis = orthonormal(-best.n);
+  if (best.type == AXIS_EDGE) edge_contact(bld, A, B, best.ia, best.ib, best.n);
+  else if (best.type == AXIS_FACE_A) face_manifold(bld, A, B, true, best.ia, best.n);
+  else face_manifold(bld, A, B, false, best.ib, best.n);
+  return bld.n;
+}
+
+}  // namespace box
+
+// ------------------------------------------------------------------ generic (cpuContacts3D.js)
+
+namespace gen {
+
+// Box faces (vertex indices) and outward normals, cpuContacts3D.js:26-41; vertex i has local
+// coordinate size/2 * (bit k of i ? +1 : -1) on axis k.
+__constant__ int kFaces[6][4] = {{1, 3, 7, 5}, {0, 4, 6, 2}, {2, 6, 7, 3}, {0, 1, 5, 4}, {4, 5, 7, 6}, {0, 2, 3, 1}};
+__constant__ float kNormals[6][3] = {{1, 0, 0}, {-1, 0, 0}, {0, 1, 0}, {0, -1, 0}, {0, 0, 1}, {0, 0, -1}};
+// Unique edges in the order geometry3D discovers them walking the faces (cpuContacts3D.js:73-86).
+__constant__ int kEdges[12][2] = {{1, 3}, {3, 7}, {7, 5}, {5, 1}, {0, 4}, {4, 6}, {6, 2}, {2, 0}, {6, 7}, {3, 2}, {0, 1}, {5, 4}};
+
+struct BoxGeo {
+  V3 v[8];
+  V3 n[6];
+};
+
+__device__ __forceinline__ float hyp(V3 a) { return sqrtf(a.x * a.x + a.y * a.y + a.z * a.z); }
+__device__ __forceinline__ V3 unitv(V3 a) {
+  float h = hyp(a);
+  float s = 1.f / (h != 0.f ? h : 1.f);
+  return a * s;
+}
+
+__device__ __forceinline__ void box_geo(BoxGeo& g, float4 p, float4 q, float4 size) {
+  const V3 c = v3(p);
+  for (int i = 0; i < 8; i++) {
+    V3 l{(size.x / 2) * ((i & 1) ? 1.f : -1.f), (size.y / 2) * ((i & 2) ? 1.f : -1.f), (size.z / 2) * ((i & 4) ? 1.f : -1.f)};
+    g.v[i] = c + rotate(q, l);
+  }
+  for (int f = 0; f < 6; f++) g.n[f] = rotate(q, V3{kNormals[f][0], kNormals[f][1], kNormals[f][2]});
+}
+
+__device__ __forceinline__ V3 box_support(const BoxGeo& g, V3 n) {
+  int best = 0;
+  for (int i = 0; i < 8; i++)
+    if (dot(g.v[i], n) > dot(g.v[best], n)) best = i;
+  return g.v[best];
+}
+
+// support of a sphere (both spine points coincide): first of the two, pushed out by r
+__device__ __forceinline__ V3 sphere_support(V3 c, float r, V3 n) { return madd(c, n, r); }
+
+__device__ __forceinline__ void closest_seg(V3 p, V3 q, V3 r, V3 s, V3& oa, V3& ob) {
+  V3 d1 = q - p, d2 = s - r, w = p - r;
+  float a = dot(d1, d1), e = dot(d2, d2), f = dot(d2, w);
+  float u = 0.f, v = 0.f;
+  if (a < 1e-16f) v = e > 1e-16f ? fmaxf(0.f, fminf(1.f, f / e)) : 0.f;
+  else {
+    float c = dot(d1, w);
+    if (e < 1e-16f) u = fmaxf(0.f, fminf(1.f, -c / a));
+    else {
+      float b = dot(d1, d2), den = a * e - b * b;
+      u = den > 1e-12f * a * e ? fmaxf(0.f, fminf(1.f, (b * f - c * e) / den)) : 0.f;
+      v = (b * u + f) / e;
+      if (v < 0) {
+        v = 0.f;
+        u = fmaxf(0.f, fminf(1.f, -c / a));
+      } else if (v > 1) {
+        v = 1.f;
+        u = fmaxf(0.f, fminf(1.f, (b - c) / a));
+      }
+    }
+  }
+  oa = madd(p, d1, u);
+  ob = madd(r, d2, v);
+}
+
+__device__ __forceinline__ V3 closest_triangle(V3 p, V3 a, V3 b, V3 c) {
+  V3 ab = b - a, ac = c - a, ap = p - a;
+  float d1 = dot(ab, ap), d2 = dot(ac, ap);
+  if (d1 <= 0 && d2 <= 0) return a;
+  V3 bp = p - b;
+  float d3 = dot(ab, bp), d4 = dot(ac, bp);
+  if (d3 >= 0 && d4 <= d3) return b;
+  float vc = d1 * d4 - d3 * d2;
+  if (vc <= 0 && d1 >= 0 && d3 <= 0) return madd(a, ab, d1 / (d1 - d3));
+  V3 cp = p - c;
+  float d5 = dot(ab, cp), d6 = dot(ac, cp);
+  if (d6 >= 0 && d5 <= d6) return c;
+  float vb = d5 * d2 - d1 * d6;
+  if (vb <= 0 && d2 >= 0 && d6 <= 0) return madd(a, ac, d2 / (d2 - d6));
+  float va = d3 * d6 - d5 * d4;
+  if (va <= 0 && d4 - d3 >= 0 && d5 - d6 >= 0) return madd(b, c - b, (d4 - d3) / (d4 - d3 + d5 - d6));
+  float den = 1.f / (va + vb + vc);
+  return a + (ab * (vb * den) + ac * (vc * den));
+}
+
+__device__ __forceinline__ V3 closest_surface(const BoxGeo& g, V3 p) {
+  float dist = INFINITY;
+  V3 best = p;
+  for (int f = 0; f < 6; f++)
+    for (int i = 1; i < 3; i++) {
+      V3 q = closest_triangle(p, g.v[kFaces[f][0]], g.v[kFaces[f][i]], g.v[kFaces[f][i + 1]]);
+      V3 d = p - q;
+      float dd = dot(d, d);
+      if (dd < dist) {
+        best = q;
+        dist = dd;
+      }
+    }
+  return best;
+}
+
+// At least one body is a sphere. Returns the contact count (0 or 1).
+__device__ int collide(float4 pA, float4 qA, float4 sA, int shA, float4 pB, float4 qB, float4 sB, int shB, M33& basis,
+                       V3& rA, V3& rB) {
+  const bool roundA = shA == SHAPE_SPHERE, roundB = shB == SHAPE_SPHERE;
+  BoxGeo box;
+  const V3 cA = v3(pA), cB = v3(pB);
+  // a sphere's spine is its centre (rotate of a zero offset adds +-0)
+  const V3 spA = cA + rotate(qA, V3{0.f, 0.f, 0.f});
+  const V3 spB = cB + rotate(qB, V3{0.f, 0.f, 0.f});
+  const float radA = sA.x / 2, radB = sB.x / 2;
+  if (!roundA) box_geo(box, pA, qA, sA);
+  else if (!roundB) box_geo(box, pB, qB, sB);
+  float gap = -INFINITY;
+  V3 n{0.f, 0.f, 1.f};
+  auto supA = [&](V3 d) { return roundA ? sphere_support(spA, radA, d) : box_support(box, d); };
+  auto supB = [&](V3 d) { return roundB ? sphere_support(spB, radB, d) : box_support(box, d); };
+  auto consider = [&](V3 axis) {
+    if (hyp(axis) < 1e-9f) return;
+    V3 v = unitv(axis);
+    V3 nv = v * -1.f;
+    float g = dot(supA(nv) - supB(v), v);
+    float rev = dot(supB(nv) - supA(v), v);
+    if (rev > g) {
+      g = rev;
+      v = v * -1.f;
+    }
+    if (g > gap + 1e-7f) {
+      gap = g;
+      n = v;
+    }
+  };
+  if (!roundA)
+    for (int f = 0; f < 6; f++) consider(box.n[f]);
+  if (!roundB)
+    for (int f = 0; f < 6; f++) consider(box.n[f]);
+  if (roundA && roundB) {
+    V3 pa, pb;
+    closest_seg(spA, spA, spB, spB, pa, pb);
+    consider(pa - pb);
+  }
+  // [round, poly] = [A, B] then [B, A]
+  for (int k = 0; k < 2; k++) {
+    const bool roundIsA = k == 0;
+    const bool isRound = roundIsA ? roundA : roundB;
+    const bool polyIsBox = roundIsA ? !roundB : !roundA;
+    if (!isRound || !polyIsBox) continue;
+    const V3 sp = roundIsA ? spA : spB;
+    for (int i = 0; i < 8; i++) {
+      // nearest(spine0, spine1, v) on a degenerate spine is spine0
+      V3 e = sp - sp;
+      V3 ap = box.v[i] - sp;
+      float ee = dot(e, e);
+      float t = dot(ap, e) / (ee != 0.f ? ee : 1.f);
+      t = fmaxf(0.f, fminf(1.f, t));
+      consider(box.v[i] - madd(sp, e, t));
+    }
+    for (int i = 0; i < 12; i++) {
+      V3 pa, pb;
+      closest_seg(sp, sp, box.v[kEdges[i][0]], box.v[kEdges[i][1]], pa, pb);
+      consider(pa - pb);
+    }
+  }
+  if (gap == -INFINITY) consider(cA - cB);
+  if (gap > 0) return 0;
+  if (gap == -INFINITY) n = V3{0.f, 0.f, 1.f};
+  V3 axisT = fabsf(n.x) < 0.7f ? V3{1.f, 0.f, 0.f} : V3{0.f, 1.f, 0.f};
+  V3 tangent = unitv(cross(n, axisT));
+  basis = M33{n, tangent, cross(n, tangent)};
+  V3 xa, xb;
+  if (roundA && roundB) {
+    V3 pa, pb;
+    closest_seg(spA, spA, spB, spB, pa, pb);
+    xa = madd(pa, n, -radA);
+    xb = madd(pb, n, radB);
+  } else if (roundA) {
+    xa = sphere_support(spA, radA, n * -1.f);
+    xb = closest_surface(box, xa);
+  } else {
+    xb = sphere_support(spB, radB, n);
+    xa = closest_surface(box, xb);
+  }
+  rA = rotateInv(qA, xa - cA);
+  rB = rotateInv(qB, xb - cB);
+  return 1;
+}
+
+}  // namespace gen
+
+// ------------------------------------------------------------------ narrowphase kernel
+
+__device__ __forceinline__ int find_pair(const uint2* __restrict__ pairs, int n, uint2 key) {
+  const unsigned long long k = (unsigned long long)key.x << 32 | key.y;
+  int a = 0, b = n;
+  while (a < b) {
+    int m = (a + b) >> 1;
+    uint2 p = pairs[m];
+    unsigned long long pk = (unsigned long long)p.x << 32 | p.y;
+    if (pk < k) a = m + 1;
+    else b = m;
+  }
+  if (a < n) {
+    uint2 p = pairs[a];
+    if (p.x == key.x && p.y == key.y) return a;
+  }
+  return -1;
+}
+
+__global__ void __launch_bounds__(128) k_narrowphase(BodyPtrs bd, const WorldDev* __restrict__ worlds, PairPtrs cur, PairPtrs prev,
+                                                     const int* __restrict__ prevN, const int* __restrict__ curN, int capacity) {
+  const int np = min(*curN, capacity);
+  const int nprev = prev.pair ? min(*prevN, capacity) : 0;
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
+    const uint2 key = cur.pair[p];
+    const int a = int(key.x), b = int(key.y);
+    const float4 pA = bd.pos[a], qA = bd.rot[a], sA = bd.size[a];
+    const float4 pB = bd.pos[b], qB = bd.rot[b], sB = bd.size[b];
+    const int shA = bd.meta[a].y, shB = bd.meta[b].y;
+    const WorldDev W = worlds[bd.meta[a].x];
+    M33 basis{V3{0, 0, 0}, V3{0, 0, 0}, V3{0, 0, 0}};
+    uint32_t feat[MAX_CONTACTS];
+    V3 rA[MAX_CONTACTS], rB[MAX_CONTACTS];
+    int n;
+    const bool rolling = shA == SHAPE_SPHERE || shB == SHAPE_SPHERE;
+    if (!rolling) {
+      box::Builder bld;
+      bld.n = 0;
+      bld.pA = pA; bld.qA = qA; bld.pB = pB; bld.qB = qB;
+      bld.feat = feat; bld.rA = rA; bld.rB = rB;
+      n = box::collide(bld, pA, qA, sA, pB, qB, sB, (W.flags & FLAG_FACE_BIAS) != 0, basis);
+    } else {
+      n = gen::collide(pA, qA, sA, shA, pB, qB, sB, shB, basis, rA[0], rB[0]);
+      feat[0] = 1u;  // feature i + 1
+    }
+    const float friction = sqrtf(sA.w * sB.w);
+    cur.count[p] = n;
+    cur.basis[3 * p + 0] = f4(basis.r0, friction);
+    cur.basis[3 * p + 1] = f4(basis.r1, 0.f);
+    cur.basis[3 * p + 2] = f4(basis.r2, 0.f);
+    if (n == 0) continue;
+    // warm start from last step's manifold of this pair (cpuPhysics3D.js:108-145)
+    const int pp = nprev > 0 ? find_pair(prev.pair, nprev, key) : -1;
+    const int pn = pp >= 0 ? prev.count[pp] : 0;
+    const float ag = W.alpha * W.gamma;
+    float penFloor = 0.f;
+    if (W.flags & FLAG_MASS_PENALTY) {
+      const float mA = bd.mass[a].x, mB = bd.mass[b].x;
+      const float mass = fminr(mA > 0.f ? mA : INFINITY, mB > 0.f ? mB : INFINITY);
+      penFloor = fmaxf(PENALTY_MIN, fminf(PENALTY_MAX, mass / (W.dt * W.dt)));
+    }
+    for (int k = 0; k < n; k++) {
+      V3 ra = rA[k], rb = rB[k];
+      V3 pen{0.f, 0.f, 0.f}, lam{0.f, 0.f, 0.f};
+      bool stick = false;
+      for (int q = 0; q < pn; q++) {
+        const float4* o = prev.ct + (size_t(pp) * MAX_CONTACTS + q) * 4;
+        const float4 o0 = o[0];
+        const uint32_t of = __float_as_uint(o0.w);
+        if ((of & ~STICK_BIT) != feat[k]) continue;
+        const float4 o1 = o[1], o2 = o[2], o3 = o[3];
+        stick = (of & STICK_BIT) != 0;
+        if (stick && !rolling) {
+          ra = v3(o0);
+          rb = v3(o1);
+        }
+        pen = v3(o2);
+        lam = v3(o3);
+        break;
+      }
+      // C0 = basis (world(a, rA) - world(b, rB)) + margin on the normal row
+      const V3 d = xform(v3(pA), qA, ra) - xform(v3(pB), qB, rb);
+      V3 C0 = mulv(basis, d);
+      C0.x += COLLISION_MARGIN;
+      lam = V3{lam.x * ag, lam.y * ag, lam.z * ag};
+      pen = V3{clampr(pen.x * W.gamma, PENALTY_MIN, PENALTY_MAX), clampr(pen.y * W.gamma, PENALTY_MIN, PENALTY_MAX),
+               clampr(pen.z * W.gamma, PENALTY_MIN, PENALTY_MAX)};
+      if (W.flags & FLAG_MASS_PENALTY) pen.x = fmaxf(pen.x, penFloor);
+      float4* o = cur.ct + (size_t(p) * MAX_CONTACTS + k) * 4;
+      o[0] = f4(ra, __uint_as_float(feat[k] | (stick ? STICK_BIT : 0u)));
+      o[1] = f4(rb, C0.x);
+      o[2] = f4(pen, C0.y);
+      o[3] = f4(lam, C0.z);
+    }
+  }
+}
+
+void launch_narrowphase(const BodyPtrs& b, const WorldDev* worlds, PairPtrs cur, PairPtrs prev, const int* prevN,
+                        const int* curN, int capacity, Counters* ctr, cudaStream_t s) {
+  (void)ctr;
+  // grid sized for the capacity; threads past the live pair count exit at once
+  int blocks = grid_blocks(capacity, 128);
+  if (blocks > 152 * 32) blocks = 152 * 32;
+  k_narrowphase<<<blocks, 128, 0, s>>>(b, worlds, cur, prev, prevN, curN, capacity); note_launches(1);
+}
+
+}  // namespace avbd

@@ -1,0 +1,328 @@
+#!/usr/bin/env python
+"""Benchmark: body-steps/s of the batched AVBD engine on the 4,096-world mix, beside the plain
+one-world-per-launch-sequence path and the CPU path.
+
+Workload (default ``world_mix``): 4,096 independent box/sphere piles with log-normal body counts
+(median 256, clipped to [16, 8192], ~2.1 M bodies in total), dt 1/60 s, 10 iterations, FP32 state.
+One benchmark step advances every world by one solver step (one launch sequence over all worlds).
+Inputs (2.1 M bodies, tens of millions of contacts) far exceed the 129 MB L2, so no L2 flush is
+needed between steps.
+
+Reported: ``value`` (device-resident, CUDA events on the engine's stream), ``e2e`` (through the
+public API with a host-side velocity-command upload and a full pose readback every step),
+per-step latency percentiles, the plain path on a sample of the worlds, the dominant kernel's
+roofline against the measured HBM copy bandwidth, and the CPU oracle on a bounded sample.
+
+``--impl reference`` times the reference's CPU path (the oracle restatement: the reference is
+JavaScript and cannot run here) on a bounded sample of the same workload with all host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path[:0] = [os.path.join(ROOT, "babylon-avbd_gb300"), os.path.join(ROOT, "oracle")]
+
+import numpy as np  # noqa: E402
+
+METRIC = "body-steps/s and p99 tick latency: batched/served vs plain GPU path at 1e-5 tol"
+UNIT = "body-steps/s"
+
+
+def args_parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--workload", choices=["world_mix", "box_pile"], default="world_mix")
+    p.add_argument("--worlds", type=int, default=4096)
+    p.add_argument("--plain-sample", type=int, default=128, help="worlds timed on the plain path")
+    p.add_argument("--cpu-sample", type=int, default=64, help="worlds timed on the CPU path")
+    p.add_argument("--cpu-seconds", type=float, default=15.0)
+    p.add_argument("--no-e2e", action="store_true")
+    return p.parse_args()
+
+
+# ------------------------------------------------------------------ distributed plumbing
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as td
+            td.init_process_group("gloo")
+            self.td = td
+
+    def barrier(self):
+        if self.world > 1:
+            self.td.barrier()
+
+    def max(self, v: float) -> float:
+        if self.world == 1:
+            return v
+        import torch
+        t = torch.tensor([v], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, v: float) -> float:
+        if self.world == 1:
+            return v
+        import torch
+        t = torch.tensor([v], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.SUM)
+        return float(t.item())
+
+
+# ------------------------------------------------------------------ clocks
+class Clocks:
+    """nvidia-smi samples every 200 ms during the timed region."""
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=clocks.sm,clocks.max.sm,power.draw,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx = float(f[1])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[3:7]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ workloads
+def build_worlds(args, rank):
+    from avbd_gb300 import workloads
+    if args.workload == "box_pile":
+        return [workloads.box_pile_c0()], {"workload": "box_pile_c0", "bodies": 1001}
+    seed = workloads.SEED_BASE + 3 + 1000 * rank
+    worlds, counts, sigma = workloads.world_mix(args.worlds, target=int(2_100_000 * args.worlds / 4096), seed=seed)
+    cfg = {"workload": f"world_mix_{args.worlds}", "worlds": args.worlds, "bodies": int(counts.sum() + len(counts)),
+           "count_median": 256, "count_clip": [16, 8192], "lognormal_sigma": round(float(sigma), 4),
+           "seed": seed, "iterations": 10, "dt": "1/60", "shapes": "70% boxes, 30% spheres",
+           "l2": "inputs larger than L2 (no flush needed)"}
+    return worlds, cfg
+
+
+def sample_worlds(worlds, k):
+    idx = np.linspace(0, len(worlds) - 1, min(k, len(worlds))).round().astype(int)
+    return [worlds[i] for i in sorted(set(idx.tolist()))]
+
+
+def cpu_baseline(worlds, warm, steps, seconds, threads=0):
+    """The oracle (FP64, reference sequential order) on a bounded sample, OpenMP over worlds."""
+    import oracle
+    ws = [oracle.OracleWorld(w, fp64=True, app=True, colored=False) for w in worlds]
+    if warm:
+        oracle.step_parallel(ws, warm, threads)
+    bodies = sum(w.n_bodies for w in worlds)
+    done, t0 = 0, time.perf_counter()
+    used = 1
+    while done < steps:
+        used = oracle.step_parallel(ws, 1, threads)
+        done += 1
+        if time.perf_counter() - t0 > seconds:
+            break
+    el = time.perf_counter() - t0
+    return {"value": bodies * done / el, "unit": UNIT, "cores": used, "kind": "port",
+            "sample": f"{len(worlds)} worlds ({bodies} bodies) x {done} steps after {warm} warm-up steps, "
+                      f"FP64 oracle in the reference's sequential order, {el:.1f} s"}
+
+
+def load_peaks():
+    try:
+        d = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def load_traffic():
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    try:
+        return json.load(open(p))
+    except Exception:
+        return {}
+
+
+# ------------------------------------------------------------------ arms
+def run_reference(args, dist):
+    if dist.rank != 0:
+        return
+    worlds, cfg = build_worlds(args, 0)
+    sample = sample_worlds(worlds, args.cpu_sample)
+    cb = cpu_baseline(sample, args.warmup, args.steps, args.cpu_seconds)
+    line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg, "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, dist):
+    import torch
+    from avbd_gb300 import createSolverPipeline
+
+    dev = dist.local
+    torch.cuda.set_device(dev)
+    worlds, cfg = build_worlds(args, dist.rank)
+    pipe = createSolverPipeline("gb300", device=dev)
+    stream = torch.cuda.ExternalStream(pipe.stream, device=dev)
+    batch = pipe.createBatch(worlds)
+    nb = batch.bodyCount
+    for _ in range(args.warmup):
+        batch.step(1)
+    pipe.synchronize()
+    # ---------------- timed region (device-resident)
+    batch.profile(True)
+    launches0 = batch.profileRead()["launches"]
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    dist.barrier()
+    pipe.synchronize()
+    torch.cuda.synchronize()
+    with Clocks(dev) as clk:
+        ev[0].record(stream)
+        for k in range(args.steps):
+            batch.step(1)
+            ev[k + 1].record(stream)
+        pipe.synchronize()
+        torch.cuda.synchronize()
+    ticks = np.array([ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)])
+    elapsed_ms = float(ev[0].elapsed_time(ev[-1]))
+    prof = batch.profileRead()
+    batch.profile(False)
+    elapsed_ms = dist.max(elapsed_ms)
+    total_bodies = dist.sum(float(nb))
+    value = total_bodies * args.steps / (elapsed_ms / 1000.0)
+    launches = prof["launches"] - launches0
+    # ---------------- roofline of the dominant kernel class
+    peak, peak_kind = load_peaks()
+    classes = {"primal": (prof["ms_primal"], prof["bytes_primal"], "k_primal"),
+               "dual": (prof["ms_dual"], prof["bytes_dual"], "k_dual_pairs"),
+               "collide": (prof["ms_collide"], prof["bytes_collide"], "collision kernels")}
+    dom = max(classes, key=lambda k: classes[k][0])
+    ms, byts, kname = classes[dom]
+    achieved = byts / (ms / 1000.0) / 1e9 if ms > 0 else 0.0
+    traffic = load_traffic().get(dom)
+    roof = {"kernel": kname, "bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
+            "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+            "traffic": traffic, "algorithmic_bytes_per_step": byts / max(prof["steps"], 1),
+            "launches_per_step": (prof["primal_launches"] / max(prof["steps"], 1)) if dom == "primal" else None}
+    breakdown = {k: round(v[0] / max(prof["steps"], 1), 3) for k, v in classes.items()}
+    breakdown["topology"] = round(prof["ms_topology"] / max(prof["steps"], 1), 3)
+    breakdown["other"] = round(prof["ms_other"] / max(prof["steps"], 1), 3)
+    # ---------------- e2e through the public API with host buffers
+    e2e = None
+    if not args.no_e2e:
+        offs = np.cumsum([0] + batch.bodyCounts[:-1])
+        # one command per world: kick its last body (world offset + count - 1) upwards
+        idx_host = torch.from_numpy((offs + np.array(batch.bodyCounts) - 1).astype(np.int64)).pin_memory()
+        vel_host = torch.zeros((len(offs), 3), dtype=torch.float32).pin_memory()
+        vel_host[:, 1] = 0.5
+        poses_host = torch.empty((nb, 8), dtype=torch.float32).pin_memory()
+        idx_np, vel_np, poses_np = idx_host.numpy(), vel_host.numpy(), poses_host.numpy()
+        dist.barrier()
+        pipe.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            batch.setVelocities(idx_np, linear=vel_np)
+            batch.step(1)
+            batch.readPoses(poses_np)
+        el = time.perf_counter() - t0
+        el = dist.max(el)
+        e2e = {"value": total_bodies * args.steps / el, "unit": UNIT,
+               "h2d_bytes_per_step": int(idx_np.size * 4 + vel_np.nbytes),
+               "d2h_bytes_per_step": int(poses_np.nbytes)}
+    # ---------------- plain path and CPU baseline (rank 0)
+    plain = cpu = None
+    if dist.rank == 0:
+        sample = sample_worlds(worlds, args.plain_sample)
+        plain_worlds = [pipe.createSolver(w) for w in sample]
+        for w in plain_worlds:
+            w.step(args.warmup)
+        pipe.synchronize()
+        psteps = max(2, min(args.steps, 5))
+        t0 = time.perf_counter()
+        for _ in range(psteps):
+            for w in plain_worlds:
+                w.step(1)
+        pipe.synchronize()
+        el = time.perf_counter() - t0
+        pb = sum(w.bodyCount for w in plain_worlds)
+        plain = {"value": pb * psteps / el, "unit": UNIT,
+                 "sample": f"{len(plain_worlds)} of {len(worlds)} worlds ({pb} bodies), each stepped in its own "
+                           f"launch sequence, {psteps} steps after {args.warmup} warm-up steps"}
+        for w in plain_worlds:
+            w.destroy()
+        cpu = cpu_baseline(sample_worlds(worlds, args.cpu_sample), args.warmup, args.steps, args.cpu_seconds)
+    pipe.destroy()
+    if dist.rank != 0:
+        return
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": cfg,
+            "tick_ms": {"p50": round(float(np.percentile(ticks, 50)), 3), "p95": round(float(np.percentile(ticks, 95)), 3),
+                        "p99": round(float(np.percentile(ticks, 99)), 3)},
+            "plain_gpu": plain, "stage_ms_per_step": breakdown, "roofline": roof, "cpu_baseline": cpu,
+            "e2e": e2e, "gpu_launches": int(launches), "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = args_parse()
+    dist = Dist()
+    if args.impl == "reference":
+        run_reference(args, dist)
+    else:
+        run_ours(args, dist)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,202 @@
+/*
+ * avbd_gb300 -- C ABI of the GB300 (sm_103a) AVBD rigid-body engine.
+ *
+ * This is the boundary a host binding (the reference's Node world API through an N-API addon,
+ * or Python ctypes) calls. Plain C types only: pointers, sizes, status codes. Every function
+ * returns 0 on success or a negative AVBD_E_* code; avbd_last_error() then describes the
+ * failure (thread-local string). No C++ exception crosses this boundary. Caller buffers are
+ * borrowed for the duration of the call only. One host thread per context (or external
+ * locking).
+ *
+ * Each entry point names the reference interface it replaces (paths in joshbrew/babylon-avbd).
+ */
+#ifndef AVBD_GB300_H
+#define AVBD_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define AVBD_OK 0
+#define AVBD_E_INVALID (-1)   /* bad argument (validated before any work is queued) */
+#define AVBD_E_CUDA (-2)      /* CUDA runtime error */
+#define AVBD_E_NOMEM (-3)     /* device or host allocation failed / over budget */
+#define AVBD_E_STATE (-4)     /* call not valid in the object's current state */
+#define AVBD_E_CAPACITY (-5)  /* a fixed capacity was exceeded */
+
+typedef struct avbd_ctx avbd_ctx;
+typedef struct avbd_world avbd_world;
+typedef struct avbd_batch avbd_batch;
+
+/* Shapes and constraint kinds (src/native/scenes.js addBox/addSphere, addJoint/addSpring). */
+#define AVBD_SHAPE_BOX 0
+#define AVBD_SHAPE_SPHERE 1
+#define AVBD_CONS_JOINT 0
+#define AVBD_CONS_SPRING 1
+#define AVBD_CONS_IGNORE 2
+
+/* Solver parameters: reference/three-avbd/src/avbd3d/ref/solver.ts:347-359 and
+ * src/native/cpu/cpuSolver3D.ts:46-79 (massPenalty, faceBias, up). */
+typedef struct avbd_params {
+  float dt;
+  float gravity;
+  float up[3];
+  int32_t iterations;
+  float alpha;
+  float beta_lin;
+  float beta_ang;
+  float gamma;
+  int32_t mass_penalty; /* contact normal penalty floor min(mA, mB)/dt^2 */
+  int32_t face_bias;    /* prefer face axes in box-box SAT (cpuBoxContacts3D.ts:457-466) */
+  int32_t color_rounds; /* Jones-Plassmann round budget per step */
+} avbd_params;
+
+/* A built scene as flat structure-of-arrays in creation order (what AvbdScene3D holds,
+ * src/native/scenes.js:107-698). Optional arrays may be NULL (defaults in brackets). */
+typedef struct avbd_scene_desc {
+  int32_t n_bodies;
+  const float* position;         /* 3n */
+  const float* rotation;         /* 4n (x, y, z, w) [identity] */
+  const float* size;             /* 3n full extents; spheres 2r */
+  const float* velocity;         /* 3n [0] */
+  const float* angular_velocity; /* 3n [0] */
+  const float* prev_velocity;    /* 3n [0] */
+  const float* mass;             /* n; <= 0 is static */
+  const float* moment;           /* 3n principal moments */
+  const float* friction;         /* n */
+  const float* radius;           /* n bounding radius */
+  const int32_t* shape;          /* n AVBD_SHAPE_* */
+  const uint32_t* group;         /* n [0xffffffff] */
+  const uint32_t* collides_with; /* n [0xffffffff] */
+  int32_t n_cons;
+  const int32_t* cons_kind;      /* n_cons AVBD_CONS_* in creation order */
+  const int32_t* cons_a;         /* -1 = world (joints) */
+  const int32_t* cons_b;
+  const float* cons_ra;          /* 3 n_cons body-local anchor (world point when a = -1) */
+  const float* cons_rb;          /* 3 n_cons */
+  const float* cons_p0;          /* joint: linear stiffness (INFINITY = hard); spring: stiffness */
+  const float* cons_p1;          /* joint: angular stiffness; spring: rest length (-1: current) */
+  const float* cons_p2;          /* joint: fracture threshold on |lambda_ang| */
+} avbd_scene_desc;
+
+/* readCounters() of src/vendor/three-avbd-lib/solver3D.ts:1460-1463 plus engine state. */
+typedef struct avbd_counters {
+  int64_t pairs;      /* candidate pairs (bounding spheres overlap) */
+  int64_t manifolds;  /* pairs with at least one contact */
+  int64_t contacts;
+  int64_t joints;     /* unbroken joints and springs */
+  int32_t colors;     /* colours used by the last step (max over worlds) */
+  int32_t conflicts;  /* bodies left sharing a colour with a neighbour */
+  int32_t overflow;   /* capacity regrowths so far */
+  int32_t steps;      /* steps taken */
+} avbd_counters;
+
+/* Per-kernel-class device time (CUDA events on the engine's stream) and algorithmic bytes,
+ * accumulated over the steps taken while profiling is on (the reference's timestamp phases,
+ * src/vendor/three-avbd-lib/solver3D.ts:1332-1447, profileDetailedNextStep). */
+typedef struct avbd_profile {
+  int32_t steps;
+  int32_t pad;
+  double ms_collide;   /* grid build, pair passes, narrowphase */
+  double ms_topology;  /* constraint lists, colouring, colour buckets */
+  double ms_primal;    /* every per-colour primal launch */
+  double ms_dual;
+  double ms_other;     /* joint/body warm start, velocities */
+  int64_t primal_launches;
+  int64_t launches;    /* kernel launches issued by the library since it was loaded */
+  double bytes_primal; /* algorithmic bytes (see the engine's traffic accounting) */
+  double bytes_dual;
+  double bytes_collide;
+} avbd_profile;
+
+/* ---------------------------------------------------------------- context */
+
+/* createSolverPipeline({backend}) (src/native/pipeline.js:14-92): binds a device and stream. */
+int avbd_ctx_create(int device, avbd_ctx** out);
+/* pipeline.destroy (src/native/pipeline.js:82-90): frees every world/batch it owns. */
+int avbd_ctx_destroy(avbd_ctx* ctx);
+/* Failure details of the last call on this thread. */
+const char* avbd_last_error(void);
+/* Library version string. */
+const char* avbd_version(void);
+/* The CUDA stream all of this context's work is queued on (cudaStream_t), so a host binding can
+ * order its own work or timing events after the engine's (the reference's device queue). */
+int avbd_ctx_stream(avbd_ctx* ctx, void** stream);
+/* Wait until all queued work of the context has finished (the reference's
+ * device.queue.onSubmittedWorkDone). */
+int avbd_ctx_synchronize(avbd_ctx* ctx);
+
+/* ---------------------------------------------------------------- plain worlds */
+
+/* pipeline.createSolver(scene, options) (src/native/pipeline.js:52-81). */
+int avbd_world_create(avbd_ctx* ctx, const avbd_scene_desc* scene, const avbd_params* params, avbd_world** out);
+/* world.destroy() */
+int avbd_world_destroy(avbd_world* w);
+/* world.step() repeated `steps` times (src/native/solver3D.js:350-359 -> AppGpuSolver3D.step,
+ * src/gpu/appGpuSolver3D.js:403-442 / CpuSolver3D.step, src/native/cpu/cpuSolver3D.ts:144-281). */
+int avbd_world_step(avbd_world* w, int32_t steps);
+/* world.readBodyState / readBodies: poses and velocities of all bodies (host arrays, any may
+ * be NULL): position 3n, rotation 4n, velocity 3n, angular 3n, prev_velocity 3n. */
+int avbd_world_read_state(avbd_world* w, float* position, float* rotation, float* velocity, float* angular, float* prev_velocity);
+/* world.readSelectedBodies(indices, {posesOnly}) (src/native/cpu/world.js:503-571):
+ * 8 floats per body (pos.xyz, friction, quat) when poses_only, else 40 (the 160-byte body
+ * record of reference/three-avbd/src/avbd3d/gpu/layout.ts:8-25). */
+int avbd_world_read_selected(avbd_world* w, const uint32_t* indices, int32_t n, int32_t poses_only, float* out);
+/* world.setPoses / setVelocities (src/native/runtime.js, scenes.d.ts:317-454); rotation or
+ * angular may be NULL. */
+int avbd_world_set_poses(avbd_world* w, const uint32_t* indices, int32_t n, const float* position, const float* rotation);
+int avbd_world_set_velocities(avbd_world* w, const uint32_t* indices, int32_t n, const float* velocity, const float* angular);
+/* world.readCounters() (src/vendor/three-avbd-lib/solver3D.ts:1460-1463). */
+int avbd_world_counters(avbd_world* w, avbd_counters* out);
+
+/* Parity dumps (readPairs / readContactList, solver3D.ts:1466-1506). Each writes at most `cap`
+ * records and stores the full count in *n. */
+/* Candidate pairs of the last step, sorted ascending by (hi, lo): 2 uint32 per pair. */
+int avbd_world_pairs(avbd_world* w, uint32_t* out, int64_t cap, int64_t* n);
+/* Contact count of each candidate pair of the last step (same order as avbd_world_pairs). */
+int avbd_world_pair_contacts(avbd_world* w, int32_t* out, int64_t cap, int64_t* n);
+/* Jones-Plassmann colour of each body after the last step (-1: static / none). */
+int avbd_world_colors(avbd_world* w, int32_t* out);
+
+/* Full solver state for one-step parity (the GpuSolver3D.seedFrom counterpart,
+ * src/vendor/three-avbd-lib/solver3D.ts:942-979): joint warm-start state (3 floats each, jid
+ * order), the live manifolds (pairs with contacts, sorted) and their contacts. Sizes first:
+ * call avbd_world_state_sizes, then avbd_world_export_state with buffers of those sizes. */
+int avbd_world_state_sizes(avbd_world* w, int32_t* n_joints, int64_t* n_manifolds, int64_t* n_contacts);
+int avbd_world_export_state(avbd_world* w, float* jpen_lin, float* jpen_ang, float* jlam_lin, float* jlam_ang,
+                            int32_t* jbroken, uint32_t* mpairs, int32_t* mcount, uint32_t* cfeature, float* cra,
+                            float* crb, float* cpen, float* clam, int32_t* cstick);
+
+/* ---------------------------------------------------------------- batched worlds */
+
+/* Many independent worlds stepped together: one launch sequence per step covers every world
+ * (no counterpart in the reference, which creates one solver per world:
+ * src/native/pipeline.js:52-81). World w of the batch keeps its own parameters. */
+int avbd_batch_create(avbd_ctx* ctx, const avbd_scene_desc* scenes, const avbd_params* params, int32_t n_worlds,
+                      avbd_batch** out);
+int avbd_batch_destroy(avbd_batch* b);
+/* Advance every world of the batch by `steps`. */
+int avbd_batch_step(avbd_batch* b, int32_t steps);
+int avbd_batch_world_count(avbd_batch* b, int32_t* n_worlds, int64_t* n_bodies);
+/* State of world `world` of the batch (as avbd_world_read_state). */
+int avbd_batch_read_state(avbd_batch* b, int32_t world, float* position, float* rotation, float* velocity,
+                          float* angular, float* prev_velocity);
+int avbd_batch_counters(avbd_batch* b, avbd_counters* out);
+/* Poses of every body of every world, 8 floats each (pos.xyz, friction, quat), world by world
+ * in creation order (readSelectedBodies(.., {posesOnly: true}) over the whole batch). */
+int avbd_batch_read_poses(avbd_batch* b, float* out);
+/* setVelocities for bodies given by batch-global index (world offset + body index). */
+int avbd_batch_set_velocities(avbd_batch* b, const uint32_t* indices, int32_t n, const float* velocity, const float* angular);
+
+/* Profiling (see avbd_profile): enable resets the accumulators; read returns them. */
+int avbd_world_profile(avbd_world* w, int32_t enable);
+int avbd_world_profile_read(avbd_world* w, avbd_profile* out);
+int avbd_batch_profile(avbd_batch* b, int32_t enable);
+int avbd_batch_profile_read(avbd_batch* b, avbd_profile* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* AVBD_GB300_H */

@@ -1,0 +1,155 @@
+"""CPU-side checks: the C-ABI library loads and exports every declared symbol, the scene
+builder validates like the reference, workloads have the configured shapes, and the oracle's
+app path behaves (no GPU needed)."""
+import ctypes
+import math
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def lib_path():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("avbd_build", os.path.join(ROOT, "babylon-avbd_gb300", "build.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.build()
+
+
+def declared_symbols():
+    names = []
+    for h in os.listdir(os.path.join(ROOT, "include")):
+        if h.endswith(".h"):
+            text = open(os.path.join(ROOT, "include", h)).read()
+            names += re.findall(r"^\s*(?:const\s+)?[a-z_0-9]+\*?\s+\**(avbd_[a-z_0-9]+)\s*\(", text, re.M)
+    return sorted(set(names))
+
+
+def test_library_exports_every_declared_symbol(lib_path):
+    lib = ctypes.CDLL(lib_path)
+    names = declared_symbols()
+    assert len(names) >= 20
+    for n in names:
+        assert hasattr(lib, n), n
+
+
+def test_ctypes_signatures_cover_header():
+    from avbd_gb300 import _lib
+    bound = {n for n, _, _ in _lib.SIGNATURES}
+    assert set(declared_symbols()) <= bound | set()
+
+
+def test_builder_validation_and_mass():
+    from avbd_gb300 import AvbdScene3D
+    s = AvbdScene3D(gravity=-9.81)
+    b = s.addBox([1, 2, 3], density=2)
+    arr = s.arrays()
+    assert arr.mass[b] == 12 and list(arr.moment[b]) == [13, 10, 5]
+    sp = s.addSphere(0.5, density=1000, position=[0, 3, 0], velocity=[1, 0, 0])
+    arr = s.arrays()
+    assert arr.shape[sp] == 1 and arr.radius[sp] == 0.5
+    assert abs(arr.mass[sp] - 4 / 3 * math.pi * 0.125 * 1000) < 1e-9
+    assert list(arr.prev_vel[sp]) == [0, 0, 0] and list(arr.vel[sp]) == [1, 0, 0]
+    with pytest.raises(ValueError):
+        s.addBox([1, -1, 1])
+    with pytest.raises(ValueError):
+        s.addBox([1, 1, 1], rotation=[0, 0, 0, 0])
+    with pytest.raises(ValueError):
+        s.addJoint(b, b)
+    with pytest.raises(ValueError):
+        AvbdScene3D(up=[0, 2, 0])
+    with pytest.raises(ValueError):
+        s.addSpring(None, b)
+    j = s.addJoint(None, b, [0, 5, 0], [0, 0, 0])
+    assert s.arrays().ca[j] == -1
+    m = s.addBox([1, 1, 1], density=1, mass=3)
+    a = s.arrays()
+    assert a.mass[m] == 3 and abs(a.moment[m][0] - 0.5) < 1e-12
+
+
+def test_world_mix_counts():
+    from avbd_gb300 import workloads
+    counts, sigma = workloads.world_counts()
+    assert len(counts) == 4096
+    assert counts.min() >= 16 and counts.max() <= 8192
+    assert abs(counts.sum() - 2_100_000) < 2000
+    assert 0.9 < sigma < 1.4
+    assert int(np.median(counts)) in range(240, 272)
+
+
+def test_box_pile_c0_layout():
+    from avbd_gb300 import workloads
+    s = workloads.box_pile_c0()
+    assert s.n_bodies == 1001 and s.mass[0] == 0 and np.all(s.mass[1:] == 1000)
+    assert np.all(np.abs(s.pos[1:, 1] - np.round((s.pos[1:, 1] - 0.55) / 1.05) * 1.05 - 0.55) <= 0.0100001)
+
+
+def test_oracle_app_stack_rests_on_ground():
+    """App path (Y up): a 5-box stack settles within the collision margin per contact."""
+    import oracle
+    from avbd_gb300.scene import SceneBuilder, SolverParams
+    b = SceneBuilder(SolverParams(dt=1 / 60, gravity=-10, up=(0, 1, 0), iterations=10))
+    b.rigid([100, 1, 100], 0, 0.5, [0, -0.5, 0])
+    for i in range(5):
+        b.rigid([1, 1, 1], 1, 0.5, [0, 0.5 + 1.2 * i, 0])
+    w = oracle.OracleWorld(b.arrays(), fp64=True, app=True)
+    w.step(600)
+    y = w.bodies()["pos"][1:, 1]
+    for i in range(5):
+        assert abs(y[i] - (0.5 + i)) < 0.011 * (i + 1), y
+
+
+def test_oracle_colored_equals_sequential_without_contacts():
+    """With no constraints the colour order cannot matter: bit-identical free fall."""
+    import oracle
+    from avbd_gb300 import workloads
+    s = workloads.mixed_pile(50, seed=3, extent=400.0)
+    a = oracle.OracleWorld(s, fp64=True, app=True, colored=False)
+    b = oracle.OracleWorld(s, fp64=True, app=True, colored=True)
+    a.step(3)
+    b.step(3)
+    assert np.array_equal(a.bodies()["pos"], b.bodies()["pos"])
+
+
+def test_oracle_fp32_narrowphase_box_box_kat():
+    """300 seeded rotated box pairs (reference tests/helpers/reference-contacts.js:20-57 LCG,
+    seed 0x51a7b0d): the float32 narrowphase agrees with float64 on hit/miss outside a 1 cm
+    skin, and the normal is unit length to 1e-4 (reference tests/gpu-stress.js:200-240)."""
+    import oracle
+    from avbd_gb300.scene import SceneBuilder, SolverParams
+    seed = 0x51A7B0D
+
+    def rnd():
+        nonlocal seed
+        seed = (seed * 1664525 + 1013904223) & 0xFFFFFFFF
+        return seed / 4294967296
+
+    hits = misses = 0
+    for _ in range(300):
+        b = SceneBuilder(SolverParams(up=(0, 1, 0)))
+        for k in range(2):
+            size = [0.2 + 1.8 * rnd() for _ in range(3)]
+            pos = [(rnd() - 0.5) * 2.0 for _ in range(3)]
+            q = [rnd() - 0.5 for _ in range(4)]
+            n = math.sqrt(sum(v * v for v in q))
+            i = b.rigid(size, 1, 0.5, pos)
+            b.bodies[i].quat = [v / n for v in q]
+        s = b.arrays()
+        s.pos = s.pos.astype(np.float32).astype(np.float64)
+        s.quat = s.quat.astype(np.float32).astype(np.float64)
+        s.size = s.size.astype(np.float32).astype(np.float64)
+        r32 = oracle.OracleWorld(s, fp64=False, app=True).collide(1, 0)
+        r64 = oracle.OracleWorld(s, fp64=True, app=True).collide(1, 0)
+        if (r32["count"] > 0) != (r64["count"] > 0):
+            continue  # grazing case inside the skin
+        if r64["count"]:
+            hits += 1
+            assert abs(np.linalg.norm(r32["basis"][0]) - 1) < 1e-4
+        else:
+            misses += 1
+    assert hits > 20 and misses > 20
