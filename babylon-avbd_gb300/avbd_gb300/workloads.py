@@ -13,7 +13,10 @@ on).
                 (r U[0.25, 0.75] m), uniform random orientation, centres uniform in a
                 2L x L x 2L volume (L = 200 m for 1,000,000 bodies, scaled with N^(1/3)),
                 over a static ground box 1.1 x the footprint, 2 m thick, top at y = 0.
-* world_mix     4,096 mixed piles with log-normal body counts (median 256, clipped to
+* lattice_pile  N config-1 bodies (same shape, size and orientation distributions) stacked in
+                a jittered cubic lattice (1.9 m spacing, +-0.05 m jitter) starting just above a
+                static ground box: a pile that is in contact from the first steps.
+* world_mix     4,096 lattice piles with log-normal body counts (median 256, clipped to
                 [16, 8,192]); sigma is chosen by bisection so the total is ~2.1 M bodies.
 * cloth_wall    a 256x256 grid of 0.1 m cubes with 4-neighbour ball joints, two corners pinned,
                 over a static 5 m sphere, beside a 100x2x50 wall of 1x0.5x0.5 m bricks hit by
@@ -115,6 +118,27 @@ def mixed_pile(n, seed, extent=None) -> SceneArrays:
     return _arrays(_concat([ground, bodies]), params(10))
 
 
+def lattice_pile(n, seed, spacing=1.9) -> SceneArrays:
+    rng = np.random.Generator(np.random.PCG64(seed))
+    ny = max(1, int(round(n ** (1.0 / 3.0) / 1.6)))
+    nxz = int(math.ceil(math.sqrt(n / ny)))
+    k = np.arange(n)
+    layer, rem = k // (nxz * nxz), k % (nxz * nxz)
+    ix, iz = rem // nxz, rem % nxz
+    pos = np.stack([(ix - (nxz - 1) / 2) * spacing, 1.05 + layer * spacing, (iz - (nxz - 1) / 2) * spacing], axis=1)
+    pos = pos + rng.uniform(-0.05, 0.05, size=(n, 3))
+    is_sphere = rng.random(n) < 0.3
+    half = rng.uniform(0.25, 1.0, size=(n, 3))
+    r = rng.uniform(0.25, 0.75, size=n)
+    size = np.where(is_sphere[:, None], (2 * r)[:, None] * np.ones((1, 3)), 2 * half)
+    quat = _uniform_quats(rng, n)
+    shape = np.where(is_sphere, SHAPE_SPHERE, SHAPE_BOX)
+    bodies = _bodies(size, np.full(n, DENSITY), FRICTION, pos, quat, shape, radius_sphere=r)
+    foot = 1.2 * nxz * spacing + 4.0
+    ground = _static_box((foot, 2.0, foot), (0.0, -1.0, 0.0))
+    return _arrays(_concat([ground, bodies]), params(10))
+
+
 def world_counts(n_worlds=4096, target=2_100_000, seed=SEED_BASE + 3, median=256, lo=16, hi=8192):
     """Log-normal world sizes; returns (counts, sigma) with sigma fitted to the target total."""
     rng = np.random.Generator(np.random.PCG64(seed))
@@ -136,7 +160,7 @@ def world_counts(n_worlds=4096, target=2_100_000, seed=SEED_BASE + 3, median=256
 
 def world_mix(n_worlds=4096, target=2_100_000, seed=SEED_BASE + 3):
     counts, sigma = world_counts(n_worlds, target, seed)
-    worlds = [mixed_pile(int(c), seed * 7919 + w) for w, c in enumerate(counts)]
+    worlds = [lattice_pile(int(c), (seed * 7919 + w) & 0xFFFFFFFFFFFF) for w, c in enumerate(counts)]
     return worlds, counts, sigma
 
 

@@ -470,13 +470,15 @@ class WorldSet {
     launch_pairs(B, worlds, nBodies, G, NC, J.broken, pairCount, pairStart, C.pair, capacity, ctr, scanTemp, s);
     CK(cudaMemcpyAsync(pairN[cur], &ctr->npairs, sizeof(int), cudaMemcpyDeviceToDevice, s));
     launch_narrowphase(B, worlds, C, Pv, pairN[cur ^ 1], pairN[cur], capacity, ctr, s);
+    // every span owns its two events (the pool recycles each event exactly once)
     cudaEvent_t e1 = prof ? mark() : nullptr;
+    cudaEvent_t e1b = prof ? mark() : nullptr;
     launch_adjacency(B, J, nJoints, C, pairN[cur], capacity, T, nBodies, scanTemp, s);
     launch_coloring(B, worlds, J, C, T, nBodies, rounds, ctr, s);
     if (prof) {
       cudaEvent_t e2 = mark();
       span(P_COLLIDE, e0, e1);
-      span(P_TOPO, e1, e2);
+      span(P_TOPO, e1b, e2);
     }
     CK(cudaMemcpyAsync(ctrHost, ctr, sizeof(Counters), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));

@@ -19,6 +19,7 @@ JavaScript and cannot run here) on a bounded sample of the same workload with al
 from __future__ import annotations
 
 import argparse
+import faulthandler
 import json
 import os
 import subprocess
@@ -30,6 +31,13 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path[:0] = [os.path.join(ROOT, "babylon-avbd_gb300"), os.path.join(ROOT, "oracle")]
 
 import numpy as np  # noqa: E402
+
+faulthandler.enable()
+
+
+def log(msg):
+    print(f"[bench {time.strftime('%H:%M:%S')}] {msg}", file=sys.stderr, flush=True)
+
 
 METRIC = "body-steps/s and p99 tick latency: batched/served vs plain GPU path at 1e-5 tol"
 UNIT = "body-steps/s"
@@ -47,6 +55,8 @@ def args_parse():
     p.add_argument("--cpu-sample", type=int, default=64, help="worlds timed on the CPU path")
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-plain", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
     return p.parse_args()
 
 
@@ -212,15 +222,19 @@ def run_ours(args, dist):
 
     dev = dist.local
     torch.cuda.set_device(dev)
+    log("building worlds")
     worlds, cfg = build_worlds(args, dist.rank)
+    log(f"{len(worlds)} worlds built; creating pipeline")
     pipe = createSolverPipeline("gb300", device=dev)
     stream = torch.cuda.ExternalStream(pipe.stream, device=dev)
     batch = pipe.createBatch(worlds)
     nb = batch.bodyCount
+    log(f"batch created ({nb} bodies); warm-up")
     for _ in range(args.warmup):
         batch.step(1)
     pipe.synchronize()
     # ---------------- timed region (device-resident)
+    log("timed region")
     batch.profile(True)
     launches0 = batch.profileRead()["launches"]
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
@@ -260,6 +274,7 @@ def run_ours(args, dist):
     breakdown["other"] = round(prof["ms_other"] / max(prof["steps"], 1), 3)
     # ---------------- e2e through the public API with host buffers
     e2e = None
+    log(f"timed region done: {elapsed_ms:.1f} ms")
     if not args.no_e2e:
         offs = np.cumsum([0] + batch.bodyCounts[:-1])
         # one command per world: kick its last body (world offset + count - 1) upwards
@@ -282,7 +297,8 @@ def run_ours(args, dist):
                "d2h_bytes_per_step": int(poses_np.nbytes)}
     # ---------------- plain path and CPU baseline (rank 0)
     plain = cpu = None
-    if dist.rank == 0:
+    log("e2e done")
+    if dist.rank == 0 and not args.no_plain:
         sample = sample_worlds(worlds, args.plain_sample)
         plain_worlds = [pipe.createSolver(w) for w in sample]
         for w in plain_worlds:
@@ -301,7 +317,10 @@ def run_ours(args, dist):
                            f"launch sequence, {psteps} steps after {args.warmup} warm-up steps"}
         for w in plain_worlds:
             w.destroy()
+        log("plain path done")
+    if dist.rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(sample_worlds(worlds, args.cpu_sample), args.warmup, args.steps, args.cpu_seconds)
+    log("cpu baseline done")
     pipe.destroy()
     if dist.rank != 0:
         return
