@@ -60,6 +60,7 @@ SIGNATURES = [
     ("avbd_world_step", C.c_int, [C.c_void_p, C.c_int32]),
     ("avbd_world_read_state", C.c_int, [C.c_void_p, _fp, _fp, _fp, _fp, _fp]),
     ("avbd_world_read_selected", C.c_int, [C.c_void_p, _up, C.c_int32, C.c_int32, _fp]),
+    ("avbd_world_read_selected_noalloc", C.c_int, [C.c_void_p, _up, C.c_int32, C.c_int32, _fp]),
     ("avbd_world_set_poses", C.c_int, [C.c_void_p, _up, C.c_int32, _fp, _fp]),
     ("avbd_world_set_velocities", C.c_int, [C.c_void_p, _up, C.c_int32, _fp, _fp]),
     ("avbd_world_counters", C.c_int, [C.c_void_p, C.POINTER(Counters)]),
@@ -81,6 +82,10 @@ SIGNATURES = [
     ("avbd_batch_profile", C.c_int, [C.c_void_p, C.c_int32]),
     ("avbd_batch_profile_read", C.c_int, [C.c_void_p, C.POINTER(Profile)]),
 ]
+
+# include/avbd_gb300.h
+AVBD_E_CAPACITY = -5
+NOALLOC_MAX_SELECTED = 8192
 
 _lib = None
 

@@ -21,6 +21,7 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <new>
 #include <stdexcept>
 #include <string>
@@ -797,6 +798,61 @@ int avbd_world_read_selected(avbd_world* w, const uint32_t* indices, int32_t n, 
   dfree(di);
   dfree(dout);
   if (e != cudaSuccess) throw Error(AVBD_E_CUDA, cudaGetErrorString(e));
+  API_END
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------- allocation-free selected reads
+// Staging for avbd_world_read_selected_noalloc: indices in the first
+// AVBD_NOALLOC_MAX_SELECTED words, then AVBD_NOALLOC_MAX_SELECTED records of 40 floats (the
+// record region starts 32 KB in, a multiple of 256 bytes). Nothing in it is read before the
+// call that uses it has written it, so no part needs clearing between calls.
+static __device__ __align__(256) float g_select_scratch[AVBD_NOALLOC_MAX_SELECTED * 41];
+
+namespace {
+
+std::mutex g_select_mutex;
+float* g_select_ptr[256] = {};
+
+// Device address of g_select_scratch on `device` (which must be current): looked up once per
+// device. In host code the symbol itself is only a host-side stand-in for the device array.
+float* select_scratch(int device) {
+  std::lock_guard<std::mutex> lock(g_select_mutex);
+  if (device < 0 || device >= 256) throw Error(AVBD_E_INVALID, "device index out of range");
+  if (!g_select_ptr[device]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_select_scratch);
+    if (e != cudaSuccess) throw Error(AVBD_E_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    g_select_ptr[device] = static_cast<float*>(p);
+  }
+  return g_select_ptr[device];
+}
+
+}  // namespace
+
+extern "C" {
+
+int avbd_world_read_selected_noalloc(avbd_world* w, const uint32_t* indices, int32_t n, int32_t poses_only, float* out) {
+  API_BEGIN
+  REQUIRE(w && (n == 0 || (indices && out)), "null argument");
+  REQUIRE(n >= 0, "negative count");
+  if (n > AVBD_NOALLOC_MAX_SELECTED)
+    throw Error(AVBD_E_CAPACITY, "avbd_world_read_selected_noalloc: at most " + std::to_string(AVBD_NOALLOC_MAX_SELECTED) +
+                                     " bodies per call (" + std::to_string(n) + " requested)");
+  WorldSet& S = *w->set;
+  bind(S.ctx);
+  for (int k = 0; k < n; k++) REQUIRE(indices[k] < uint32_t(S.worldsHost[0].bodyCount), "body index out of range");
+  if (n == 0) return AVBD_OK;
+  float* scratch = select_scratch(S.ctx->device);
+  uint32_t* dIdx = reinterpret_cast<uint32_t*>(scratch);
+  float* dOut = scratch + AVBD_NOALLOC_MAX_SELECTED;
+  const size_t stride = poses_only ? 8 : 40;
+  CK(cudaMemcpyAsync(dIdx, indices, size_t(n) * 4, cudaMemcpyHostToDevice, S.s));
+  k_read_selected<<<grid_blocks(n, 128), 128, 0, S.s>>>(S.B, S.worlds, dIdx, n, 0, poses_only, dOut); note_launches(1);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(out, dOut, size_t(n) * stride * 4, cudaMemcpyDeviceToHost, S.s));
+  CK(cudaStreamSynchronize(S.s));
   API_END
 }
 

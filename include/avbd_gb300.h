@@ -144,6 +144,19 @@ int avbd_world_read_state(avbd_world* w, float* position, float* rotation, float
  * 8 floats per body (pos.xyz, friction, quat) when poses_only, else 40 (the 160-byte body
  * record of reference/three-avbd/src/avbd3d/gpu/layout.ts:8-25). */
 int avbd_world_read_selected(avbd_world* w, const uint32_t* indices, int32_t n, int32_t poses_only, float* out);
+/* Allocation-free variant of avbd_world_read_selected. No counterpart in the reference.
+ * For hosts that must not allocate device memory while they run: a render or input loop that
+ * reads poses every frame (cudaMalloc and cudaFree can block until the whole device is idle, which
+ * stalls the frame), a serving process that has committed its device-memory budget to world state,
+ * or a JavaScript binding that must not block its event loop. The staging for the indices and the
+ * records lives in one fixed per-GPU device buffer of AVBD_NOALLOC_MAX_SELECTED records (about
+ * 1.3 MB, held by every GPU that loads the library until the process exits). The first call on a
+ * device looks that buffer up (make the first call before any stream capture). Requests with
+ * n > AVBD_NOALLOC_MAX_SELECTED fail with AVBD_E_CAPACITY. Every call shares the buffer, which keeps
+ * the last call's contents: calls whose work overlaps on the GPU (different threads or streams)
+ * race; serialise them. Output is identical to avbd_world_read_selected. */
+#define AVBD_NOALLOC_MAX_SELECTED 8192
+int avbd_world_read_selected_noalloc(avbd_world* w, const uint32_t* indices, int32_t n, int32_t poses_only, float* out);
 /* world.setPoses / setVelocities (src/native/runtime.js, scenes.d.ts:317-454); rotation or
  * angular may be NULL. */
 int avbd_world_set_poses(avbd_world* w, const uint32_t* indices, int32_t n, const float* position, const float* rotation);
