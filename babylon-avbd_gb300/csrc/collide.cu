@@ -438,26 +438,35 @@ __device__ void edge_contact(Builder& bld, const OBB& A, const OBB& B, int axA, 
   if (bld.n == 0) bld.add(support_point(A, nAB), support_point(B, -nAB), key);
 }
 
-// Returns the contact count (0: separated); basis rows n (B to A), t1, t2.
-__device__ int collide(Builder& bld, float4 pA, float4 qA, float4 sA, float4 pB, float4 qB, float4 sB, bool faceBias, M33& basis) {
+// SAT over the 15 axes (collide.ts:312-338 with the faceBias rule); false when separated.
+__device__ __forceinline__ bool sat(float4 pA, float4 qA, float4 sA, float4 pB, float4 qB, float4 sB, bool faceBias, Sat& best) {
   OBB A = make_obb(pA, qA, sA), B = make_obb(pB, qB, sB);
   V3 delta = B.c - A.c;
   Sat bf{AXIS_FACE_A, 0, 0, -FLT_MAX, V3{0, 0, 0}, false};
   Sat be{AXIS_EDGE, 0, 0, -FLT_MAX, V3{0, 0, 0}, false};
   for (int i = 0; i < 3; i++)
-    if (!test_axis(A, B, delta, A.ax[i], AXIS_FACE_A, i, -1, bf)) return 0;
+    if (!test_axis(A, B, delta, A.ax[i], AXIS_FACE_A, i, -1, bf)) return false;
   for (int i = 0; i < 3; i++)
-    if (!test_axis(A, B, delta, B.ax[i], AXIS_FACE_B, -1, i, bf)) return 0;
+    if (!test_axis(A, B, delta, B.ax[i], AXIS_FACE_B, -1, i, bf)) return false;
+#pragma unroll 1
   for (int i = 0; i < 3; i++)
+#pragma unroll 1
     for (int j = 0; j < 3; j++)
-      if (!test_axis(A, B, delta, cross(A.ax[i], B.ax[j]), AXIS_EDGE, i, j, be)) return 0;
-  if (!bf.valid) return 0;
-  Sat best = bf;
+      if (!test_axis(A, B, delta, cross(A.ax[i], B.ax[j]), AXIS_EDGE, i, j, be)) return false;
+  if (!bf.valid) return false;
+  best = bf;
   if (be.valid) {
     const float rel = 0.95f, absT = 0.01f;
     bool edgeWins = !faceBias ? rel * be.sep > bf.sep + absT : be.sep > rel * bf.sep + absT;
     if (edgeWins) best = be;
   }
+  return true;
+}
+
+// Contacts for the axis SAT chose (collide.ts:340-344); basis rows n (B to A), t1, t2.
+__device__ __forceinline__ int contacts(Builder& bld, float4 pA, float4 qA, float4 sA, float4 pB, float4 qB, float4 sB, const Sat& best,
+                                        M33& basis) {
+  OBB A = make_obb(pA, qA, sA), B = make_obb(pB, qB, sB);
   basis = orthonormal(-best.n);
   if (best.type == AXIS_EDGE) edge_contact(bld, A, B, best.ia, best.ib, best.n);
   else if (best.type == AXIS_FACE_A) face_manifold(bld, A, B, true, best.ia, best.n);
@@ -677,91 +686,167 @@ __device__ __forceinline__ int find_pair(const uint2* __restrict__ pairs, int n,
   return -1;
 }
 
-__global__ void __launch_bounds__(128) k_narrowphase(BodyPtrs bd, const WorldDev* __restrict__ worlds, PairPtrs cur, PairPtrs prev,
-                                                     const int* __restrict__ prevN, const int* __restrict__ curN, int capacity) {
+// Warm start and store the contacts of pair p (cpuPhysics3D.js:108-145): match the previous
+// step's contacts of the same pair by feature, keep sticking anchors (not for rolling pairs),
+// C0 = basis (xA - xB) + margin, decayed lambda, clamped penalty, mass-penalty floor.
+__device__ __forceinline__ void finish_pair(const BodyPtrs& bd, const WorldDev& W, PairPtrs& cur, const PairPtrs& prev, int nprev,
+                                            int p, uint2 key, float4 pA, float4 qA, float4 sA, float4 pB, float4 qB, float4 sB,
+                                            bool rolling, int n, const M33& basis, const uint32_t* feat, const V3* rA, const V3* rB) {
+  const float friction = sqrtf(sA.w * sB.w);
+  cur.count[p] = n;
+  cur.basis[3 * p + 0] = f4(basis.r0, friction);
+  cur.basis[3 * p + 1] = f4(basis.r1, 0.f);
+  cur.basis[3 * p + 2] = f4(basis.r2, 0.f);
+  if (n == 0) return;
+  const int pp = nprev > 0 ? find_pair(prev.pair, nprev, key) : -1;
+  const int pn = pp >= 0 ? prev.count[pp] : 0;
+  const float ag = W.alpha * W.gamma;
+  float penFloor = 0.f;
+  if (W.flags & FLAG_MASS_PENALTY) {
+    const float mA = bd.mass[key.x].x, mB = bd.mass[key.y].x;
+    const float mass = fminr(mA > 0.f ? mA : INFINITY, mB > 0.f ? mB : INFINITY);
+    penFloor = fmaxf(PENALTY_MIN, fminf(PENALTY_MAX, mass / (W.dt * W.dt)));
+  }
+#pragma unroll 1
+  for (int k = 0; k < n; k++) {
+    V3 ra = rA[k], rb = rB[k];
+    V3 pen{0.f, 0.f, 0.f}, lam{0.f, 0.f, 0.f};
+    bool stick = false;
+#pragma unroll 1
+    for (int q = 0; q < pn; q++) {
+      const float4* o = prev.ct + (size_t(pp) * MAX_CONTACTS + q) * 4;
+      const float4 o0 = o[0];
+      const uint32_t of = __float_as_uint(o0.w);
+      if ((of & ~STICK_BIT) != feat[k]) continue;
+      const float4 o1 = o[1], o2 = o[2], o3 = o[3];
+      stick = (of & STICK_BIT) != 0;
+      if (stick && !rolling) {
+        ra = v3(o0);
+        rb = v3(o1);
+      }
+      pen = v3(o2);
+      lam = v3(o3);
+      break;
+    }
+    const V3 d = xform(v3(pA), qA, ra) - xform(v3(pB), qB, rb);
+    V3 C0 = mulv(basis, d);
+    C0.x += COLLISION_MARGIN;
+    lam = V3{lam.x * ag, lam.y * ag, lam.z * ag};
+    pen = V3{clampr(pen.x * W.gamma, PENALTY_MIN, PENALTY_MAX), clampr(pen.y * W.gamma, PENALTY_MIN, PENALTY_MAX),
+             clampr(pen.z * W.gamma, PENALTY_MIN, PENALTY_MAX)};
+    if (W.flags & FLAG_MASS_PENALTY) pen.x = fmaxf(pen.x, penFloor);
+    float4* o = cur.ct + (size_t(p) * MAX_CONTACTS + k) * 4;
+    o[0] = f4(ra, __uint_as_float(feat[k] | (stick ? STICK_BIT : 0u)));
+    o[1] = f4(rb, C0.x);
+    o[2] = f4(pen, C0.y);
+    o[3] = f4(lam, C0.z);
+  }
+}
+
+// warp-aggregated append of `p` to list (count in *n)
+__device__ __forceinline__ void append(int* list, int* n, int p, bool take) {
+  const unsigned m = __ballot_sync(__activemask(), take);
+  if (!take) return;
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(m) - 1;
+  int base = 0;
+  if (lane == leader) base = atomicAdd(n, __popc(m));
+  base = __shfl_sync(m, base, leader);
+  list[base + __popc(m & ((1u << lane) - 1))] = p;
+}
+
+// Pass 1: box-box pairs run SAT; separated ones are finished here (no contacts), the others are
+// queued with their chosen axis. Pairs with a sphere are queued for the generic path.
+__global__ void __launch_bounds__(256) k_np_classify(BodyPtrs bd, const WorldDev* __restrict__ worlds, PairPtrs cur,
+                                                     const int* __restrict__ curN, int capacity, NarrowScratch ns) {
   const int np = min(*curN, capacity);
+  for (int base = blockIdx.x * blockDim.x; base < np; base += gridDim.x * blockDim.x) {
+    const int p = base + threadIdx.x;
+    bool boxHit = false, sphere = false;
+    if (p < np) {
+      const uint2 key = cur.pair[p];
+      const int a = int(key.x), b = int(key.y);
+      const int shA = bd.meta[a].y, shB = bd.meta[b].y;
+      if (shA == SHAPE_SPHERE || shB == SHAPE_SPHERE) {
+        sphere = true;
+      } else {
+        const WorldDev& W = worlds[bd.meta[a].x];
+        box::Sat best;
+        if (box::sat(bd.pos[a], bd.rot[a], bd.size[a], bd.pos[b], bd.rot[b], bd.size[b], (W.flags & FLAG_FACE_BIAS) != 0, best)) {
+          boxHit = true;
+          ns.sat[p] = make_float4(best.n.x, best.n.y, best.n.z, __int_as_float(best.type | ((best.ia & 0xff) << 8) | ((best.ib & 0xff) << 16)));
+        } else {
+          cur.count[p] = 0;
+        }
+      }
+    }
+    append(ns.boxList, &ns.ctr[0], p, boxHit);
+    append(ns.sphereList, &ns.ctr[1], p, sphere);
+  }
+}
+
+// Pass 2a: contacts of box-box pairs that SAT found overlapping.
+__global__ void __launch_bounds__(128) k_np_box(BodyPtrs bd, const WorldDev* __restrict__ worlds, PairPtrs cur, PairPtrs prev,
+                                                const int* __restrict__ prevN, int capacity, NarrowScratch ns) {
+  const int n = ns.ctr[0];
   const int nprev = prev.pair ? min(*prevN, capacity) : 0;
-  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const int p = ns.boxList[k];
+    const uint2 key = cur.pair[p];
+    const int a = int(key.x), b = int(key.y);
+    const float4 pA = bd.pos[a], qA = bd.rot[a], sA = bd.size[a];
+    const float4 pB = bd.pos[b], qB = bd.rot[b], sB = bd.size[b];
+    const WorldDev& W = worlds[bd.meta[a].x];
+    const float4 sr = ns.sat[p];
+    const int code = __float_as_int(sr.w);
+    box::Sat best;
+    best.type = code & 0xff;
+    best.ia = (code >> 8) & 0xff;
+    best.ib = (code >> 16) & 0xff;
+    best.n = v3(sr);
+    best.valid = true;
+    best.sep = 0.f;
+    uint32_t feat[MAX_CONTACTS];
+    V3 rA[MAX_CONTACTS], rB[MAX_CONTACTS];
+    box::Builder bld;
+    bld.n = 0;
+    bld.pA = pA; bld.qA = qA; bld.pB = pB; bld.qB = qB;
+    bld.feat = feat; bld.rA = rA; bld.rB = rB;
+    M33 basis;
+    const int nc = box::contacts(bld, pA, qA, sA, pB, qB, sB, best, basis);
+    finish_pair(bd, W, cur, prev, nprev, p, key, pA, qA, sA, pB, qB, sB, false, nc, basis, feat, rA, rB);
+  }
+}
+
+// Pass 2b: pairs with a sphere (generic support-function SAT, one contact).
+__global__ void __launch_bounds__(128) k_np_sphere(BodyPtrs bd, const WorldDev* __restrict__ worlds, PairPtrs cur, PairPtrs prev,
+                                                   const int* __restrict__ prevN, int capacity, NarrowScratch ns) {
+  const int n = ns.ctr[1];
+  const int nprev = prev.pair ? min(*prevN, capacity) : 0;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const int p = ns.sphereList[k];
     const uint2 key = cur.pair[p];
     const int a = int(key.x), b = int(key.y);
     const float4 pA = bd.pos[a], qA = bd.rot[a], sA = bd.size[a];
     const float4 pB = bd.pos[b], qB = bd.rot[b], sB = bd.size[b];
     const int shA = bd.meta[a].y, shB = bd.meta[b].y;
-    const WorldDev W = worlds[bd.meta[a].x];
+    const WorldDev& W = worlds[bd.meta[a].x];
     M33 basis{V3{0, 0, 0}, V3{0, 0, 0}, V3{0, 0, 0}};
-    uint32_t feat[MAX_CONTACTS];
-    V3 rA[MAX_CONTACTS], rB[MAX_CONTACTS];
-    int n;
-    const bool rolling = shA == SHAPE_SPHERE || shB == SHAPE_SPHERE;
-    if (!rolling) {
-      box::Builder bld;
-      bld.n = 0;
-      bld.pA = pA; bld.qA = qA; bld.pB = pB; bld.qB = qB;
-      bld.feat = feat; bld.rA = rA; bld.rB = rB;
-      n = box::collide(bld, pA, qA, sA, pB, qB, sB, (W.flags & FLAG_FACE_BIAS) != 0, basis);
-    } else {
-      n = gen::collide(pA, qA, sA, shA, pB, qB, sB, shB, basis, rA[0], rB[0]);
-      feat[0] = 1u;  // feature i + 1
-    }
-    const float friction = sqrtf(sA.w * sB.w);
-    cur.count[p] = n;
-    cur.basis[3 * p + 0] = f4(basis.r0, friction);
-    cur.basis[3 * p + 1] = f4(basis.r1, 0.f);
-    cur.basis[3 * p + 2] = f4(basis.r2, 0.f);
-    if (n == 0) continue;
-    // warm start from last step's manifold of this pair (cpuPhysics3D.js:108-145)
-    const int pp = nprev > 0 ? find_pair(prev.pair, nprev, key) : -1;
-    const int pn = pp >= 0 ? prev.count[pp] : 0;
-    const float ag = W.alpha * W.gamma;
-    float penFloor = 0.f;
-    if (W.flags & FLAG_MASS_PENALTY) {
-      const float mA = bd.mass[a].x, mB = bd.mass[b].x;
-      const float mass = fminr(mA > 0.f ? mA : INFINITY, mB > 0.f ? mB : INFINITY);
-      penFloor = fmaxf(PENALTY_MIN, fminf(PENALTY_MAX, mass / (W.dt * W.dt)));
-    }
-    for (int k = 0; k < n; k++) {
-      V3 ra = rA[k], rb = rB[k];
-      V3 pen{0.f, 0.f, 0.f}, lam{0.f, 0.f, 0.f};
-      bool stick = false;
-      for (int q = 0; q < pn; q++) {
-        const float4* o = prev.ct + (size_t(pp) * MAX_CONTACTS + q) * 4;
-        const float4 o0 = o[0];
-        const uint32_t of = __float_as_uint(o0.w);
-        if ((of & ~STICK_BIT) != feat[k]) continue;
-        const float4 o1 = o[1], o2 = o[2], o3 = o[3];
-        stick = (of & STICK_BIT) != 0;
-        if (stick && !rolling) {
-          ra = v3(o0);
-          rb = v3(o1);
-        }
-        pen = v3(o2);
-        lam = v3(o3);
-        break;
-      }
-      // C0 = basis (world(a, rA) - world(b, rB)) + margin on the normal row
-      const V3 d = xform(v3(pA), qA, ra) - xform(v3(pB), qB, rb);
-      V3 C0 = mulv(basis, d);
-      C0.x += COLLISION_MARGIN;
-      lam = V3{lam.x * ag, lam.y * ag, lam.z * ag};
-      pen = V3{clampr(pen.x * W.gamma, PENALTY_MIN, PENALTY_MAX), clampr(pen.y * W.gamma, PENALTY_MIN, PENALTY_MAX),
-               clampr(pen.z * W.gamma, PENALTY_MIN, PENALTY_MAX)};
-      if (W.flags & FLAG_MASS_PENALTY) pen.x = fmaxf(pen.x, penFloor);
-      float4* o = cur.ct + (size_t(p) * MAX_CONTACTS + k) * 4;
-      o[0] = f4(ra, __uint_as_float(feat[k] | (stick ? STICK_BIT : 0u)));
-      o[1] = f4(rb, C0.x);
-      o[2] = f4(pen, C0.y);
-      o[3] = f4(lam, C0.z);
-    }
+    uint32_t feat[1] = {1u};  // feature i + 1
+    V3 rA[1], rB[1];
+    const int nc = gen::collide(pA, qA, sA, shA, pB, qB, sB, shB, basis, rA[0], rB[0]);
+    finish_pair(bd, W, cur, prev, nprev, p, key, pA, qA, sA, pB, qB, sB, true, nc, basis, feat, rA, rB);
   }
 }
 
 void launch_narrowphase(const BodyPtrs& b, const WorldDev* worlds, PairPtrs cur, PairPtrs prev, const int* prevN,
-                        const int* curN, int capacity, Counters* ctr, cudaStream_t s) {
-  (void)ctr;
-  // grid sized for the capacity; threads past the live pair count exit at once
-  int blocks = grid_blocks(capacity, 128);
-  if (blocks > 152 * 32) blocks = 152 * 32;
-  k_narrowphase<<<blocks, 128, 0, s>>>(b, worlds, cur, prev, prevN, curN, capacity); note_launches(1);
+                        const int* curN, int capacity, NarrowScratch ns, cudaStream_t s) {
+  cudaMemsetAsync(ns.ctr, 0, 2 * sizeof(int), s);
+  int blocks = grid_blocks(capacity, 256);
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  k_np_classify<<<blocks, 256, 0, s>>>(b, worlds, cur, curN, capacity, ns); note_launches(1);
+  k_np_box<<<152 * 16, 128, 0, s>>>(b, worlds, cur, prev, prevN, capacity, ns); note_launches(1);
+  k_np_sphere<<<152 * 16, 128, 0, s>>>(b, worlds, cur, prev, prevN, capacity, ns); note_launches(1);
 }
 
 }  // namespace avbd

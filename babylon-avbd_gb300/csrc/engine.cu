@@ -87,6 +87,7 @@ class WorldSet {
   int cur = 0;
   int capacity = 0;
   Grid G{};
+  NarrowScratch NS{};
   NoCollide NC{};
   Topo T{};
   int* pairCount = nullptr;
@@ -202,6 +203,11 @@ class WorldSet {
     }
     dfree(T.adjList);
     T.adjList = nullptr;
+    dfree(NS.sat);
+    dfree(NS.boxList);
+    dfree(NS.sphereList);
+    dfree(NS.ctr);
+    NS = NarrowScratch{};
   }
 
   static void validate(const avbd_scene_desc& d, const avbd_params& p) {
@@ -454,6 +460,10 @@ class WorldSet {
     }
     capacity = cap;
     T.adjList = dalloc<uint32_t>(2 * (size_t(nJoints) + size_t(cap)) + 1);
+    NS.sat = dalloc<float4>(cap);
+    NS.boxList = dalloc<int>(cap);
+    NS.sphereList = dalloc<int>(cap);
+    NS.ctr = dalloc<int>(2);
     size_t need = scanNeed();
     if (need > scanBytes) {
       dfree(scanTemp);
@@ -470,7 +480,7 @@ class WorldSet {
     launch_grid_build(B, worlds, nBodies, G, scanTemp, s);
     launch_pairs(B, worlds, nBodies, G, NC, J.broken, pairCount, pairStart, C.pair, capacity, ctr, scanTemp, s);
     CK(cudaMemcpyAsync(pairN[cur], &ctr->npairs, sizeof(int), cudaMemcpyDeviceToDevice, s));
-    launch_narrowphase(B, worlds, C, Pv, pairN[cur ^ 1], pairN[cur], capacity, ctr, s);
+    launch_narrowphase(B, worlds, C, Pv, pairN[cur ^ 1], pairN[cur], capacity, NS, s);
     // every span owns its two events (the pool recycles each event exactly once)
     cudaEvent_t e1 = prof ? mark() : nullptr;
     cudaEvent_t e1b = prof ? mark() : nullptr;

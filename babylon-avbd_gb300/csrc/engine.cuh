@@ -85,6 +85,15 @@ struct Grid {
   int* large;          // large bodies of each world, global ids, ascending
 };
 
+// Narrowphase scratch (per step): SAT results of overlapping box pairs, the queued pair lists
+// and their counts (ctr[0] box hits, ctr[1] sphere pairs).
+struct NarrowScratch {
+  float4* sat;
+  int* boxList;
+  int* sphereList;
+  int* ctr;
+};
+
 struct NoCollide {
   unsigned long long* keys;  // (hi << 32 | lo), sorted
   int* jid;                  // joint/spring id (broken ones stop blocking), -1 for ignore pairs
@@ -114,7 +123,7 @@ void launch_pairs(const BodyPtrs& b, const WorldDev* worlds, int nBodies, Grid g
                   int* pairCount, int* pairStart, uint2* pairsOut, int capacity, Counters* ctr, void* scanTemp,
                   cudaStream_t s);
 void launch_narrowphase(const BodyPtrs& b, const WorldDev* worlds, PairPtrs cur, PairPtrs prev, const int* prevN,
-                        const int* curN, int capacity, Counters* ctr, cudaStream_t s);
+                        const int* curN, int capacity, NarrowScratch ns, cudaStream_t s);
 
 // solve.cu
 void launch_joint_warmstart(const BodyPtrs& b, const WorldDev* worlds, JointPtrs j, int nJoints, Counters* ctr, cudaStream_t s);

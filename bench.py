@@ -269,6 +269,10 @@ def run_ours(args, dist):
             "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_kind,
             "traffic": traffic, "algorithmic_bytes_per_step": byts / max(prof["steps"], 1),
             "launches_per_step": (prof["primal_launches"] / max(prof["steps"], 1)) if dom == "primal" else None}
+    roof["classes"] = {k: {"ms_per_step": round(v[0] / max(prof["steps"], 1), 3),
+                           "algorithmic_gb_per_step": round(v[1] / max(prof["steps"], 1) / 1e9, 4),
+                           "achieved_gbs": round(v[1] / (v[0] / 1000.0) / 1e9, 1) if v[0] > 0 else None}
+                       for k, v in classes.items()}
     breakdown = {k: round(v[0] / max(prof["steps"], 1), 3) for k, v in classes.items()}
     breakdown["topology"] = round(prof["ms_topology"] / max(prof["steps"], 1), 3)
     breakdown["other"] = round(prof["ms_other"] / max(prof["steps"], 1), 3)
