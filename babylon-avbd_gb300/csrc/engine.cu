@@ -97,6 +97,7 @@ class WorldSet {
   void* scanTemp = nullptr;
   size_t scanBytes = 0;
   int maxIter = 0, rounds = 64;
+  size_t itemCap = 0;
   int steps = 0, regrowths = 0;
   bool haveStats = false;
   // profiling: event pairs per kernel class, harvested after each step's counter readback
@@ -183,8 +184,8 @@ class WorldSet {
     void* ptrs[] = {worlds, B.pos, B.rot, B.pos0, B.rot0, B.posY, B.rotY, B.vel, B.ang, B.vprev, B.size, B.mass, B.meta,
                     J.ab, J.rA, J.rB, J.stiff, J.penLin, J.penAng, J.lamLin, J.lamAng, J.C0Lin, J.C0Ang, J.restQ, J.broken,
                     G.cellCount, G.cellFill, G.cellBodies, G.bodyBucket, G.large, NC.keys, NC.jid, T.adjStart, T.adjFill,
-                    T.colorPrev, T.color, T.won, T.pending, T.colorBodies, pairCount, pairStart, ctr, scanTemp, traffic,
-                    poseStage};
+                    T.colorPrev, T.color, T.won, T.pending, T.colorBodies, T.itemStart, T.itemRef, T.contrib, pairCount,
+                    pairStart, ctr, scanTemp, traffic, poseStage};
     for (void* p : ptrs) dfree(p);
     freePairs();
     if (ctrHost) cudaFreeHost(ctrHost);
@@ -409,6 +410,7 @@ class WorldSet {
     T.won = dalloc<int>(N);
     T.pending = dalloc<unsigned char>(N);
     T.colorBodies = dalloc<int>(N);
+    T.itemStart = dalloc<int>(N + 1);
     std::vector<int> minus(N, -1);
     CK(cudaMemcpy(T.colorPrev, minus.data(), N * 4, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(T.color, minus.data(), N * 4, cudaMemcpyHostToDevice));
@@ -472,6 +474,28 @@ class WorldSet {
     }
   }
 
+  // item lists and the per-colour contribution planes, sized from this step's counts
+  void ensureItems() {
+    size_t need = size_t(std::max(ctrHost->itemsTotal, 1));
+    int maxColor = 1;
+    for (int c = 0; c < MAX_COLORS; c++) maxColor = std::max(maxColor, ctrHost->colorItems[c]);
+    if (need > itemCap || maxColor > T.contribCap) {
+      CK(cudaStreamSynchronize(s));
+      size_t cap = std::max(need, itemCap);
+      cap = cap + cap / 4 + 1024;
+      dfree(T.itemRef);
+      T.itemRef = nullptr;
+      T.itemRef = dalloc<int2>(cap);
+      itemCap = cap;
+      int ccap = std::max(maxColor, T.contribCap);
+      ccap = ccap + ccap / 4 + 1024;
+      dfree(T.contrib);
+      T.contrib = nullptr;
+      T.contrib = dalloc<float4>(size_t(ccap) * 7);
+      T.contribCap = ccap;
+    }
+  }
+
   // ------------------------------------------------------------------ step
   void collideAndColor() {
     PairPtrs& C = P[cur];
@@ -486,6 +510,7 @@ class WorldSet {
     cudaEvent_t e1b = prof ? mark() : nullptr;
     launch_adjacency(B, J, nJoints, C, pairN[cur], capacity, T, nBodies, scanTemp, s);
     launch_coloring(B, worlds, J, C, T, nBodies, rounds, ctr, s);
+    launch_items_count(C, T, nBodies, ctr, scanTemp, s);
     if (prof) {
       cudaEvent_t e2 = mark();
       span(P_COLLIDE, e0, e1);
@@ -508,6 +533,8 @@ class WorldSet {
       regrowths++;
     }
     PairPtrs& C = P[cur];
+    ensureItems();
+    launch_items_fill(C, T, nBodies, ctr, s);
     cudaEvent_t o0 = prof ? mark() : nullptr;
     launch_joint_warmstart(B, worlds, J, nJoints, ctr, s);
     launch_body_warmstart(B, worlds, nBodies, s);
@@ -518,7 +545,7 @@ class WorldSet {
         const int cnt = ctrHost->colorCount[c];
         if (!cnt) continue;
         cudaEvent_t a = prof ? mark() : nullptr;
-        launch_primal(B, worlds, J, C, T, ctr, c, it, cnt, s);
+        launch_primal(B, worlds, J, C, T, ctr, c, it, cnt, ctrHost->colorItems[c], s);
         if (prof) {
           span(P_PRIMAL, a, mark());
           profPrimalLaunches++;

@@ -74,6 +74,8 @@ struct Counters {
   int joints;
   int colorCount[MAX_COLORS];
   int colorStart[MAX_COLORS + 1];
+  int itemsTotal;
+  int colorItems[MAX_COLORS];
 };
 
 struct Grid {
@@ -109,6 +111,11 @@ struct Topo {
   int* won;        // round scratch
   unsigned char* pending;
   int* colorBodies;
+  // manifold-contact work items of the dynamic bodies, bucket order (see launch_primal):
+  int* itemStart;  // per bucket slot, N + 1 (exclusive scan of item counts)
+  int2* itemRef;   // item -> (pair, contact | side << 3)
+  float4* contrib; // per item of the current colour: 7 planes of `contribCap` float4
+  int contribCap;
 };
 
 // ---------------------------------------------------------------- launchers
@@ -132,8 +139,12 @@ void launch_adjacency(const BodyPtrs& b, JointPtrs j, int nJoints, PairPtrs cur,
                       Topo t, int nBodies, void* scanTemp, cudaStream_t s);
 void launch_coloring(const BodyPtrs& b, const WorldDev* worlds, JointPtrs j, PairPtrs cur, Topo t, int nBodies, int rounds,
                      Counters* ctr, cudaStream_t s);
+// Per step, before the counter readback: per-body manifold-contact item counts, their scan and
+// the per-colour item totals. After the readback (with itemRef/contrib large enough): fill.
+void launch_items_count(PairPtrs cur, Topo t, int nBodies, Counters* ctr, void* scanTemp, cudaStream_t s);
+void launch_items_fill(PairPtrs cur, Topo t, int nBodies, const Counters* ctr, cudaStream_t s);
 void launch_primal(const BodyPtrs& b, const WorldDev* worlds, JointPtrs j, PairPtrs cur, Topo t, const Counters* ctr,
-                   int color, int iteration, int maxBodies, cudaStream_t s);
+                   int color, int iteration, int nBodiesColor, int nItemsColor, cudaStream_t s);
 void launch_dual(const BodyPtrs& b, const WorldDev* worlds, JointPtrs j, int nJoints, PairPtrs cur, const int* npairs,
                  int capacity, int iteration, cudaStream_t s);
 void launch_velocities(const BodyPtrs& b, const WorldDev* worlds, int nBodies, cudaStream_t s);
