@@ -48,9 +48,40 @@ __device__ __forceinline__ uint32_t cell_hash(int world, int cx, int cy, int cz)
 
 __device__ __forceinline__ int cell_coord(float x, float cell) { return __float2int_rd(x / cell); }
 
+// The tick's active lists: bodies and joints of the active worlds (world by world) and the
+// body -> list position map, from the active-world table (prefixes computed on the host).
+__device__ __forceinline__ int active_world(const Tick& t, int k, int field) {
+  int a = 0, b = t.nActive;  // last entry with prefix <= k
+  while (b - a > 1) {
+    const int m = (a + b) >> 1;
+    if ((field == 0 ? t.active[m].y : t.active[m].z) <= k) a = m;
+    else b = m;
+  }
+  return a;
+}
+
+__global__ void k_tick_lists(Tick t, const WorldDev* __restrict__ worlds, Topo topo) {
+  const int total = max(t.nBodies, t.nJoints);
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < total; k += gridDim.x * blockDim.x) {
+    if (k < t.nBodies) {
+      const int a = active_world(t, k, 0);
+      const int4 e = t.active[a];
+      const int b = worlds[e.x].bodyOff + (k - e.y);
+      t.bodies[k] = b;
+      topo.activeIndex[b] = k;
+    }
+    if (k < t.nJoints) {
+      const int a = active_world(t, k, 1);
+      const int4 e = t.active[a];
+      t.joints[k] = worlds[e.x].jointOff + (k - e.z);
+    }
+  }
+}
+
 __global__ void k_grid_count(const float4* __restrict__ pos, const int4* __restrict__ meta, const WorldDev* __restrict__ worlds,
-                             int n, uint32_t mask, int* __restrict__ cellCount, int* __restrict__ bodyBucket) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+                             Tick t, uint32_t mask, int* __restrict__ cellCount, int* __restrict__ bodyBucket) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < t.nBodies; k += gridDim.x * blockDim.x) {
+    const int i = t.bodies[k];
     const float4 p = pos[i];
     const int w = meta[i].x;
     const WorldDev& W = worlds[w];
@@ -64,24 +95,31 @@ __global__ void k_grid_count(const float4* __restrict__ pos, const int4* __restr
   }
 }
 
-__global__ void k_grid_scatter(const int* __restrict__ bodyBucket, int n, const int* __restrict__ cellStart,
+__global__ void k_grid_scatter(const int* __restrict__ bodyBucket, Tick t, const int* __restrict__ cellStart,
                                int* __restrict__ cellFill, int* __restrict__ cellBodies) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    int b = bodyBucket[i];
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < t.nBodies; k += gridDim.x * blockDim.x) {
+    const int i = t.bodies[k];
+    const int b = bodyBucket[i];
     if (b < 0) continue;
-    int slot = cellStart[b] + atomicAdd(&cellFill[b], 1);
+    const int slot = cellStart[b] + atomicAdd(&cellFill[b], 1);
     cellBodies[slot] = i;
   }
 }
 
-void launch_grid_build(const BodyPtrs& b, const WorldDev* worlds, int nBodies, Grid g, void* scanTemp, cudaStream_t s) {
+void launch_tick_begin(Tick t, Topo topo, const WorldDev* worlds, cudaStream_t s) {
+  const int total = t.nBodies > t.nJoints ? t.nBodies : t.nJoints;
+  if (total == 0) return;
+  k_tick_lists<<<grid_blocks(total, 256), 256, 0, s>>>(t, worlds, topo); note_launches(1);
+}
+
+void launch_grid_build(const BodyPtrs& b, const WorldDev* worlds, Tick t, Grid g, void* scanTemp, cudaStream_t s) {
   const int table = int(g.tableMask) + 1;
   cudaMemsetAsync(g.cellCount, 0, sizeof(int) * (table + 1), s);
   cudaMemsetAsync(g.cellFill, 0, sizeof(int) * table, s);
-  if (nBodies == 0) return;
-  k_grid_count<<<grid_blocks(nBodies, 256), 256, 0, s>>>(b.pos, b.meta, worlds, nBodies, g.tableMask, g.cellCount, g.bodyBucket); note_launches(1);
+  if (t.nBodies == 0) return;
+  k_grid_count<<<grid_blocks(t.nBodies, 256), 256, 0, s>>>(b.pos, b.meta, worlds, t, g.tableMask, g.cellCount, g.bodyBucket); note_launches(1);
   scan_exclusive(g.cellCount, table + 1, nullptr, scanTemp, s);
-  k_grid_scatter<<<grid_blocks(nBodies, 256), 256, 0, s>>>(g.bodyBucket, nBodies, g.cellCount, g.cellFill, g.cellBodies); note_launches(1);
+  k_grid_scatter<<<grid_blocks(t.nBodies, 256), 256, 0, s>>>(g.bodyBucket, t, g.cellCount, g.cellFill, g.cellBodies); note_launches(1);
 }
 
 // ------------------------------------------------------------------ pair predicate
@@ -165,29 +203,56 @@ __device__ __forceinline__ void for_each_partner(const PairCtx& c, const WorldDe
   }
 }
 
-__global__ void k_pair_count(PairCtx c, const WorldDev* __restrict__ worlds, Grid g, int n, int* __restrict__ pairCount) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+// Pair passes over the tick's active bodies (k = list position). Each world writes its pairs into
+// its own region of the buffer it does not hold its last state in; a world whose pairs exceed its
+// region records how many it needs (the host grows the region and re-runs the tick).
+__global__ void k_pair_count(PairCtx c, const WorldDev* __restrict__ worlds, Grid g, Tick t, int* __restrict__ pairCount) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k <= t.nBodies; k += gridDim.x * blockDim.x) {
     int cnt = 0;
-    for_each_partner(c, worlds, g, i, [&](int) { cnt++; });
-    pairCount[i] = cnt;
+    if (k < t.nBodies) for_each_partner(c, worlds, g, t.bodies[k], [&](int) { cnt++; });
+    pairCount[k] = cnt;
   }
 }
 
-__global__ void k_pair_write(PairCtx c, const WorldDev* __restrict__ worlds, Grid g, int n, const int* __restrict__ pairStart,
-                             uint2* __restrict__ out, int capacity) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const int start = pairStart[i];
-    int k = 0;
+// per active world: pairs found, region overflow, pair counts of the active-pair prefix
+__global__ void k_pair_worlds(const WorldDev* __restrict__ worlds, Tick t, const int* __restrict__ pairStart, Counters* ctr) {
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < t.nActive; a += gridDim.x * blockDim.x) {
+    const int4 e = t.active[a];
+    const WorldDev& W = worlds[e.x];
+    const int need = pairStart[e.y + W.bodyCount] - pairStart[e.y];
+    const int cur = 1 - t.which[e.x];
+    const int n = min(need, W.pairCap);
+    t.pairN[cur * t.maxWorlds + e.x] = n;
+    t.pairPrefix[a] = n;
+    if (need > W.pairCap) {
+      t.wover[e.x] = need;
+      atomicAdd(&ctr->overflowWorlds, 1);
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) t.pairPrefix[t.nActive] = 0;
+}
+
+__global__ void k_pair_write(PairCtx c, const WorldDev* __restrict__ worlds, Grid g, Tick t, const int* __restrict__ pairStart,
+                             uint2* __restrict__ pairs) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < t.nBodies; k += gridDim.x * blockDim.x) {
+    const int i = t.bodies[k];
+    const int w = c.meta[i].x;
+    const WorldDev& W = worlds[w];
+    const int4 e = t.active[t.wactive[w]];
+    const int local = pairStart[k] - pairStart[e.y];
+    const int cap = W.pairCap;
+    uint2* out = pairs + (size_t)(1 - t.which[w]) * t.slotStride + W.pairOff;
+    int n = 0;
     for_each_partner(c, worlds, g, i, [&](int j) {
-      const int slot = start + k++;
-      if (slot < capacity) out[slot] = make_uint2(uint32_t(i), uint32_t(j));
+      const int slot = local + n++;
+      if (slot < cap) out[slot] = make_uint2(uint32_t(i), uint32_t(j));
     });
     // insertion sort of this body's range by partner (a body has a few dozen partners at most)
-    const int end = min(start + k, capacity);
-    for (int a = start + 1; a < end; a++) {
+    const int end = min(local + n, cap);
+    for (int a = local + 1; a < end; a++) {
       const uint2 v = out[a];
       int b = a;
-      while (b > start && out[b - 1].y > v.y) {
+      while (b > local && out[b - 1].y > v.y) {
         out[b] = out[b - 1];
         b--;
       }
@@ -196,24 +261,34 @@ __global__ void k_pair_write(PairCtx c, const WorldDev* __restrict__ worlds, Gri
   }
 }
 
-__global__ void k_pair_finish(Counters* ctr, int capacity) {
-  ctr->npairs = min(ctr->pairsNeeded, capacity);
+// active pair slots: the written part of each active world's region, world by world
+__global__ void k_pair_slots(const WorldDev* __restrict__ worlds, Tick t, const Counters* __restrict__ ctr) {
+  const int total = ctr->activePairs;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += gridDim.x * blockDim.x) {
+    int a = 0, b = t.nActive;
+    while (b - a > 1) {
+      const int m = (a + b) >> 1;
+      if (t.pairPrefix[m] <= q) a = m;
+      else b = m;
+    }
+    const int w = t.active[a].x;
+    t.pairs[q] = (1 - t.which[w]) * t.slotStride + worlds[w].pairOff + (q - t.pairPrefix[a]);
+  }
 }
 
-void launch_pairs(const BodyPtrs& b, const WorldDev* worlds, int nBodies, Grid g, NoCollide nc, const int* jbroken,
-                  int* pairCount, int* pairStart, uint2* pairsOut, int capacity, Counters* ctr, void* scanTemp,
-                  cudaStream_t s) {
+void launch_pairs(const BodyPtrs& b, const WorldDev* worlds, Tick t, Grid g, NoCollide nc, const int* jbroken, int* pairCount,
+                  PairPtrs P, Counters* ctr, void* scanTemp, cudaStream_t s) {
   PairCtx c{b.pos, b.mass, b.meta, nc, jbroken};
-  if (nBodies == 0) {
-    cudaMemsetAsync(&ctr->pairsNeeded, 0, sizeof(int), s);
-    k_pair_finish<<<1, 1, 0, s>>>(ctr, capacity); note_launches(1);
-    return;
-  }
-  k_pair_count<<<grid_blocks(nBodies, 128), 128, 0, s>>>(c, worlds, g, nBodies, pairCount); note_launches(1);
-  cudaMemcpyAsync(pairStart, pairCount, sizeof(int) * nBodies, cudaMemcpyDeviceToDevice, s);
-  scan_exclusive(pairStart, nBodies, &ctr->pairsNeeded, scanTemp, s);
-  k_pair_write<<<grid_blocks(nBodies, 128), 128, 0, s>>>(c, worlds, g, nBodies, pairStart, pairsOut, capacity); note_launches(1);
-  k_pair_finish<<<1, 1, 0, s>>>(ctr, capacity); note_launches(1);
+  cudaMemsetAsync(ctr, 0, 2 * sizeof(int), s);  // activePairs, overflowWorlds
+  if (t.nActive == 0) return;
+  k_pair_count<<<grid_blocks(t.nBodies + 1, 128), 128, 0, s>>>(c, worlds, g, t, pairCount); note_launches(1);
+  scan_exclusive(pairCount, t.nBodies + 1, nullptr, scanTemp, s);
+  k_pair_worlds<<<grid_blocks(t.nActive, 128), 128, 0, s>>>(worlds, t, pairCount, ctr); note_launches(1);
+  scan_exclusive(t.pairPrefix, t.nActive + 1, &ctr->activePairs, scanTemp, s);
+  k_pair_write<<<grid_blocks(t.nBodies, 128), 128, 0, s>>>(c, worlds, g, t, pairCount, P.pair); note_launches(1);
+  int blocks = grid_blocks(t.nBodies * 8LL, 256);
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  k_pair_slots<<<blocks, 256, 0, s>>>(worlds, t, ctr); note_launches(1);
 }
 
 // ------------------------------------------------------------------ box-box (collide.ts)
@@ -669,8 +744,9 @@ __device__ int collide(float4 pA, float4 qA, float4 sA, int shA, float4 pB, floa
 
 // ------------------------------------------------------------------ narrowphase kernel
 
-__device__ __forceinline__ int find_pair(const uint2* __restrict__ pairs, int n, uint2 key) {
+__device__ __forceinline__ int find_pair(const uint2* __restrict__ pairs, int base, int n, uint2 key) {
   const unsigned long long k = (unsigned long long)key.x << 32 | key.y;
+  pairs += base;
   int a = 0, b = n;
   while (a < b) {
     int m = (a + b) >> 1;
@@ -681,7 +757,7 @@ __device__ __forceinline__ int find_pair(const uint2* __restrict__ pairs, int n,
   }
   if (a < n) {
     uint2 p = pairs[a];
-    if (p.x == key.x && p.y == key.y) return a;
+    if (p.x == key.x && p.y == key.y) return base + a;
   }
   return -1;
 }
@@ -689,7 +765,7 @@ __device__ __forceinline__ int find_pair(const uint2* __restrict__ pairs, int n,
 // Warm start and store the contacts of pair p (cpuPhysics3D.js:108-145): match the previous
 // step's contacts of the same pair by feature, keep sticking anchors (not for rolling pairs),
 // C0 = basis (xA - xB) + margin, decayed lambda, clamped penalty, mass-penalty floor.
-__device__ __forceinline__ void finish_pair(const BodyPtrs& bd, const WorldDev& W, PairPtrs& cur, const PairPtrs& prev, int nprev,
+__device__ __forceinline__ void finish_pair(const BodyPtrs& bd, const WorldDev& W, const Tick& t, int w, PairPtrs& cur,
                                             int p, uint2 key, float4 pA, float4 qA, float4 sA, float4 pB, float4 qB, float4 sB,
                                             bool rolling, int n, const M33& basis, const uint32_t* feat, const V3* rA, const V3* rB) {
   const float friction = sqrtf(sA.w * sB.w);
@@ -698,8 +774,11 @@ __device__ __forceinline__ void finish_pair(const BodyPtrs& bd, const WorldDev& 
   cur.basis[3 * p + 1] = f4(basis.r1, 0.f);
   cur.basis[3 * p + 2] = f4(basis.r2, 0.f);
   if (n == 0) return;
-  const int pp = nprev > 0 ? find_pair(prev.pair, nprev, key) : -1;
-  const int pn = pp >= 0 ? prev.count[pp] : 0;
+  // the world's previous pairs: its region in the buffer it holds its last state in
+  const int pw = t.which[w];
+  const int nprev = t.pairN[pw * t.maxWorlds + w];
+  const int pp = nprev > 0 ? find_pair(cur.pair, pw * t.slotStride + W.pairOff, nprev, key) : -1;
+  const int pn = pp >= 0 ? cur.count[pp] : 0;
   const float ag = W.alpha * W.gamma;
   float penFloor = 0.f;
   if (W.flags & FLAG_MASS_PENALTY) {
@@ -714,7 +793,7 @@ __device__ __forceinline__ void finish_pair(const BodyPtrs& bd, const WorldDev& 
     bool stick = false;
 #pragma unroll 1
     for (int q = 0; q < pn; q++) {
-      const float4* o = prev.ct + (size_t(pp) * MAX_CONTACTS + q) * 4;
+      const float4* o = cur.ct + (size_t(pp) * MAX_CONTACTS + q) * 4;
       const float4 o0 = o[0];
       const uint32_t of = __float_as_uint(o0.w);
       if ((of & ~STICK_BIT) != feat[k]) continue;
@@ -757,13 +836,14 @@ __device__ __forceinline__ void append(int* list, int* n, int p, bool take) {
 
 // Pass 1: box-box pairs run SAT; separated ones are finished here (no contacts), the others are
 // queued with their chosen axis. Pairs with a sphere are queued for the generic path.
-__global__ void __launch_bounds__(256) k_np_classify(BodyPtrs bd, const WorldDev* __restrict__ worlds, PairPtrs cur,
-                                                     const int* __restrict__ curN, int capacity, NarrowScratch ns) {
-  const int np = min(*curN, capacity);
+__global__ void __launch_bounds__(256) k_np_classify(BodyPtrs bd, const WorldDev* __restrict__ worlds, PairPtrs cur, Tick t,
+                                                     const Counters* __restrict__ ctr, NarrowScratch ns) {
+  const int np = ctr->activePairs;
   for (int base = blockIdx.x * blockDim.x; base < np; base += gridDim.x * blockDim.x) {
-    const int p = base + threadIdx.x;
+    const int q = base + threadIdx.x;
+    const int p = q < np ? t.pairs[q] : 0;
     bool boxHit = false, sphere = false;
-    if (p < np) {
+    if (q < np) {
       const uint2 key = cur.pair[p];
       const int a = int(key.x), b = int(key.y);
       const int shA = bd.meta[a].y, shB = bd.meta[b].y;
@@ -774,30 +854,30 @@ __global__ void __launch_bounds__(256) k_np_classify(BodyPtrs bd, const WorldDev
         box::Sat best;
         if (box::sat(bd.pos[a], bd.rot[a], bd.size[a], bd.pos[b], bd.rot[b], bd.size[b], (W.flags & FLAG_FACE_BIAS) != 0, best)) {
           boxHit = true;
-          ns.sat[p] = make_float4(best.n.x, best.n.y, best.n.z, __int_as_float(best.type | ((best.ia & 0xff) << 8) | ((best.ib & 0xff) << 16)));
+          ns.sat[q] = make_float4(best.n.x, best.n.y, best.n.z, __int_as_float(best.type | ((best.ia & 0xff) << 8) | ((best.ib & 0xff) << 16)));
         } else {
           cur.count[p] = 0;
         }
       }
     }
-    append(ns.boxList, &ns.ctr[0], p, boxHit);
+    append(ns.boxList, &ns.ctr[0], q, boxHit);
     append(ns.sphereList, &ns.ctr[1], p, sphere);
   }
 }
 
 // Pass 2a: contacts of box-box pairs that SAT found overlapping.
-__global__ void __launch_bounds__(128) k_np_box(BodyPtrs bd, const WorldDev* __restrict__ worlds, PairPtrs cur, PairPtrs prev,
-                                                const int* __restrict__ prevN, int capacity, NarrowScratch ns) {
+__global__ void __launch_bounds__(128) k_np_box(BodyPtrs bd, const WorldDev* __restrict__ worlds, PairPtrs cur, Tick t,
+                                                NarrowScratch ns) {
   const int n = ns.ctr[0];
-  const int nprev = prev.pair ? min(*prevN, capacity) : 0;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-    const int p = ns.boxList[k];
+    const int q = ns.boxList[k];
+    const int p = t.pairs[q];
     const uint2 key = cur.pair[p];
     const int a = int(key.x), b = int(key.y);
     const float4 pA = bd.pos[a], qA = bd.rot[a], sA = bd.size[a];
     const float4 pB = bd.pos[b], qB = bd.rot[b], sB = bd.size[b];
     const WorldDev& W = worlds[bd.meta[a].x];
-    const float4 sr = ns.sat[p];
+    const float4 sr = ns.sat[q];
     const int code = __float_as_int(sr.w);
     box::Sat best;
     best.type = code & 0xff;
@@ -814,15 +894,14 @@ __global__ void __launch_bounds__(128) k_np_box(BodyPtrs bd, const WorldDev* __r
     bld.feat = feat; bld.rA = rA; bld.rB = rB;
     M33 basis;
     const int nc = box::contacts(bld, pA, qA, sA, pB, qB, sB, best, basis);
-    finish_pair(bd, W, cur, prev, nprev, p, key, pA, qA, sA, pB, qB, sB, false, nc, basis, feat, rA, rB);
+    finish_pair(bd, W, t, bd.meta[a].x, cur, p, key, pA, qA, sA, pB, qB, sB, false, nc, basis, feat, rA, rB);
   }
 }
 
 // Pass 2b: pairs with a sphere (generic support-function SAT, one contact).
-__global__ void __launch_bounds__(128) k_np_sphere(BodyPtrs bd, const WorldDev* __restrict__ worlds, PairPtrs cur, PairPtrs prev,
-                                                   const int* __restrict__ prevN, int capacity, NarrowScratch ns) {
+__global__ void __launch_bounds__(128) k_np_sphere(BodyPtrs bd, const WorldDev* __restrict__ worlds, PairPtrs cur, Tick t,
+                                                   NarrowScratch ns) {
   const int n = ns.ctr[1];
-  const int nprev = prev.pair ? min(*prevN, capacity) : 0;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
     const int p = ns.sphereList[k];
     const uint2 key = cur.pair[p];
@@ -835,18 +914,19 @@ __global__ void __launch_bounds__(128) k_np_sphere(BodyPtrs bd, const WorldDev* 
     uint32_t feat[1] = {1u};  // feature i + 1
     V3 rA[1], rB[1];
     const int nc = gen::collide(pA, qA, sA, shA, pB, qB, sB, shB, basis, rA[0], rB[0]);
-    finish_pair(bd, W, cur, prev, nprev, p, key, pA, qA, sA, pB, qB, sB, true, nc, basis, feat, rA, rB);
+    finish_pair(bd, W, t, bd.meta[a].x, cur, p, key, pA, qA, sA, pB, qB, sB, true, nc, basis, feat, rA, rB);
   }
 }
 
-void launch_narrowphase(const BodyPtrs& b, const WorldDev* worlds, PairPtrs cur, PairPtrs prev, const int* prevN,
-                        const int* curN, int capacity, NarrowScratch ns, cudaStream_t s) {
+void launch_narrowphase(const BodyPtrs& b, const WorldDev* worlds, Tick t, PairPtrs P, NarrowScratch ns, const Counters* ctr,
+                        int pairBudget, cudaStream_t s) {
   cudaMemsetAsync(ns.ctr, 0, 2 * sizeof(int), s);
-  int blocks = grid_blocks(capacity, 256);
+  if (t.nActive == 0) return;
+  int blocks = grid_blocks(pairBudget, 256);
   if (blocks > 152 * 16) blocks = 152 * 16;
-  k_np_classify<<<blocks, 256, 0, s>>>(b, worlds, cur, curN, capacity, ns); note_launches(1);
-  k_np_box<<<152 * 16, 128, 0, s>>>(b, worlds, cur, prev, prevN, capacity, ns); note_launches(1);
-  k_np_sphere<<<152 * 16, 128, 0, s>>>(b, worlds, cur, prev, prevN, capacity, ns); note_launches(1);
+  k_np_classify<<<blocks, 256, 0, s>>>(b, worlds, P, t, ctr, ns); note_launches(1);
+  k_np_box<<<152 * 16, 128, 0, s>>>(b, worlds, P, t, ns); note_launches(1);
+  k_np_sphere<<<152 * 16, 128, 0, s>>>(b, worlds, P, t, ns); note_launches(1);
 }
 
 }  // namespace avbd

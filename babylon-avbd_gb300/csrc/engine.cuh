@@ -1,15 +1,21 @@
 // Internal interface of the AVBD engine: device layouts shared by the kernel translation units
 // and the host orchestration (engine.cu). Not part of the C ABI.
 //
-// Layout in HBM (structure of arrays, one float4 per field, all worlds of a set concatenated):
-//   bodies   pos(xyz, bounding radius) rot  pos0(x-) rot0  posY(inertial) rotY
-//            vel  ang  vprev  size(xyz, friction)  mass(m, Ix, Iy, Iz)  meta(world, shape, group, mask)
-//   joints   body pair, rA(xyz, kind) rB(xyz, rest) stiff(lin, ang, fracture, torqueArm)
-//            penLin penAng lamLin lamAng C0Lin C0Ang restQ, broken flag
-//   pairs    (hi, lo) sorted ascending; per pair: contact count, basis rows n(w: friction), t1, t2,
-//            and 8 contact slots of 4 float4: rA(xyz, feature|stick) rB(xyz, C0.n) pen(xyz, C0.t1)
-//            lam(xyz, C0.t2). Two pair buffers (previous step, this step) swap every step.
-//   topology per-body constraint lists (CSR), Jones-Plassmann colour state, colour buckets.
+// Every world is a self-contained segment of one arena in HBM:
+//   bodies   a contiguous range of the body arrays (structure of arrays, one float4 per field):
+//            pos(xyz, bounding radius) rot pos0(x-) rot0 posY(inertial) rotY vel ang vprev
+//            size(xyz, friction) mass(m, Ix, Iy, Iz) meta(world, shape, group, mask)
+//   joints   a contiguous range of the joint arrays: body pair, rA(xyz, kind) rB(xyz, rest)
+//            stiff(lin, ang, fracture, torqueArm) penLin penAng lamLin lamAng C0Lin C0Ang restQ, broken
+//   pairs    a region of pair slots, present in two buffers (slot + k * slotStride, k = 0, 1): the
+//            world's previous state lives in buffer which[w], a step writes the other buffer and
+//            flips which[w]. Per slot: (hi, lo) sorted ascending within the world, contact count,
+//            basis rows n(w: friction), t1, t2, and 8 contact slots of 4 float4: rA(xyz,
+//            feature|stick) rB(xyz, C0.n) pen(xyz, C0.t1) lam(xyz, C0.t2).
+//   colours  two buffers of per-body colour state, selected like the pairs.
+// A step (a "tick") runs over an explicit list of active worlds: the bodies, joints and pair slots
+// of those worlds only. Worlds not stepped keep their state untouched, so a world evolves the
+// same way whether it is stepped alone, in a batch, or parked between requests.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -20,6 +26,7 @@ namespace avbd {
 
 constexpr int MAX_CONTACTS = 8;
 constexpr int MAX_COLORS = 64;
+constexpr int MAX_LARGE = 64;  // large-body slots per world
 constexpr float PENALTY_MIN = 1.0f;
 constexpr float PENALTY_MAX = 1e10f;
 constexpr float COLLISION_MARGIN = 0.01f;
@@ -34,14 +41,15 @@ constexpr int KIND_SPRING = 1;
 constexpr int FLAG_MASS_PENALTY = 1;
 constexpr int FLAG_FACE_BIAS = 2;
 
-// Per-world parameters and ranges (80 bytes).
+// Per-world parameters and ranges (96 bytes).
 struct WorldDev {
   float dt, gravity, alpha, gamma;
   float betaLin, betaAng, cell, largeR;
   float up0, up1, up2;
   int iterations;
   int flags, bodyOff, bodyCount, largeOff;
-  int largeCount, jointOff, jointCount, pad;
+  int largeCount, jointOff, jointCount, pairOff;
+  int pairCap, pad0, pad1, pad2;
 };
 
 struct BodyPtrs {
@@ -55,18 +63,38 @@ struct JointPtrs {
   int* broken;
 };
 
+// Both pair buffers (slots [0, slotStride) and [slotStride, 2 slotStride)).
 struct PairPtrs {
   uint2* pair;     // (hi, lo)
   int* count;      // contacts (0: no manifold)
-  float4* basis;   // 3 per pair
-  float4* ct;      // 4 per contact slot, 8 slots per pair
+  float4* basis;   // 3 per slot
+  float4* ct;      // 4 per contact, 8 contacts per slot
 };
 
-// Device counters (one block of ints, reset each step where noted).
+// The active set of one tick.
+struct Tick {
+  const int4* active;   // per active world, by body offset: (world, bodyPrefix, jointPrefix, -)
+  int nActive;
+  const int* wactive;   // world -> index in `active` (-1: not stepped)
+  int* which;           // world -> buffer holding its last completed state
+  int* bodies;          // active bodies, world by world
+  int nBodies;
+  int* joints;          // active joints
+  int nJoints;
+  int* pairs;           // active pair slots (count in Counters::activePairs)
+  int* pairPrefix;      // [nActive + 1] scanned pair counts of the active worlds
+  int* pairN;           // [2 * maxWorlds]: pairs of world w in buffer k at [k * maxWorlds + w]
+  int* wover;           // world -> pair slots needed when its region overflowed (0: fits)
+  int maxWorlds;
+  int slotStride;       // pair slots per buffer
+  int bodyStride;       // colour entries per buffer
+};
+
+// Device counters (one block of ints, reset each tick where noted).
 struct Counters {
-  int npairs;      // candidate pairs written
-  int pairsNeeded; // candidate pairs found (> capacity: overflow)
-  int remaining;   // colouring: bodies still pending
+  int activePairs;      // pair slots written this tick (all active worlds)
+  int overflowWorlds;   // worlds whose pair region overflowed
+  int remaining;        // colouring: bodies still pending
   int ncolors;
   int conflicts;
   int manifolds;
@@ -84,11 +112,12 @@ struct Grid {
   int* cellFill;
   int* cellBodies;     // small bodies bucketed
   int* bodyBucket;     // per body (-1: large)
-  int* large;          // large bodies of each world, global ids, ascending
+  int* large;          // MAX_LARGE slots per world: its large bodies, ascending
 };
 
-// Narrowphase scratch (per step): SAT results of overlapping box pairs, the queued pair lists
-// and their counts (ctr[0] box hits, ctr[1] sphere pairs).
+// Narrowphase scratch (per tick), indexed by position q in the tick's active pair list: SAT
+// results of overlapping box pairs, the queued lists (box hits by q, sphere pairs by slot) and
+// their counts (ctr[0] box hits, ctr[1] sphere pairs).
 struct NarrowScratch {
   float4* sat;
   int* boxList;
@@ -102,18 +131,19 @@ struct NoCollide {
   int n;
 };
 
+// Per-tick topology, indexed by a body's position k in the tick's active body list.
 struct Topo {
-  int* adjStart;  // N + 1
-  int* adjFill;   // N
+  int* adjStart;   // nBodies + 1
+  int* adjFill;    // nBodies
   uint32_t* adjList;
-  int* colorPrev;  // colour state carried from the previous step
-  int* color;      // this step's colours
-  int* won;        // round scratch
-  unsigned char* pending;
-  int* colorBodies;
+  int* activeIndex;  // body -> k (valid for active bodies)
+  int* color;        // both colour buffers, 2 * bodyStride entries (see Tick::which)
+  int* won;          // round scratch, per body
+  unsigned char* pending;  // per body
+  int* colorBodies;  // active indices k, bucketed by colour
   // manifold-contact work items of the dynamic bodies, bucket order (see launch_primal):
-  int* itemStart;  // per bucket slot, N + 1 (exclusive scan of item counts)
-  int2* itemRef;   // item -> (pair, contact | side << 3)
+  int* itemStart;  // per bucket slot, nBodies + 1 (exclusive scan of item counts)
+  int2* itemRef;   // item -> (pair slot, contact | side << 3)
   float4* contrib; // per item of the current colour: 7 planes of `contribCap` float4
   int contribCap;
 };
@@ -123,47 +153,43 @@ struct Topo {
 size_t scan_temp_bytes(int n);
 // exclusive scan of n ints in place; writes the total to *total (device) if non-null
 void scan_exclusive(int* data, int n, int* total, void* temp, cudaStream_t s);
-
-// collide.cu
-void launch_grid_build(const BodyPtrs& b, const WorldDev* worlds, int nBodies, Grid g, void* scanTemp, cudaStream_t s);
-void launch_pairs(const BodyPtrs& b, const WorldDev* worlds, int nBodies, Grid g, NoCollide nc, const int* jbroken,
-                  int* pairCount, int* pairStart, uint2* pairsOut, int capacity, Counters* ctr, void* scanTemp,
-                  cudaStream_t s);
-void launch_narrowphase(const BodyPtrs& b, const WorldDev* worlds, PairPtrs cur, PairPtrs prev, const int* prevN,
-                        const int* curN, int capacity, NarrowScratch ns, cudaStream_t s);
-
-// solve.cu
-void launch_joint_warmstart(const BodyPtrs& b, const WorldDev* worlds, JointPtrs j, int nJoints, Counters* ctr, cudaStream_t s);
-void launch_body_warmstart(const BodyPtrs& b, const WorldDev* worlds, int nBodies, cudaStream_t s);
-void launch_adjacency(const BodyPtrs& b, JointPtrs j, int nJoints, PairPtrs cur, const int* npairs, int capacity,
-                      Topo t, int nBodies, void* scanTemp, cudaStream_t s);
-void launch_coloring(const BodyPtrs& b, const WorldDev* worlds, JointPtrs j, PairPtrs cur, Topo t, int nBodies, int rounds,
-                     Counters* ctr, cudaStream_t s);
-// Per step, before the counter readback: per-body manifold-contact item counts, their scan and
-// the per-colour item totals. After the readback (with itemRef/contrib large enough): fill.
-void launch_items_count(PairPtrs cur, Topo t, int nBodies, Counters* ctr, void* scanTemp, cudaStream_t s);
-void launch_items_fill(PairPtrs cur, Topo t, int nBodies, const Counters* ctr, cudaStream_t s);
-void launch_primal(const BodyPtrs& b, const WorldDev* worlds, JointPtrs j, PairPtrs cur, Topo t, const Counters* ctr,
-                   int color, int iteration, int nBodiesColor, int nItemsColor, cudaStream_t s);
-void launch_dual(const BodyPtrs& b, const WorldDev* worlds, JointPtrs j, int nJoints, PairPtrs cur, const int* npairs,
-                 int capacity, int iteration, cudaStream_t s);
-void launch_velocities(const BodyPtrs& b, const WorldDev* worlds, int nBodies, cudaStream_t s);
-void launch_count_active(JointPtrs j, int nJoints, PairPtrs cur, const int* npairs, int capacity, Counters* ctr, cudaStream_t s);
-
 int grid_blocks(long long n, int threads);
-
 // Kernel launches issued by this library (host counter, for the benchmark's launch count).
 void note_launches(int n);
 long long launches_total();
 
-// Algorithmic bytes of one step's kernels, from the step's live counts (the bytes each kernel
-// must move at minimum; see launch_traffic).
-struct Traffic {
-  unsigned long long primalPerIter;  // all colours of one iteration
-  unsigned long long dualPerIter;
-  unsigned long long collide;        // grid + pairs + narrowphase
-};
-void launch_traffic(const BodyPtrs& b, JointPtrs j, int nJoints, PairPtrs cur, const int* npairs, int capacity, Topo t,
-                    int nBodies, unsigned long long* out3, cudaStream_t s);
+// collide.cu
+void launch_tick_begin(Tick t, Topo topo, const WorldDev* worlds, cudaStream_t s);
+void launch_grid_build(const BodyPtrs& b, const WorldDev* worlds, Tick t, Grid g, void* scanTemp, cudaStream_t s);
+void launch_pairs(const BodyPtrs& b, const WorldDev* worlds, Tick t, Grid g, NoCollide nc, const int* jbroken, int* pairCount,
+                  PairPtrs P, Counters* ctr, void* scanTemp, cudaStream_t s);
+void launch_narrowphase(const BodyPtrs& b, const WorldDev* worlds, Tick t, PairPtrs P, NarrowScratch ns, const Counters* ctr,
+                        int pairBudget, cudaStream_t s);
+
+// solve.cu
+void launch_joint_prepare(const BodyPtrs& b, JointPtrs j, int j0, int j1, cudaStream_t s);
+void launch_joint_warmstart(const BodyPtrs& b, const WorldDev* worlds, JointPtrs j, Tick t, cudaStream_t s);
+void launch_body_warmstart(const BodyPtrs& b, const WorldDev* worlds, Tick t, cudaStream_t s);
+void launch_adjacency(const BodyPtrs& b, JointPtrs j, PairPtrs P, Tick t, const Counters* ctr, Topo topo, int pairBudget,
+                      void* scanTemp, cudaStream_t s);
+void launch_coloring(const BodyPtrs& b, const WorldDev* worlds, JointPtrs j, PairPtrs P, Tick t, Topo topo, int rounds,
+                     Counters* ctr, cudaStream_t s);
+// Per tick, before the counter readback: per-body manifold-contact item counts, their scan and
+// the per-colour item totals. After the readback (with itemRef/contrib large enough): fill.
+void launch_items_count(PairPtrs P, Tick t, Topo topo, Counters* ctr, void* scanTemp, cudaStream_t s);
+void launch_items_fill(PairPtrs P, Tick t, Topo topo, const Counters* ctr, cudaStream_t s);
+void launch_primal(const BodyPtrs& b, const WorldDev* worlds, JointPtrs j, PairPtrs P, Tick t, Topo topo, const Counters* ctr,
+                   int color, int iteration, int nBodiesColor, int nItemsColor, cudaStream_t s);
+void launch_dual(const BodyPtrs& b, const WorldDev* worlds, JointPtrs j, PairPtrs P, Tick t, const Counters* ctr, int pairBudget,
+                 int iteration, cudaStream_t s);
+void launch_velocities(const BodyPtrs& b, const WorldDev* worlds, Tick t, cudaStream_t s);
+void launch_tick_end(Tick t, cudaStream_t s);
+void launch_count_active(JointPtrs j, PairPtrs P, const int* slots, int nSlots, const int* joints, int nJoints, Counters* out,
+                         cudaStream_t s);
+
+// Algorithmic bytes of one tick's kernels from its live counts (the bytes each kernel must
+// move at minimum; see launch_traffic): out3 = {primal per iteration, dual per iteration, collision}.
+void launch_traffic(const BodyPtrs& b, JointPtrs j, PairPtrs P, Tick t, Topo topo, const Counters* ctr, int pairBudget,
+                    unsigned long long* out3, cudaStream_t s);
 
 }  // namespace avbd
