@@ -47,6 +47,17 @@ class Profile(C.Structure):
                 ("bytes_primal", C.c_double), ("bytes_dual", C.c_double), ("bytes_collide", C.c_double)]
 
 
+class ServerDesc(C.Structure):
+    _fields_ = [("budget_bytes", C.c_int64), ("initial_bodies", C.c_int32), ("initial_worlds", C.c_int32)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [(k, C.c_int64) for k in (
+        "budget_bytes", "device_bytes", "peak_device_bytes", "live_worlds", "resident_worlds",
+        "evicted_worlds", "pending_worlds", "resident_bodies", "admitted", "rejected", "evictions",
+        "restores", "ticks", "body_steps", "completed")]
+
+
 # (name, restype, argtypes); every function returns int status unless noted
 SIGNATURES = [
     ("avbd_last_error", C.c_char_p, []),
@@ -81,6 +92,18 @@ SIGNATURES = [
     ("avbd_world_profile_read", C.c_int, [C.c_void_p, C.POINTER(Profile)]),
     ("avbd_batch_profile", C.c_int, [C.c_void_p, C.c_int32]),
     ("avbd_batch_profile_read", C.c_int, [C.c_void_p, C.POINTER(Profile)]),
+    ("avbd_server_create", C.c_int, [C.c_void_p, C.POINTER(ServerDesc), C.POINTER(C.c_void_p)]),
+    ("avbd_server_destroy", C.c_int, [C.c_void_p]),
+    ("avbd_server_admit", C.c_int, [C.c_void_p, C.POINTER(SceneDesc), C.POINTER(Params), _i64p]),
+    ("avbd_server_advance", C.c_int, [C.c_void_p, C.c_int64, C.c_int32, _i64p]),
+    ("avbd_server_tick", C.c_int, [C.c_void_p, _ip]),
+    ("avbd_server_completed", C.c_int, [C.c_void_p, _i64p, C.c_int32, _ip]),
+    ("avbd_server_read_poses", C.c_int, [C.c_void_p, _i64p, C.c_int32, _fp]),
+    ("avbd_server_read_state", C.c_int, [C.c_void_p, C.c_int64, _fp, _fp, _fp, _fp, _fp]),
+    ("avbd_server_world_info", C.c_int, [C.c_void_p, C.c_int64, _ip, _i64p, _i64p, _ip]),
+    ("avbd_server_evict", C.c_int, [C.c_void_p, C.c_int64]),
+    ("avbd_server_release", C.c_int, [C.c_void_p, C.c_int64]),
+    ("avbd_server_read_stats", C.c_int, [C.c_void_p, C.POINTER(ServerStats)]),
 ]
 
 # include/avbd_gb300.h

@@ -70,6 +70,15 @@ class SolverPipeline:
         self._children.append(b)
         return b
 
+    def createServer(self, budgetBytes: int, initialBodies: int = 0, initialWorlds: int = 0) -> "Server":
+        """A world server holding at most ``budgetBytes`` of device memory (see ``Server``)."""
+        self._live()
+        if not (isinstance(budgetBytes, (int, np.integer)) and budgetBytes > 0):
+            raise ValueError("budgetBytes must be a positive integer")
+        s = Server(self, int(budgetBytes), int(initialBodies), int(initialWorlds))
+        self._children.append(s)
+        return s
+
     def destroy(self):
         if self._h is None:
             return
@@ -334,6 +343,118 @@ class Batch:
         if self._h is None:
             return
         L.check(L.lib().avbd_batch_destroy(self._h))
+        self._h = None
+        if self in self._pipe._children:
+            self._pipe._children.remove(self)
+
+
+class Server:
+    """Continuous batching of many worlds (``avbd_server_*``).
+
+    ``admit(scene)`` returns a world id; ``advance(id, k)`` queues k steps and returns a ticket;
+    each ``tick()`` steps every world with queued steps once, in one launch sequence, and
+    ``completed()`` lists the tickets whose steps have all run. Worlds that do not fit in the
+    device budget evict the least recently used idle worlds to host memory; evicted worlds are
+    restored when work for them arrives. Results equal those of the same world stepped alone.
+    """
+
+    def __init__(self, pipe: SolverPipeline, budget: int, initial_bodies: int, initial_worlds: int):
+        self._pipe = pipe
+        h = C.c_void_p()
+        desc = L.ServerDesc(budget, initial_bodies, initial_worlds)
+        L.check(L.lib().avbd_server_create(pipe._h, C.byref(desc), C.byref(h)))
+        self._h = h
+        self._counts = {}
+        self._packed = None
+
+    def _live(self):
+        if self._h is None:
+            raise RuntimeError("The server has been destroyed")
+
+    def admit(self, scene) -> int:
+        """Admit a world; raises ``AvbdError`` (code ``AVBD_E_CAPACITY``) if it cannot fit."""
+        self._live()
+        packed = scene if isinstance(scene, L.PackedScene) else L.PackedScene(_arrays(scene))
+        wid = C.c_int64()
+        L.check(L.lib().avbd_server_admit(self._h, C.byref(packed.desc), C.byref(packed.params), C.byref(wid)))
+        self._counts[wid.value] = packed.n_bodies
+        return wid.value
+
+    def advance(self, world: int, steps: int = 1) -> int:
+        self._live()
+        if steps < 0:
+            raise ValueError("steps must be non-negative")
+        t = C.c_int64()
+        L.check(L.lib().avbd_server_advance(self._h, int(world), int(steps), C.byref(t)))
+        return t.value
+
+    def tick(self) -> int:
+        """One step of every world with queued steps; returns how many worlds were stepped."""
+        self._live()
+        n = C.c_int32()
+        L.check(L.lib().avbd_server_tick(self._h, C.byref(n)))
+        return n.value
+
+    def completed(self, cap: int = 65536) -> list:
+        self._live()
+        out = np.zeros(max(int(cap), 1), dtype=np.int64)
+        n = C.c_int32()
+        done = []
+        while True:
+            L.check(L.lib().avbd_server_completed(self._h, out.ctypes.data_as(L._i64p), out.size, C.byref(n)))
+            done.extend(int(x) for x in out[:n.value])
+            if n.value < out.size:
+                return done
+
+    def readPoses(self, worlds) -> np.ndarray:
+        """Poses of every body of the listed worlds, world after world: (bodies, 8) float32."""
+        self._live()
+        ids = np.ascontiguousarray(np.asarray(worlds, dtype=np.int64).reshape(-1))
+        for w in ids:
+            if int(w) not in self._counts:
+                raise ValueError(f"no such world {int(w)}")
+        total = int(sum(self._counts[int(w)] for w in ids))
+        out = np.zeros((total, 8), dtype=np.float32)
+        L.check(L.lib().avbd_server_read_poses(self._h, ids.ctypes.data_as(L._i64p), ids.size, L.fptr(out)))
+        return out
+
+    def readBodyState(self, world: int) -> dict:
+        self._live()
+        n = self._counts.get(int(world))
+        if n is None:
+            raise ValueError(f"no such world {world}")
+        out = {k: np.zeros((n, 4 if k == "rotation" else 3), dtype=np.float32)
+               for k in ("position", "rotation", "velocity", "angular", "prev_velocity")}
+        L.check(L.lib().avbd_server_read_state(self._h, int(world), *(L.fptr(out[k]) for k in
+                                                                       ("position", "rotation", "velocity", "angular", "prev_velocity"))))
+        return out
+
+    def info(self, world: int) -> dict:
+        self._live()
+        nb, res = C.c_int32(), C.c_int32()
+        q, d = C.c_int64(), C.c_int64()
+        L.check(L.lib().avbd_server_world_info(self._h, int(world), C.byref(nb), C.byref(q), C.byref(d), C.byref(res)))
+        return {"bodies": nb.value, "queued": q.value, "steps": d.value, "resident": bool(res.value)}
+
+    def evict(self, world: int):
+        self._live()
+        L.check(L.lib().avbd_server_evict(self._h, int(world)))
+
+    def release(self, world: int):
+        self._live()
+        L.check(L.lib().avbd_server_release(self._h, int(world)))
+        self._counts.pop(int(world), None)
+
+    def stats(self) -> dict:
+        self._live()
+        st = L.ServerStats()
+        L.check(L.lib().avbd_server_read_stats(self._h, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in L.ServerStats._fields_}
+
+    def destroy(self):
+        if self._h is None:
+            return
+        L.check(L.lib().avbd_server_destroy(self._h))
         self._h = None
         if self in self._pipe._children:
             self._pipe._children.remove(self)

@@ -209,3 +209,27 @@ def cloth_wall(seed=SEED_BASE + 2, grid=256, wall=(100, 2, 50)) -> SceneArrays:
                 ra=np.array(ra, np.float64), rb=np.array(rb, np.float64), p0=np.full(m, INF),
                 p1=np.zeros(m), p2=np.full(m, INF))
     return _arrays(b, params(15), cons)
+
+
+def request_stream(n_requests=20_000, rate=10_000.0, seed=SEED_BASE + 4, warm_creates=256, create_share=0.1,
+                   median=256, lo=16, hi=65_536, sigma=1.2078):
+    """A serving request stream: Poisson arrivals at `rate` per second; each request creates a
+    world (log-normal body count with the given median and sigma, clipped to [lo, hi]; a box and
+    sphere pile as in the world mix) or advances a uniformly chosen earlier world by K in
+    {1, 4, 16} steps. The first `warm_creates` requests are creates, then creates make up
+    `create_share` of the requests. Returns a dict of arrays in arrival order."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    arrival = np.cumsum(rng.exponential(1.0 / rate, n_requests))
+    create = rng.random(n_requests) < create_share
+    create[:warm_creates] = True
+    z = rng.standard_normal(n_requests)
+    counts = np.clip(np.rint(median * np.exp(sigma * z)), lo, hi).astype(np.int64)
+    steps = rng.choice(np.array([1, 4, 16]), size=n_requests)
+    u = rng.random(n_requests)
+    made = np.cumsum(create) - create  # worlds created before each request
+    target = np.where(create, -1, np.minimum((u * made).astype(np.int64), np.maximum(made - 1, 0)))
+    counts = np.where(create, counts, 0)
+    steps = np.where(create, 0, steps)
+    world_seed = (seed * 7919 + np.arange(n_requests)) & 0xFFFFFFFFFFFF
+    return {"arrival": arrival, "create": create, "count": counts, "steps": steps, "target": target,
+            "world_seed": world_seed, "sigma": sigma, "rate": rate, "seed": seed}

@@ -28,6 +28,7 @@ UNITS = {
     "collide.cu": ["-fmad=false"],
     "solve.cu": ["-fmad=false"],
     "engine.cu": ["-fmad=false"],
+    "server.cu": [],
 }
 
 

@@ -1,0 +1,1202 @@
+// The world arena: device arrays holding many worlds as self-contained segments, and the host
+// logic that adds, steps, evicts and restores them. Shared by the world/batch ABI (engine.cu)
+// and the server ABI (server.cu).
+//
+// An Arena holds worlds as self-contained segments of one set of device arrays (engine.cuh):
+// a body range, a joint range and a pair-slot region per world, with range allocators on the
+// host. A tick advances any subset of the resident worlds by one step, in one launch sequence
+// over the bodies, joints and pairs of those worlds only:
+//
+//   collision   active lists -> grid -> pair count / scan / write into each world's region ->
+//               narrowphase (SAT classification, per-type contacts) with warm-start matching
+//   topology    constraint lists (CSR, sorted) -> Jones-Plassmann colouring -> buckets -> items
+//   [one counter readback: pair-region overflow, colour sizes, work items]
+//   solve       joint warm start -> body warm start -> iterations x (colours + dual) -> velocities
+//
+// Everything before the readback writes only the buffers the tick is filling (pairs, contacts,
+// colours, lists); each world's previous state stays in the buffer named by which[w] until the
+// tick completes. When a world's pair region overflows, the region grows and the tick re-runs
+// from the same state, so capacities never alter a result. A world evolves the same way alone,
+// in a batch, or parked between requests of a server, and can be evicted to host memory and
+// restored exactly. The reference's counterpart is one WebGPU submission per world and step
+// (src/gpu/gpuSolverStep.js:16-256).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <functional>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <new>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/avbd_gb300.h"
+#include "engine.cuh"
+
+using namespace avbd;
+
+namespace avbd {
+
+// Message of the last failed ABI call on this thread (avbd_last_error).
+void set_error(const std::string& message);
+
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+#define CK(call)                                                                                          \
+  do {                                                                                                    \
+    cudaError_t e_ = (call);                                                                              \
+    if (e_ != cudaSuccess) throw Error(AVBD_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+template <class T> inline T* dalloc(size_t n) {
+  void* p = nullptr;
+  if (n == 0) n = 1;
+  cudaError_t e = cudaMalloc(&p, n * sizeof(T));
+  if (e != cudaSuccess) throw Error(AVBD_E_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  return static_cast<T*>(p);
+}
+
+inline void dfree(void* p) {
+  if (p) cudaFree(p);
+}
+
+// First-fit allocator of index ranges [0, cap).
+struct RangeAlloc {
+  int cap = 0;
+  std::map<int, int> freeRanges;  // start -> length
+  void init(int c) {
+    cap = c;
+    freeRanges.clear();
+    if (c > 0) freeRanges[0] = c;
+  }
+  int find(int n) const {
+    if (n == 0) return 0;
+    for (auto& f : freeRanges)
+      if (f.second >= n) return f.first;
+    return -1;
+  }
+  int alloc(int n) {
+    if (n == 0) return 0;
+    for (auto it = freeRanges.begin(); it != freeRanges.end(); ++it) {
+      if (it->second < n) continue;
+      const int start = it->first, len = it->second;
+      freeRanges.erase(it);
+      if (len > n) freeRanges[start + n] = len - n;
+      return start;
+    }
+    return -1;
+  }
+  void release(int start, int n) {
+    if (n <= 0) return;
+    auto it = freeRanges.emplace(start, n).first;
+    auto next = std::next(it);
+    if (next != freeRanges.end() && it->first + it->second == next->first) {
+      it->second += next->second;
+      freeRanges.erase(next);
+    }
+    if (it != freeRanges.begin()) {
+      auto prev = std::prev(it);
+      if (prev->first + prev->second == it->first) {
+        prev->second += it->second;
+        freeRanges.erase(it);
+      }
+    }
+  }
+  void grow(int newCap) {
+    if (newCap <= cap) return;
+    const int old = cap;
+    cap = newCap;
+    release(old, newCap - old);
+  }
+};
+
+}  // namespace avbd
+
+struct avbd_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<void*> owned;  // Arenas created under this context
+};
+
+namespace avbd {
+
+// World state kept on the host while a world is evicted (all indices world-local).
+struct Snapshot {
+  std::vector<float4> body[11];  // pos rot pos0 rot0 posY rotY vel ang vprev size mass
+  std::vector<int4> meta;
+  std::vector<int2> jab;
+  std::vector<float4> joint[10];  // rA rB stiff penLin penAng lamLin lamAng C0Lin C0Ang restQ
+  std::vector<int> jbroken;
+  std::vector<int> colors;
+  std::vector<uint2> pairs;
+  std::vector<int> counts;
+  std::vector<float4> basis, ct;
+};
+
+struct WorldRec {
+  bool live = false, resident = false;
+  WorldDev dev{};
+  int nBodies = 0, nJoints = 0;
+  int which = 0;
+  std::vector<std::pair<unsigned long long, int>> nc;  // local (hi << 32 | lo) -> local joint id or -1
+  std::vector<int> largeLocal;
+  long long pending = 0;
+  unsigned long long lastUse = 0;
+  std::unique_ptr<Snapshot> snap;
+};
+
+class Arena {
+ public:
+  avbd_ctx* ctx;
+  cudaStream_t s;
+  int bodyCap = 0, jointCap = 0, slotCap = 0, maxWorlds = 0;
+  RangeAlloc bodyA, jointA, slotA;
+  std::vector<int> freeSlots;
+  std::vector<WorldRec> W;
+  // device
+  WorldDev* worlds = nullptr;
+  BodyPtrs B{};
+  JointPtrs J{};
+  PairPtrs P{};
+  Grid G{};
+  NarrowScratch NS{};
+  NoCollide NC{};
+  int ncCap = 0;
+  Topo T{};
+  int *which = nullptr, *pairN = nullptr, *wover = nullptr, *wactive = nullptr;
+  int4* active = nullptr;
+  int *activeBodies = nullptr, *activeJoints = nullptr, *activePairs = nullptr, *pairPrefix = nullptr, *pairCount = nullptr;
+  Counters* ctr = nullptr;
+  Counters* ctrHost = nullptr;
+  int4* activeHost = nullptr;
+  int* wactiveHost = nullptr;
+  void* scanTemp = nullptr;
+  size_t scanBytes = 0;
+  size_t itemCap = 0;
+  int rounds = 64;
+  // the last tick (its lists stay valid until the next tick)
+  std::vector<int> lastActive;
+  int lastPairs = 0, lastJoints = 0;
+  long long steps = 0, regrowths = 0, evictions = 0, restores = 0;
+  bool haveStats = false;
+  // profiling: event pairs per kernel class, harvested after each tick's counter readback
+  enum { P_COLLIDE, P_TOPO, P_PRIMAL, P_DUAL, P_OTHER, P_CLASSES };
+  struct Rec {
+    int cls;
+    cudaEvent_t a, b;
+  };
+  bool prof = false;
+  std::vector<Rec> recs;
+  std::vector<cudaEvent_t> pool;
+  double profMs[P_CLASSES] = {0, 0, 0, 0, 0};
+  long long profPrimalLaunches = 0;
+  int profSteps = 0;
+  double profBytes[3] = {0, 0, 0};
+  unsigned long long* traffic = nullptr;  // device: primal, dual, collide bytes of one tick
+  float4* poseStage = nullptr;
+
+  // Called when a world's pair region must grow in a tick and the slot buffers cannot place
+  // `slots` more: an owner with a memory budget may free slot ranges (evicting worlds that are
+  // not being stepped) or grow the buffers itself; otherwise the buffers grow here.
+  std::function<void(int slots)> onSlotPressure;
+
+  // Host -> device uploads of world set-up go through one pinned staging buffer on the arena's
+  // stream (sources may be temporaries); flush() waits for them and recycles the buffer.
+  char* stage = nullptr;
+  size_t stageCap = 0, stageUsed = 0;
+
+  void put(void* dst, const void* src, size_t bytes) {
+    if (bytes == 0) return;
+    if (stageUsed + bytes > stageCap) {
+      flush();
+      if (bytes > stageCap) {
+        if (stage) cudaFreeHost(stage);
+        stage = nullptr;
+        stageCap = 0;
+        const size_t cap = std::max<size_t>(bytes, size_t(4) << 20);
+        CK(cudaHostAlloc((void**)&stage, cap, cudaHostAllocDefault));
+        stageCap = cap;
+      }
+    }
+    std::memcpy(stage + stageUsed, src, bytes);
+    CK(cudaMemcpyAsync(dst, stage + stageUsed, bytes, cudaMemcpyHostToDevice, s));
+    stageUsed += (bytes + 255) & ~size_t(255);
+  }
+  void flush() {
+    CK(cudaStreamSynchronize(s));
+    stageUsed = 0;
+  }
+  void get(void* dst, const void* src, size_t bytes) {
+    if (bytes == 0) return;
+    CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    stageUsed = 0;
+  }
+
+  Arena(avbd_ctx* c, int bodies, int joints, int slots, int worldsMax) : ctx(c), s(c->stream) {
+    allocate(std::max(bodies, 1), std::max(joints, 1), std::max(slots, 1024), std::max(worldsMax, 1));
+  }
+  ~Arena() {
+    cudaStreamSynchronize(s);
+    harvest();
+    for (cudaEvent_t e : pool) cudaEventDestroy(e);
+    release();
+  }
+
+  // ------------------------------------------------------------------ device memory
+  void allocate(int nb, int nj, int slots, int nw) {
+    bodyCap = nb;
+    jointCap = nj;
+    maxWorlds = nw;
+    bodyA.init(nb);
+    jointA.init(nj);
+    W.resize(nw);
+    for (int w = nw - 1; w >= 0; w--) freeSlots.push_back(w);
+    const size_t N = size_t(nb), NJ = size_t(nj);
+    for (float4** p : {&B.pos, &B.rot, &B.pos0, &B.rot0, &B.posY, &B.rotY, &B.vel, &B.ang, &B.vprev, &B.size, &B.mass})
+      *p = dalloc<float4>(N);
+    B.meta = dalloc<int4>(N);
+    J.ab = dalloc<int2>(NJ);
+    for (float4** p : {&J.rA, &J.rB, &J.stiff, &J.penLin, &J.penAng, &J.lamLin, &J.lamAng, &J.C0Lin, &J.C0Ang, &J.restQ})
+      *p = dalloc<float4>(NJ);
+    J.broken = dalloc<int>(NJ);
+    worlds = dalloc<WorldDev>(nw);
+    which = dalloc<int>(nw);
+    pairN = dalloc<int>(2 * size_t(nw));
+    wover = dalloc<int>(nw);
+    wactive = dalloc<int>(nw);
+    active = dalloc<int4>(nw);
+    CK(cudaMemset(which, 0, sizeof(int) * nw));
+    CK(cudaMemset(pairN, 0, sizeof(int) * 2 * nw));
+    CK(cudaMemset(wover, 0, sizeof(int) * nw));
+    CK(cudaMemset(wactive, 0xff, sizeof(int) * nw));
+    CK(cudaHostAlloc((void**)&activeHost, sizeof(int4) * nw, cudaHostAllocDefault));
+    CK(cudaHostAlloc((void**)&wactiveHost, sizeof(int) * nw, cudaHostAllocDefault));
+    for (int w = 0; w < nw; w++) wactiveHost[w] = -1;
+    activeBodies = dalloc<int>(N);
+    activeJoints = dalloc<int>(NJ);
+    pairPrefix = dalloc<int>(size_t(nw) + 1);
+    pairCount = dalloc<int>(N + 1);
+    uint32_t table = 1024;
+    while (table < 2u * uint32_t(N)) table <<= 1;
+    G.tableMask = table - 1;
+    G.cellCount = dalloc<int>(size_t(table) + 1);
+    G.cellFill = dalloc<int>(table);
+    G.cellBodies = dalloc<int>(N);
+    G.bodyBucket = dalloc<int>(N);
+    G.large = dalloc<int>(size_t(nw) * MAX_LARGE);
+    T.adjStart = dalloc<int>(N + 1);
+    T.adjFill = dalloc<int>(std::max<size_t>(N + 1, MAX_COLORS));
+    T.activeIndex = dalloc<int>(N);
+    T.color = dalloc<int>(2 * N);
+    T.won = dalloc<int>(N);
+    T.pending = dalloc<unsigned char>(N);
+    CK(cudaMemset(T.pending, 0, N));
+    T.colorBodies = dalloc<int>(N);
+    T.itemStart = dalloc<int>(N + 1);
+    ctr = dalloc<Counters>(1);
+    CK(cudaMemset(ctr, 0, sizeof(Counters)));
+    CK(cudaHostAlloc((void**)&ctrHost, sizeof(Counters), cudaHostAllocDefault));
+    std::memset(ctrHost, 0, sizeof(Counters));
+    NC.keys = dalloc<unsigned long long>(1);
+    NC.jid = dalloc<int>(1);
+    ncCap = 1;
+    slotCap = 0;
+    allocSlots(slots);
+  }
+
+  void release() {
+    void* ptrs[] = {B.pos, B.rot, B.pos0, B.rot0, B.posY, B.rotY, B.vel, B.ang, B.vprev, B.size, B.mass, B.meta, J.ab, J.rA,
+                    J.rB, J.stiff, J.penLin, J.penAng, J.lamLin, J.lamAng, J.C0Lin, J.C0Ang, J.restQ, J.broken, worlds,
+                    which, pairN, wover, wactive, active, activeBodies, activeJoints, pairPrefix, pairCount, G.cellCount,
+                    G.cellFill, G.cellBodies, G.bodyBucket, G.large, T.adjStart, T.adjFill, T.activeIndex, T.color, T.won,
+                    T.pending, T.colorBodies, T.itemStart, T.itemRef, T.contrib, ctr, NC.keys, NC.jid, scanTemp, traffic,
+                    poseStage, P.pair, P.count, P.basis, P.ct, NS.sat, NS.boxList, NS.sphereList, NS.ctr, activePairs,
+                    T.adjList};
+    for (void* p : ptrs) dfree(p);
+    if (ctrHost) cudaFreeHost(ctrHost);
+    if (activeHost) cudaFreeHost(activeHost);
+    if (wactiveHost) cudaFreeHost(wactiveHost);
+    if (stage) cudaFreeHost(stage);
+  }
+
+  // Pair-slot buffers (both halves) and everything sized by them; keeps existing regions.
+  void allocSlots(int cap) {
+    PairPtrs np;
+    np.pair = dalloc<uint2>(2 * size_t(cap));
+    np.count = dalloc<int>(2 * size_t(cap));
+    np.basis = dalloc<float4>(2 * size_t(cap) * 3);
+    np.ct = dalloc<float4>(2 * size_t(cap) * MAX_CONTACTS * 4);
+    if (slotCap > 0) {
+      for (int k = 0; k < 2; k++) {
+        const size_t o = size_t(k) * slotCap, n = size_t(k) * cap;
+        CK(cudaMemcpyAsync(np.pair + n, P.pair + o, size_t(slotCap) * sizeof(uint2), cudaMemcpyDeviceToDevice, s));
+        CK(cudaMemcpyAsync(np.count + n, P.count + o, size_t(slotCap) * sizeof(int), cudaMemcpyDeviceToDevice, s));
+        CK(cudaMemcpyAsync(np.basis + 3 * n, P.basis + 3 * o, size_t(slotCap) * 3 * sizeof(float4), cudaMemcpyDeviceToDevice, s));
+        CK(cudaMemcpyAsync(np.ct + 32 * n, P.ct + 32 * o, size_t(slotCap) * 32 * sizeof(float4), cudaMemcpyDeviceToDevice, s));
+      }
+      CK(cudaStreamSynchronize(s));
+    }
+    for (void* p : {(void*)P.pair, (void*)P.count, (void*)P.basis, (void*)P.ct, (void*)NS.sat, (void*)NS.boxList,
+                    (void*)NS.sphereList, (void*)NS.ctr, (void*)activePairs, (void*)T.adjList})
+      dfree(p);
+    P = np;
+    NS.sat = dalloc<float4>(cap);
+    NS.boxList = dalloc<int>(cap);
+    NS.sphereList = dalloc<int>(cap);
+    NS.ctr = dalloc<int>(2);
+    activePairs = dalloc<int>(cap);
+    T.adjList = dalloc<uint32_t>(2 * (size_t(jointCap) + size_t(cap)) + 1);
+    if (slotCap == 0) slotA.init(cap);
+    else slotA.grow(cap);
+    slotCap = cap;
+    lastPairs = 0;  // the last tick's pair list was in the buffers just replaced
+    size_t need = std::max(scan_temp_bytes(int(G.tableMask) + 2), scan_temp_bytes(bodyCap + 2));
+    need = std::max(need, scan_temp_bytes(maxWorlds + 2));
+    if (need > scanBytes) {
+      dfree(scanTemp);
+      scanTemp = dalloc<char>(need);
+      scanBytes = need;
+    }
+  }
+
+  // Growth keeps every world's ranges (offsets are unchanged; new capacity is appended).
+  template <class X> void regrow(X*& d, size_t keep, size_t m) {
+    X* n = dalloc<X>(m);
+    if (keep) CK(cudaMemcpyAsync(n, d, keep * sizeof(X), cudaMemcpyDeviceToDevice, s));
+    CK(cudaStreamSynchronize(s));
+    dfree(d);
+    d = n;
+  }
+  template <class X> void rescratch(X*& d, size_t m) {
+    dfree(d);
+    d = nullptr;
+    d = dalloc<X>(m);
+  }
+  void ensureScan() {
+    size_t need = std::max(scan_temp_bytes(int(G.tableMask) + 2), scan_temp_bytes(bodyCap + 2));
+    need = std::max(need, scan_temp_bytes(maxWorlds + 2));
+    if (need > scanBytes) {
+      rescratch(reinterpret_cast<char*&>(scanTemp), need);
+      scanBytes = need;
+    }
+  }
+
+  static uint32_t tableFor(size_t n) {
+    uint32_t table = 1024;
+    while (table < 2u * uint32_t(n)) table <<= 1;
+    return table;
+  }
+
+  void growBodies(int nb) {
+    if (nb <= bodyCap) return;
+    flush();
+    const size_t o = size_t(bodyCap), N = size_t(nb);
+    for (float4** p : {&B.pos, &B.rot, &B.pos0, &B.rot0, &B.posY, &B.rotY, &B.vel, &B.ang, &B.vprev, &B.size, &B.mass})
+      regrow(*p, o, N);
+    regrow(B.meta, o, N);
+    int* c = dalloc<int>(2 * N);  // both colour buffers, stride = capacity
+    CK(cudaMemcpyAsync(c, T.color, o * 4, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(c + N, T.color + o, o * 4, cudaMemcpyDeviceToDevice, s));
+    CK(cudaStreamSynchronize(s));
+    dfree(T.color);
+    T.color = c;
+    rescratch(T.pending, N);
+    CK(cudaMemset(T.pending, 0, N));
+    for (int** p : {&T.activeIndex, &T.won, &T.colorBodies, &activeBodies, &G.cellBodies, &G.bodyBucket}) rescratch(*p, N);
+    for (int** p : {&T.itemStart, &T.adjStart, &pairCount}) rescratch(*p, N + 1);
+    rescratch(T.adjFill, std::max<size_t>(N + 1, MAX_COLORS));
+    const uint32_t table = tableFor(N);
+    if (table != G.tableMask + 1) {
+      G.tableMask = table - 1;
+      rescratch(G.cellCount, size_t(table) + 1);
+      rescratch(G.cellFill, size_t(table));
+    }
+    bodyA.grow(nb);
+    bodyCap = nb;
+    ensureScan();
+  }
+
+  void growJoints(int nj) {
+    if (nj <= jointCap) return;
+    flush();
+    const size_t o = size_t(jointCap), N = size_t(nj);
+    regrow(J.ab, o, N);
+    for (float4** p : {&J.rA, &J.rB, &J.stiff, &J.penLin, &J.penAng, &J.lamLin, &J.lamAng, &J.C0Lin, &J.C0Ang, &J.restQ})
+      regrow(*p, o, N);
+    regrow(J.broken, o, N);
+    rescratch(activeJoints, N);
+    rescratch(T.adjList, 2 * (N + size_t(slotCap)) + 1);
+    jointA.grow(nj);
+    jointCap = nj;
+  }
+
+  void growWorlds(int nw) {
+    if (nw <= maxWorlds) return;
+    flush();
+    const size_t o = size_t(maxWorlds), N = size_t(nw);
+    regrow(worlds, o, N);
+    regrow(which, o, N);
+    regrow(wover, o, N);
+    CK(cudaMemset(which + o, 0, (N - o) * 4));
+    CK(cudaMemset(wover + o, 0, (N - o) * 4));
+    int* pn = dalloc<int>(2 * N);  // pairN: both buffers, stride = world capacity
+    CK(cudaMemset(pn, 0, 2 * N * 4));
+    CK(cudaMemcpyAsync(pn, pairN, o * 4, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(pn + N, pairN + o, o * 4, cudaMemcpyDeviceToDevice, s));
+    CK(cudaStreamSynchronize(s));
+    dfree(pairN);
+    pairN = pn;
+    regrow(G.large, o * MAX_LARGE, N * MAX_LARGE);
+    rescratch(wactive, N);
+    rescratch(active, N);
+    rescratch(pairPrefix, N + 1);
+    int4* ah = nullptr;
+    int* wh = nullptr;
+    CK(cudaHostAlloc((void**)&ah, sizeof(int4) * N, cudaHostAllocDefault));
+    CK(cudaHostAlloc((void**)&wh, sizeof(int) * N, cudaHostAllocDefault));
+    std::memcpy(wh, wactiveHost, o * 4);
+    for (size_t w = o; w < N; w++) wh[w] = -1;
+    cudaFreeHost(activeHost);
+    cudaFreeHost(wactiveHost);
+    activeHost = ah;
+    wactiveHost = wh;
+    W.resize(N);
+    for (int w = nw - 1; w >= int(o); w--) freeSlots.insert(freeSlots.begin(), w);
+    maxWorlds = nw;
+    ensureScan();
+  }
+
+  // Device bytes of an arena with these capacities: the arrays above and the pair-slot buffers.
+  // The per-tick work-item scratch (scratchBytes) comes on top; it grows with the contacts of
+  // the worlds being stepped (about 0.5 KB per body in settled piles, hence the reserve).
+  size_t scratchBytes() const { return itemCap * sizeof(int2) + size_t(T.contribCap) * 7 * sizeof(float4); }
+  static size_t scratchReserve(long long nb) { return size_t(nb) * 1024; }
+  size_t footprint(long long nb, long long nj, long long slots, long long nw) const {
+    const size_t perBody = 12 * 16 + 2 * 4 + 1 + 11 * 4;
+    const size_t perJoint = 8 + 10 * 16 + 4 + 4 + 8;
+    const size_t perSlot = 2 * (8 + 4 + 3 * 16 + MAX_CONTACTS * 64) + 16 + 3 * 4 + 8;
+    const size_t perWorld = sizeof(WorldDev) + 4 * 4 + 16 + 4 + MAX_LARGE * 4;
+    return size_t(nb) * perBody + size_t(tableFor(size_t(nb))) * 8 + size_t(nj) * perJoint + size_t(slots) * perSlot +
+           size_t(nw) * perWorld + size_t(ncCap) * 12 + scanBytes;
+  }
+  size_t deviceBytes() const { return footprint(bodyCap, jointCap, slotCap, maxWorlds) + scratchBytes(); }
+
+  // Capacities after making room for one more world of (nb, nj, slots): each array that cannot
+  // place it grows by at least half.
+  void plannedCaps(int nb, int nj, int slots, long long caps[4], bool minimal, bool newWorld = true) const {
+    auto next = [&](const RangeAlloc& a, int cap, int need) -> long long {
+      if (a.find(need) >= 0) return cap;
+      // the trailing free range (if any) merges with the growth
+      int tail = 0;
+      if (!a.freeRanges.empty()) {
+        auto last = std::prev(a.freeRanges.end());
+        if (last->first + last->second == a.cap) tail = last->second;
+      }
+      const long long exact = (long long)cap + (need - tail);
+      return minimal ? exact : std::max<long long>(exact, (long long)cap + cap / 2);
+    };
+    caps[0] = next(bodyA, bodyCap, nb);
+    caps[1] = next(jointA, jointCap, nj);
+    caps[2] = next(slotA, slotCap, slots);
+    caps[3] = newWorld && freeSlots.empty() ? (minimal ? maxWorlds + 1 : maxWorlds + std::max(16, maxWorlds / 2)) : maxWorlds;
+  }
+  void growTo(const long long caps[4]) {
+    if (caps[0] > 0x3fffffffLL || caps[2] > 0x3fffffffLL || caps[1] > 0x3fffffffLL) throw Error(AVBD_E_CAPACITY, "arena index space exhausted");
+    growBodies(int(caps[0]));
+    growJoints(int(caps[1]));
+    if (caps[2] > slotCap) allocSlots(int(caps[2]));
+    growWorlds(int(caps[3]));
+  }
+  // Make room for one more world (without a budget): grow what does not fit.
+  void ensureRoom(int nb, int nj, int slots, bool newWorld = true) {
+    long long caps[4];
+    plannedCaps(nb, nj, slots, caps, false, newWorld);
+    growTo(caps);
+  }
+
+  Tick tick(int nActive, int nb, int nj) {
+    Tick t;
+    t.active = active;
+    t.nActive = nActive;
+    t.wactive = wactive;
+    t.which = which;
+    t.bodies = activeBodies;
+    t.nBodies = nb;
+    t.joints = activeJoints;
+    t.nJoints = nj;
+    t.pairs = activePairs;
+    t.pairPrefix = pairPrefix;
+    t.pairN = pairN;
+    t.wover = wover;
+    t.maxWorlds = maxWorlds;
+    t.slotStride = slotCap;
+    t.bodyStride = bodyCap;
+    return t;
+  }
+
+  // ------------------------------------------------------------------ worlds
+  static void validate(const avbd_scene_desc& d, const avbd_params& p) {
+    if (d.n_bodies < 0 || d.n_cons < 0) throw Error(AVBD_E_INVALID, "negative body or constraint count");
+    if (d.n_bodies > 0 && (!d.position || !d.size || !d.mass || !d.moment || !d.friction || !d.radius || !d.shape))
+      throw Error(AVBD_E_INVALID, "scene is missing a required body array");
+    if (d.n_cons > 0 && (!d.cons_kind || !d.cons_a || !d.cons_b || !d.cons_ra || !d.cons_rb || !d.cons_p0 || !d.cons_p1 || !d.cons_p2))
+      throw Error(AVBD_E_INVALID, "scene is missing a required constraint array");
+    if (!(p.dt > 0.f) || !std::isfinite(p.dt)) throw Error(AVBD_E_INVALID, "timeStep must be positive");
+    if (p.iterations <= 0) throw Error(AVBD_E_INVALID, "iterations must be a positive integer");
+    if (!std::isfinite(p.gravity)) throw Error(AVBD_E_INVALID, "gravity must be finite");
+    for (int i = 0; i < d.n_bodies; i++) {
+      if (d.shape[i] != AVBD_SHAPE_BOX && d.shape[i] != AVBD_SHAPE_SPHERE) throw Error(AVBD_E_INVALID, "unknown body shape");
+      for (int k = 0; k < 3; k++) {
+        if (!std::isfinite(d.position[3 * i + k])) throw Error(AVBD_E_INVALID, "position must be finite");
+        if (!(d.size[3 * i + k] > 0.f)) throw Error(AVBD_E_INVALID, "size must be positive");
+      }
+    }
+    for (int c = 0; c < d.n_cons; c++) {
+      int k = d.cons_kind[c];
+      if (k != AVBD_CONS_JOINT && k != AVBD_CONS_SPRING && k != AVBD_CONS_IGNORE) throw Error(AVBD_E_INVALID, "unknown constraint kind");
+      int a = d.cons_a[c], b = d.cons_b[c];
+      if (b < 0 || b >= d.n_bodies || a < -1 || a >= d.n_bodies || a == b) throw Error(AVBD_E_INVALID, "constraint bodies out of range");
+      if (a < 0 && k != AVBD_CONS_JOINT) throw Error(AVBD_E_INVALID, "only joints may attach to the world");
+    }
+  }
+
+  static int jointsOf(const avbd_scene_desc& d) {
+    int nj = 0;
+    for (int c = 0; c < d.n_cons; c++) nj += d.cons_kind[c] != AVBD_CONS_IGNORE;
+    return nj;
+  }
+  static int initialPairCap(int n) { return 8 * n + 32; }
+
+  bool fits(int nb, int nj, int slots) const { return bodyA.find(nb) >= 0 && jointA.find(nj) >= 0 && slotA.find(slots) >= 0; }
+
+  // World parameters, large bodies (radius > 2 x median, at most 64) and the grid cell.
+  static void worldParams(const avbd_scene_desc& d, const avbd_params& p, WorldRec& R) {
+    WorldDev& Wd = R.dev;
+    std::memset(&Wd, 0, sizeof(Wd));
+    Wd.dt = p.dt;
+    Wd.gravity = p.gravity;
+    Wd.alpha = p.alpha;
+    Wd.gamma = p.gamma;
+    Wd.betaLin = p.beta_lin;
+    Wd.betaAng = p.beta_ang;
+    Wd.up0 = p.up[0];
+    Wd.up1 = p.up[1];
+    Wd.up2 = p.up[2];
+    Wd.iterations = p.iterations;
+    Wd.flags = (p.mass_penalty ? FLAG_MASS_PENALTY : 0) | (p.face_bias ? FLAG_FACE_BIAS : 0);
+    Wd.bodyCount = d.n_bodies;
+    R.largeLocal.clear();
+    float largeR = INFINITY;
+    if (d.n_bodies > 0) {
+      std::vector<float> sorted(d.radius, d.radius + d.n_bodies);
+      std::sort(sorted.begin(), sorted.end());
+      float thr = 2.f * sorted[sorted.size() / 2];
+      int nl = 0;
+      for (float r : sorted) nl += r > thr;
+      if (nl > MAX_LARGE) thr = sorted[sorted.size() - (MAX_LARGE + 1)];
+      float maxSmall = 0.f;
+      for (float r : sorted)
+        if (!(r > thr)) maxSmall = std::max(maxSmall, r);
+      largeR = thr;
+      Wd.cell = std::max(2.f * maxSmall * 1.001f, 1e-3f);
+      for (int i = 0; i < d.n_bodies; i++)
+        if (d.radius[i] > largeR) R.largeLocal.push_back(i);
+    } else {
+      Wd.cell = 1.f;
+    }
+    Wd.largeR = largeR;
+    Wd.largeCount = int(R.largeLocal.size());
+    R.nBodies = d.n_bodies;
+    R.nJoints = jointsOf(d);
+    Wd.jointCount = R.nJoints;
+    R.nc.clear();
+    int j = 0;
+    for (int c = 0; c < d.n_cons; c++) {
+      const int kind = d.cons_kind[c];
+      const int jid = kind != AVBD_CONS_IGNORE ? j++ : -1;
+      const int a = d.cons_a[c], b = d.cons_b[c];
+      if (a >= 0) R.nc.push_back({(unsigned long long)(uint32_t)std::max(a, b) << 32 | (uint32_t)std::min(a, b), jid});
+    }
+  }
+
+  int takeSlot() {
+    if (freeSlots.empty()) throw Error(AVBD_E_CAPACITY, "world table full");
+    int w = freeSlots.back();
+    freeSlots.pop_back();
+    return w;
+  }
+
+  void placeRanges(WorldRec& R, int slotsWanted) {
+    const int bo = bodyA.alloc(R.nBodies);
+    if (bo < 0) throw Error(AVBD_E_NOMEM, "body capacity of the arena exhausted");
+    const int jo = jointA.alloc(R.nJoints);
+    if (jo < 0) {
+      bodyA.release(bo, R.nBodies);
+      throw Error(AVBD_E_NOMEM, "joint capacity of the arena exhausted");
+    }
+    const int po = slotA.alloc(slotsWanted);
+    if (po < 0) {
+      bodyA.release(bo, R.nBodies);
+      jointA.release(jo, R.nJoints);
+      throw Error(AVBD_E_NOMEM, "pair-slot capacity of the arena exhausted");
+    }
+    R.dev.bodyOff = bo;
+    R.dev.jointOff = jo;
+    R.dev.pairOff = po;
+    R.dev.pairCap = slotsWanted;
+  }
+
+  void uploadWorldDev(int w) { put(worlds + w, &W[w].dev, sizeof(WorldDev)); }
+
+  void uploadLarge(int w) {
+    std::vector<int> L(MAX_LARGE, 0);
+    for (size_t k = 0; k < W[w].largeLocal.size(); k++) L[k] = W[w].dev.bodyOff + W[w].largeLocal[k];
+    put(G.large + size_t(w) * MAX_LARGE, L.data(), sizeof(int) * MAX_LARGE);
+  }
+
+  void rebuildNoCollide() {
+    std::vector<std::pair<unsigned long long, int>> all;
+    for (int w = 0; w < maxWorlds; w++) {
+      const WorldRec& R = W[w];
+      if (!R.live || !R.resident) continue;
+      const unsigned long long off = (unsigned long long)R.dev.bodyOff;
+      for (auto& e : R.nc) {
+        unsigned long long hi = (e.first >> 32) + off, lo = (e.first & 0xffffffffull) + off;
+        all.push_back({hi << 32 | lo, e.second >= 0 ? R.dev.jointOff + e.second : -1});
+      }
+    }
+    std::sort(all.begin(), all.end());
+    if (int(all.size()) > ncCap) {
+      dfree(NC.keys);
+      dfree(NC.jid);
+      NC.keys = nullptr;
+      NC.jid = nullptr;
+      ncCap = int(all.size()) + int(all.size()) / 2 + 16;
+      NC.keys = dalloc<unsigned long long>(ncCap);
+      NC.jid = dalloc<int>(ncCap);
+    }
+    NC.n = int(all.size());
+    if (!all.empty()) {
+      std::vector<unsigned long long> k(all.size());
+      std::vector<int> id(all.size());
+      for (size_t i = 0; i < all.size(); i++) { k[i] = all[i].first; id[i] = all[i].second; }
+      put(NC.keys, k.data(), k.size() * 8);
+      put(NC.jid, id.data(), id.size() * 4);
+    }
+  }
+
+  // Add a world (with rebuild = false, call rebuildNoCollide after a batch of additions).
+  int addWorld(const avbd_scene_desc& d, const avbd_params& p, bool rebuild = true) {
+    validate(d, p);
+    ensureRoom(d.n_bodies, jointsOf(d), initialPairCap(d.n_bodies));  // may move W: before any reference into it
+    const int w = takeSlot();
+    WorldRec& R = W[w];
+    try {
+      worldParams(d, p, R);
+      R.dev.largeOff = w * MAX_LARGE;
+      placeRanges(R, initialPairCap(d.n_bodies));
+    } catch (...) {
+      R = WorldRec();
+      freeSlots.push_back(w);
+      throw;
+    }
+    R.live = true;
+    R.resident = true;
+    R.which = 0;
+    R.pending = 0;
+    rounds = std::max(rounds, p.color_rounds > 0 ? p.color_rounds : 64);
+    // bodies
+    const size_t n = size_t(d.n_bodies), off = size_t(R.dev.bodyOff);
+    if (n) {
+      std::vector<float4> pos(n), rot(n), vel(n), ang(n), vprev(n), size(n), mass(n);
+      std::vector<int4> meta(n);
+      auto v3at = [&](const float* a, size_t k) { return a ? make_float4(a[3 * k], a[3 * k + 1], a[3 * k + 2], 0.f) : make_float4(0, 0, 0, 0); };
+      for (size_t i = 0; i < n; i++) {
+        pos[i] = v3at(d.position, i);
+        pos[i].w = d.radius[i];
+        rot[i] = d.rotation ? make_float4(d.rotation[4 * i], d.rotation[4 * i + 1], d.rotation[4 * i + 2], d.rotation[4 * i + 3])
+                            : make_float4(0, 0, 0, 1);
+        vel[i] = v3at(d.velocity, i);
+        ang[i] = v3at(d.angular_velocity, i);
+        vprev[i] = v3at(d.prev_velocity, i);
+        size[i] = v3at(d.size, i);
+        size[i].w = d.friction[i];
+        mass[i] = make_float4(d.mass[i], d.moment[3 * i], d.moment[3 * i + 1], d.moment[3 * i + 2]);
+        const uint32_t grp = d.group ? d.group[i] : 0xffffffffu, msk = d.collides_with ? d.collides_with[i] : 0xffffffffu;
+        meta[i] = make_int4(w, d.shape[i], int(grp), int(msk));
+      }
+      const float4* src[11] = {pos.data(), rot.data(), pos.data(), rot.data(), pos.data(), rot.data(), vel.data(), ang.data(),
+                               vprev.data(), size.data(), mass.data()};
+      float4* dst[11] = {B.pos, B.rot, B.pos0, B.rot0, B.posY, B.rotY, B.vel, B.ang, B.vprev, B.size, B.mass};
+      for (int k = 0; k < 11; k++) put(dst[k] + off, src[k], n * 16);
+      put(B.meta + off, meta.data(), n * 16);
+      std::vector<int> minus(n, -1);
+      put(T.color + off, minus.data(), n * 4);
+      put(T.color + bodyCap + off, minus.data(), n * 4);
+    }
+    // joints and springs (global body ids)
+    const size_t nj = size_t(R.nJoints), joff = size_t(R.dev.jointOff);
+    if (nj) {
+      std::vector<int2> jab(nj);
+      std::vector<float4> jra(nj), jrb(nj), jst(nj), jz(nj, make_float4(0, 0, 0, 0)), jq(nj, make_float4(0, 0, 0, 1));
+      std::vector<int> jbr(nj, 0);
+      size_t j = 0;
+      for (int c = 0; c < d.n_cons; c++) {
+        const int kind = d.cons_kind[c];
+        if (kind == AVBD_CONS_IGNORE) continue;
+        const int a = d.cons_a[c] >= 0 ? int(off) + d.cons_a[c] : -1;
+        const int b = int(off) + d.cons_b[c];
+        jab[j] = make_int2(a, b);
+        int kk = kind == AVBD_CONS_JOINT ? KIND_JOINT : KIND_SPRING;
+        float kf;
+        std::memcpy(&kf, &kk, 4);
+        jra[j] = make_float4(d.cons_ra[3 * c], d.cons_ra[3 * c + 1], d.cons_ra[3 * c + 2], kf);
+        jrb[j] = make_float4(d.cons_rb[3 * c], d.cons_rb[3 * c + 1], d.cons_rb[3 * c + 2], kind == AVBD_CONS_SPRING ? d.cons_p1[c] : 0.f);
+        jst[j] = kind == AVBD_CONS_JOINT ? make_float4(d.cons_p0[c], d.cons_p1[c], d.cons_p2[c], 0.f)
+                                         : make_float4(d.cons_p0[c], 0.f, INFINITY, 0.f);
+        j++;
+      }
+      put(J.ab + joff, jab.data(), nj * 8);
+      put(J.rA + joff, jra.data(), nj * 16);
+      put(J.rB + joff, jrb.data(), nj * 16);
+      put(J.stiff + joff, jst.data(), nj * 16);
+      for (float4* q : {J.penLin, J.penAng, J.lamLin, J.lamAng, J.C0Lin, J.C0Ang}) put(q + joff, jz.data(), nj * 16);
+      put(J.restQ + joff, jq.data(), nj * 16);
+      put(J.broken + joff, jbr.data(), nj * 4);
+    }
+    const int zero = 0;
+    put(which + w, &zero, 4);
+    put(pairN + w, &zero, 4);
+    put(pairN + maxWorlds + w, &zero, 4);
+    put(wover + w, &zero, 4);
+    uploadLarge(w);
+    uploadWorldDev(w);
+    launch_joint_prepare(B, J, R.dev.jointOff, R.dev.jointOff + R.nJoints, s);
+    if (rebuild) rebuildNoCollide();
+    flush();
+    return w;
+  }
+
+  void freeRanges(WorldRec& R) {
+    bodyA.release(R.dev.bodyOff, R.nBodies);
+    jointA.release(R.dev.jointOff, R.nJoints);
+    slotA.release(R.dev.pairOff, R.dev.pairCap);
+  }
+
+  void removeWorld(int w) {
+    if (w < 0 || w >= maxWorlds || !W[w].live) throw Error(AVBD_E_INVALID, "no such world");
+    CK(cudaStreamSynchronize(s));
+    WorldRec& R = W[w];
+    if (R.resident) freeRanges(R);
+    R = WorldRec();
+    freeSlots.push_back(w);
+    rebuildNoCollide();
+    flush();
+  }
+
+  template <class X> void getRange(std::vector<X>& out, const X* d, size_t off, size_t n) {
+    out.resize(n);
+    get(out.data(), d + off, n * sizeof(X));
+  }
+  template <class X> void putRange(X* d, size_t off, const std::vector<X>& in) {
+    put(d + off, in.data(), in.size() * sizeof(X));
+  }
+
+  int prevPairs(int w) {
+    int n = 0;
+    get(&n, pairN + size_t(W[w].which) * maxWorlds + w, 4);
+    return n;
+  }
+
+  // Move a resident world's state to host memory and free its ranges.
+  void evict(int w) {
+    WorldRec& R = W[w];
+    if (!R.live || !R.resident) throw Error(AVBD_E_INVALID, "world is not resident");
+    CK(cudaStreamSynchronize(s));
+    auto S = std::make_unique<Snapshot>();
+    const size_t off = R.dev.bodyOff, n = R.nBodies, joff = R.dev.jointOff, nj = R.nJoints;
+    const float4* bsrc[11] = {B.pos, B.rot, B.pos0, B.rot0, B.posY, B.rotY, B.vel, B.ang, B.vprev, B.size, B.mass};
+    for (int k = 0; k < 11; k++) getRange(S->body[k], bsrc[k], off, n);
+    getRange(S->meta, B.meta, off, n);
+    getRange(S->jab, J.ab, joff, nj);
+    for (auto& ab : S->jab) {
+      if (ab.x >= 0) ab.x -= int(off);
+      ab.y -= int(off);
+    }
+    const float4* jsrc[10] = {J.rA, J.rB, J.stiff, J.penLin, J.penAng, J.lamLin, J.lamAng, J.C0Lin, J.C0Ang, J.restQ};
+    for (int k = 0; k < 10; k++) getRange(S->joint[k], jsrc[k], joff, nj);
+    getRange(S->jbroken, J.broken, joff, nj);
+    getRange(S->colors, T.color, size_t(R.which) * bodyCap + off, n);
+    const int np = prevPairs(w);
+    const size_t base = size_t(R.which) * slotCap + R.dev.pairOff;
+    getRange(S->pairs, P.pair, base, np);
+    for (auto& pr : S->pairs) {
+      pr.x -= uint32_t(off);
+      pr.y -= uint32_t(off);
+    }
+    getRange(S->counts, P.count, base, np);
+    getRange(S->basis, P.basis, 3 * base, 3 * size_t(np));
+    getRange(S->ct, P.ct, 32 * base, 32 * size_t(np));
+    freeRanges(R);
+    R.resident = false;
+    R.snap = std::move(S);
+    evictions++;
+    rebuildNoCollide();
+    flush();
+  }
+
+  // Bring an evicted world back (into any free ranges); its state continues exactly.
+  int restoreSlots(int w) const {
+    const int np = int(W[w].snap->pairs.size());
+    return std::max(initialPairCap(W[w].nBodies), np + np / 4 + 64);
+  }
+  void restore(int w) {
+    if (w < 0 || w >= maxWorlds || !W[w].live || W[w].resident || !W[w].snap) throw Error(AVBD_E_INVALID, "world is not evicted");
+    ensureRoom(W[w].nBodies, W[w].nJoints, restoreSlots(w), false);  // may move W: before any reference into it
+    WorldRec& R = W[w];
+    Snapshot& S = *R.snap;
+    const int np = int(S.pairs.size());
+    placeRanges(R, restoreSlots(w));
+    const size_t off = R.dev.bodyOff, joff = R.dev.jointOff;
+    float4* bdst[11] = {B.pos, B.rot, B.pos0, B.rot0, B.posY, B.rotY, B.vel, B.ang, B.vprev, B.size, B.mass};
+    for (int k = 0; k < 11; k++) putRange(bdst[k], off, S.body[k]);
+    putRange(B.meta, off, S.meta);
+    for (auto& ab : S.jab) {
+      if (ab.x >= 0) ab.x += int(off);
+      ab.y += int(off);
+    }
+    putRange(J.ab, joff, S.jab);
+    float4* jdst[10] = {J.rA, J.rB, J.stiff, J.penLin, J.penAng, J.lamLin, J.lamAng, J.C0Lin, J.C0Ang, J.restQ};
+    for (int k = 0; k < 10; k++) putRange(jdst[k], joff, S.joint[k]);
+    putRange(J.broken, joff, S.jbroken);
+    putRange(T.color, off, S.colors);
+    for (auto& pr : S.pairs) {
+      pr.x += uint32_t(off);
+      pr.y += uint32_t(off);
+    }
+    const size_t base = R.dev.pairOff;  // buffer 0
+    putRange(P.pair, base, S.pairs);
+    putRange(P.count, base, S.counts);
+    putRange(P.basis, 3 * base, S.basis);
+    putRange(P.ct, 32 * base, S.ct);
+    R.which = 0;
+    const int zero = 0;
+    put(which + w, &zero, 4);
+    put(pairN + w, &np, 4);
+    put(pairN + maxWorlds + w, &zero, 4);
+    put(wover + w, &zero, 4);
+    uploadLarge(w);
+    uploadWorldDev(w);
+    R.resident = true;
+    R.snap.reset();
+    restores++;
+    rebuildNoCollide();
+    flush();
+  }
+
+  // A world's pair region overflowed: give it `need` slots (+25 %), keeping its previous state.
+  void growRegion(int w, int need) {
+    const int cap = need + need / 4 + 64;
+    int po = slotA.alloc(cap);
+    if (po < 0 && onSlotPressure) {
+      onSlotPressure(cap);
+      po = slotA.alloc(cap);
+    }
+    if (po < 0) {
+      allocSlots(std::max(slotCap + cap + 1024, slotCap + slotCap / 2));
+      po = slotA.alloc(cap);
+    }
+    WorldRec& R = W[w];
+    const int np = prevPairs(w);
+    const size_t k = size_t(R.which) * slotCap;
+    const size_t src = k + R.dev.pairOff, dst = k + po;
+    if (np) {
+      CK(cudaMemcpyAsync(P.pair + dst, P.pair + src, size_t(np) * sizeof(uint2), cudaMemcpyDeviceToDevice, s));
+      CK(cudaMemcpyAsync(P.count + dst, P.count + src, size_t(np) * sizeof(int), cudaMemcpyDeviceToDevice, s));
+      CK(cudaMemcpyAsync(P.basis + 3 * dst, P.basis + 3 * src, size_t(np) * 3 * sizeof(float4), cudaMemcpyDeviceToDevice, s));
+      CK(cudaMemcpyAsync(P.ct + 32 * dst, P.ct + 32 * src, size_t(np) * 32 * sizeof(float4), cudaMemcpyDeviceToDevice, s));
+    }
+    slotA.release(R.dev.pairOff, R.dev.pairCap);
+    R.dev.pairOff = po;
+    R.dev.pairCap = cap;
+    uploadWorldDev(w);
+    flush();
+    regrowths++;
+  }
+
+  // ------------------------------------------------------------------ profiling
+  cudaEvent_t event() {
+    if (!pool.empty()) {
+      cudaEvent_t e = pool.back();
+      pool.pop_back();
+      return e;
+    }
+    cudaEvent_t e;
+    CK(cudaEventCreate(&e));
+    return e;
+  }
+  cudaEvent_t mark() {
+    cudaEvent_t e = event();
+    CK(cudaEventRecord(e, s));
+    return e;
+  }
+  void span(int cls, cudaEvent_t a, cudaEvent_t b) { recs.push_back(Rec{cls, a, b}); }
+  void harvest() {
+    for (const Rec& r : recs) {
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess) profMs[r.cls] += ms;
+      pool.push_back(r.a);
+      pool.push_back(r.b);
+    }
+    recs.clear();
+  }
+  void profile(bool on) {
+    CK(cudaStreamSynchronize(s));
+    harvest();
+    prof = on;
+    for (double& v : profMs) v = 0;
+    for (double& v : profBytes) v = 0;
+    profPrimalLaunches = 0;
+    profSteps = 0;
+    if (!traffic) traffic = dalloc<unsigned long long>(3);
+  }
+  void profileRead(avbd_profile* o) {
+    CK(cudaStreamSynchronize(s));
+    harvest();
+    std::memset(o, 0, sizeof(*o));
+    o->steps = profSteps;
+    o->ms_collide = profMs[P_COLLIDE];
+    o->ms_topology = profMs[P_TOPO];
+    o->ms_primal = profMs[P_PRIMAL];
+    o->ms_dual = profMs[P_DUAL];
+    o->ms_other = profMs[P_OTHER];
+    o->primal_launches = profPrimalLaunches;
+    o->launches = launches_total();
+    o->bytes_primal = profBytes[0];
+    o->bytes_dual = profBytes[1];
+    o->bytes_collide = profBytes[2];
+  }
+
+  // ------------------------------------------------------------------ ticks
+  void ensureItems() {
+    const size_t need = size_t(std::max(ctrHost->itemsTotal, 1));
+    int maxColor = 1;
+    for (int c = 0; c < MAX_COLORS; c++) maxColor = std::max(maxColor, ctrHost->colorItems[c]);
+    if (need > itemCap) {
+      CK(cudaStreamSynchronize(s));
+      const size_t cap = need + need / 4 + 1024;
+      dfree(T.itemRef);
+      T.itemRef = nullptr;
+      T.itemRef = dalloc<int2>(cap);
+      itemCap = cap;
+    }
+    if (maxColor > T.contribCap) {
+      CK(cudaStreamSynchronize(s));
+      const int ccap = maxColor + maxColor / 4 + 1024;
+      dfree(T.contrib);
+      T.contrib = nullptr;
+      T.contrib = dalloc<float4>(size_t(ccap) * 7);
+      T.contribCap = ccap;
+    }
+  }
+
+  // One step of the given resident worlds.
+  void stepWorlds(std::vector<int> act) {
+    std::sort(act.begin(), act.end(), [&](int a, int b) { return W[a].dev.bodyOff < W[b].dev.bodyOff; });
+    act.erase(std::unique(act.begin(), act.end()), act.end());
+    for (int w : act)
+      if (w < 0 || w >= maxWorlds || !W[w].live || !W[w].resident) throw Error(AVBD_E_INVALID, "stepping a world that is not resident");
+    for (int w : lastActive) wactiveHost[w] = -1;
+    lastActive.clear();
+    int nb = 0, nj = 0, maxIter = 0;
+    for (size_t a = 0; a < act.size(); a++) {
+      const WorldRec& R = W[act[a]];
+      activeHost[a] = make_int4(act[a], nb, nj, 0);
+      wactiveHost[act[a]] = int(a);
+      nb += R.nBodies;
+      nj += R.nJoints;
+      maxIter = std::max(maxIter, R.dev.iterations);
+    }
+    const int na = int(act.size());
+    if (na) CK(cudaMemcpyAsync(active, activeHost, sizeof(int4) * na, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(wactive, wactiveHost, sizeof(int) * maxWorlds, cudaMemcpyHostToDevice, s));
+    lastActive = act;
+    long long budget = 0;
+    for (int attempt = 0;; attempt++) {
+      budget = 0;
+      for (int w : act) budget += W[w].dev.pairCap;
+      const int pairBudget = int(std::min<long long>(budget, slotCap));
+      Tick t = tick(na, nb, nj);
+      cudaEvent_t e0 = prof ? mark() : nullptr;
+      launch_tick_begin(t, T, worlds, s);
+      launch_grid_build(B, worlds, t, G, scanTemp, s);
+      launch_pairs(B, worlds, t, G, NC, J.broken, pairCount, P, ctr, scanTemp, s);
+      launch_narrowphase(B, worlds, t, P, NS, ctr, pairBudget, s);
+      // every span owns its two events (the pool recycles each event exactly once)
+      cudaEvent_t e1 = prof ? mark() : nullptr;
+      cudaEvent_t e1b = prof ? mark() : nullptr;
+      launch_adjacency(B, J, P, t, ctr, T, pairBudget, scanTemp, s);
+      launch_coloring(B, worlds, J, P, t, T, rounds, ctr, s);
+      launch_items_count(P, t, T, ctr, scanTemp, s);
+      if (prof) {
+        cudaEvent_t e2 = mark();
+        span(P_COLLIDE, e0, e1);
+        span(P_TOPO, e1b, e2);
+      }
+      CK(cudaMemcpyAsync(ctrHost, ctr, sizeof(Counters), cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+      CK(cudaGetLastError());
+      if (prof) harvest();
+      if (ctrHost->overflowWorlds == 0) break;
+      if (attempt > 8) throw Error(AVBD_E_CAPACITY, "pair regions did not converge");
+      std::vector<int> over(maxWorlds);
+      get(over.data(), wover, sizeof(int) * maxWorlds);
+      for (int w : act)
+        if (over[w] > 0) {
+          growRegion(w, over[w]);
+          const int zero = 0;
+          put(wover + w, &zero, 4);
+        }
+    }
+    const int pairBudget = int(std::min<long long>(budget, slotCap));
+    Tick t = tick(na, nb, nj);
+    ensureItems();
+    launch_items_fill(P, t, T, ctr, s);
+    cudaEvent_t o0 = prof ? mark() : nullptr;
+    launch_joint_warmstart(B, worlds, J, t, s);
+    launch_body_warmstart(B, worlds, t, s);
+    if (prof) span(P_OTHER, o0, mark());
+    const int ncolors = ctrHost->ncolors;
+    for (int it = 0; it < maxIter; it++) {
+      for (int c = 0; c < ncolors; c++) {
+        const int cnt = ctrHost->colorCount[c];
+        if (!cnt) continue;
+        cudaEvent_t a = prof ? mark() : nullptr;
+        launch_primal(B, worlds, J, P, t, T, ctr, c, it, cnt, ctrHost->colorItems[c], s);
+        if (prof) {
+          span(P_PRIMAL, a, mark());
+          profPrimalLaunches += ctrHost->colorItems[c] > 0 ? 2 : 1;
+        }
+      }
+      cudaEvent_t d = prof ? mark() : nullptr;
+      launch_dual(B, worlds, J, P, t, ctr, pairBudget, it, s);
+      if (prof) span(P_DUAL, d, mark());
+    }
+    cudaEvent_t v0 = prof ? mark() : nullptr;
+    launch_velocities(B, worlds, t, s);
+    if (prof) span(P_OTHER, v0, mark());
+    if (prof) {
+      CK(cudaMemsetAsync(traffic, 0, 3 * sizeof(unsigned long long), s));
+      launch_traffic(B, J, P, t, T, ctr, pairBudget, traffic, s);
+      unsigned long long tb[3];
+      CK(cudaMemcpyAsync(tb, traffic, sizeof(tb), cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+      profBytes[0] += double(tb[0]) * maxIter;
+      profBytes[1] += double(tb[1]) * maxIter;
+      profBytes[2] += double(tb[2]);
+      profSteps++;
+    }
+    launch_tick_end(t, s);
+    for (int w : act) W[w].which ^= 1;
+    lastPairs = ctrHost->activePairs;
+    lastJoints = nj;
+    steps++;
+    haveStats = false;
+    CK(cudaGetLastError());
+  }
+
+  // ------------------------------------------------------------------ reads
+  void syncStats() {
+    if (haveStats) return;
+    launch_count_active(J, P, activePairs, lastPairs, activeJoints, lastJoints, ctr, s);
+    CK(cudaMemcpyAsync(ctrHost, ctr, sizeof(Counters), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    haveStats = true;
+  }
+
+  void counters(avbd_counters* o) {
+    syncStats();
+    o->pairs = lastPairs;
+    o->manifolds = ctrHost->manifolds;
+    o->contacts = ctrHost->contacts;
+    o->joints = ctrHost->joints;
+    o->colors = ctrHost->ncolors;
+    o->conflicts = ctrHost->conflicts;
+    o->overflow = int32_t(regrowths);
+    o->steps = int32_t(steps);
+  }
+
+  template <class X> std::vector<X> fetch(const X* d, size_t off, size_t n) {
+    std::vector<X> h(n);
+    if (n) CK(cudaMemcpyAsync(h.data(), d + off, n * sizeof(X), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return h;
+  }
+
+  const WorldRec& resident(int w) const {
+    if (w < 0 || w >= maxWorlds || !W[w].live) throw Error(AVBD_E_INVALID, "no such world");
+    if (!W[w].resident) throw Error(AVBD_E_STATE, "world is evicted");
+    return W[w];
+  }
+
+  void readState(int w, float* position, float* rotation, float* velocity, float* angular, float* prevVel) {
+    const WorldRec& R = resident(w);
+    const size_t off = R.dev.bodyOff, n = R.nBodies;
+    auto put3 = [&](float* out, const float4* d) {
+      if (!out) return;
+      auto h = fetch(d, off, n);
+      for (size_t i = 0; i < n; i++) { out[3 * i] = h[i].x; out[3 * i + 1] = h[i].y; out[3 * i + 2] = h[i].z; }
+    };
+    put3(position, B.pos);
+    put3(velocity, B.vel);
+    put3(angular, B.ang);
+    put3(prevVel, B.vprev);
+    if (rotation) {
+      auto h = fetch(B.rot, off, n);
+      for (size_t i = 0; i < n; i++) { rotation[4 * i] = h[i].x; rotation[4 * i + 1] = h[i].y; rotation[4 * i + 2] = h[i].z; rotation[4 * i + 3] = h[i].w; }
+    }
+  }
+
+  // the world's pairs of its last completed step (its region in buffer which[w]); global ids
+  void lastPairsOf(int w, std::vector<uint2>& pairs, std::vector<int>* counts, std::vector<float4>* ct) {
+    const WorldRec& R = resident(w);
+    const int np = prevPairs(w);
+    const size_t base = size_t(R.which) * slotCap + R.dev.pairOff;
+    pairs = fetch(P.pair, base, np);
+    if (counts) *counts = fetch(P.count, base, np);
+    if (ct) *ct = fetch(P.ct, 32 * base, 32 * size_t(np));
+  }
+};
+
+}  // namespace avbd
+
+// ABI helpers: every entry point runs inside API_BEGIN/API_END, so no C++ exception crosses it.
+#define API_BEGIN try {
+#define API_END                                  \
+  }                                              \
+  catch (const avbd::Error& e) {                 \
+    avbd::set_error(e.what());                   \
+    return e.code;                               \
+  }                                              \
+  catch (const std::bad_alloc&) {                \
+    avbd::set_error("host allocation failed");   \
+    return AVBD_E_NOMEM;                         \
+  }                                              \
+  catch (const std::exception& e) {              \
+    avbd::set_error(e.what());                   \
+    return AVBD_E_STATE;                         \
+  }                                              \
+  return AVBD_OK;
+
+#define REQUIRE(cond, msg) \
+  if (!(cond)) throw avbd::Error(AVBD_E_INVALID, msg)

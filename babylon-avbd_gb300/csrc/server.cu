@@ -1,0 +1,434 @@
+// Serving entry points of the C ABI (avbd_server_*): continuous batching of many worlds over
+// one arena (arena.hpp), with admission under a device-memory budget and LRU eviction.
+//
+// A world's queued steps run one per tick; every tick steps all worlds that have queued steps,
+// in one launch sequence. Tickets record the step count at which an advance request is done.
+// When a world must be admitted or restored and the arena cannot place it, the arena grows
+// while its footprint stays within the budget; past that, idle worlds (nothing queued) are
+// evicted to host memory, least recently used first. Eviction and restoring move a world's
+// complete state (bodies, joints, carried colours, last contacts), so served results equal
+// those of a world stepped on its own.
+#include <deque>
+#include <set>
+#include <unordered_map>
+
+#include "arena.hpp"
+
+using namespace avbd;
+
+namespace {
+
+struct Ticket {
+  long long target;  // the world's step count at which the request is done
+  int64_t id;
+};
+
+struct Served {
+  int slot = -1;
+  int nBodies = 0;
+  long long queued = 0;
+  long long done = 0;
+  unsigned long long lastUse = 0;
+  std::deque<Ticket> tickets;
+};
+
+// Poses of listed resident worlds: seg = (first body, bodies, first output body, -), ascending
+// in the output position.
+__global__ void k_gather_poses(BodyPtrs bd, const int4* __restrict__ seg, int nseg, int total, float4* __restrict__ out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+    int a = 0, b = nseg;
+    while (b - a > 1) {
+      const int m = (a + b) >> 1;
+      if (seg[m].z <= i) a = m;
+      else b = m;
+    }
+    const int4 e = seg[a];
+    const int k = i - e.z;
+    if (k >= e.y) continue;  // output rows of evicted worlds (filled on the host)
+    const int body = e.x + k;
+    const float4 p = bd.pos[body];
+    out[2 * size_t(i)] = make_float4(p.x, p.y, p.z, bd.size[body].w);
+    out[2 * size_t(i) + 1] = bd.rot[body];
+  }
+}
+
+}  // namespace
+
+struct avbd_server {
+  avbd_ctx* ctx = nullptr;
+  Arena* A = nullptr;
+  int64_t budget = 0;
+  size_t peak = 0;
+  std::unordered_map<int64_t, Served> worlds;
+  std::set<int64_t> busy;  // worlds with queued steps
+  int64_t nextId = 1, nextTicket = 1;
+  unsigned long long clock = 0;
+  std::deque<int64_t> completed;
+  long long admitted = 0, rejected = 0, ticks = 0, bodySteps = 0, completedCount = 0;
+  int4* segDev = nullptr;
+  size_t segCap = 0;
+  float4* poseDev = nullptr;
+  size_t poseCap = 0;
+
+  // Bytes held against the budget: the arena's arrays, its work-item scratch (at least the
+  // reserve for its body capacity) and the pose-read buffers.
+  size_t accounted(long long nb, long long nj, long long slots, long long nw) const {
+    return A->footprint(nb, nj, slots, nw) + std::max(A->scratchBytes(), Arena::scratchReserve(nb)) + segCap * sizeof(int4) +
+           poseCap * 2 * sizeof(float4);
+  }
+  size_t deviceBytes() const { return accounted(A->bodyCap, A->jointCap, A->slotCap, A->maxWorlds); }
+  void notePeak() { peak = std::max(peak, deviceBytes()); }
+
+  Served& get(int64_t id) {
+    auto it = worlds.find(id);
+    if (it == worlds.end()) throw Error(AVBD_E_INVALID, "no such world");
+    return it->second;
+  }
+
+  // The least recently used resident world with nothing queued (other than `keepSlot`).
+  int lruIdle(int keepSlot) const {
+    int best = -1;
+    unsigned long long bestUse = ~0ull;
+    for (auto& kv : worlds) {
+      const Served& w = kv.second;
+      if (w.queued > 0 || w.slot == keepSlot || !A->W[w.slot].resident) continue;
+      if (w.lastUse < bestUse) {
+        bestUse = w.lastUse;
+        best = w.slot;
+      }
+    }
+    return best;
+  }
+
+  // Room for one world of (nb, nj, slots) (newWorld: and a world-table entry): grow within the
+  // budget, else evict idle worlds.
+  bool makeRoom(int nb, int nj, int slots, int keepSlot, bool newWorld = true) {
+    for (;;) {
+      if (A->fits(nb, nj, slots) && (!newWorld || !A->freeSlots.empty())) return true;
+      long long caps[4];
+      bool grown = false;
+      for (bool minimal : {false, true}) {
+        A->plannedCaps(nb, nj, slots, caps, minimal, newWorld);
+        if (accounted(caps[0], caps[1], caps[2], caps[3]) <= size_t(budget)) {
+          A->growTo(caps);
+          notePeak();
+          grown = true;
+          break;
+        }
+      }
+      if (grown) continue;
+      const int victim = lruIdle(keepSlot);
+      if (victim < 0) return false;
+      A->evict(victim);
+    }
+  }
+
+  void ensurePoseBuffers(size_t nseg, size_t bodies) {
+    if (nseg > segCap) {
+      dfree(segDev);
+      segDev = nullptr;
+      segCap = nseg + nseg / 2 + 64;
+      segDev = dalloc<int4>(segCap);
+    }
+    if (bodies > poseCap) {
+      dfree(poseDev);
+      poseDev = nullptr;
+      poseCap = bodies + bodies / 2 + 1024;
+      poseDev = dalloc<float4>(2 * poseCap);
+    }
+    notePeak();
+  }
+};
+
+namespace {
+
+void forget(avbd_ctx* ctx, Arena* A) {
+  auto& v = ctx->owned;
+  v.erase(std::remove(v.begin(), v.end(), (void*)A), v.end());
+}
+
+void bind(avbd_ctx* c) { CK(cudaSetDevice(c->device)); }
+
+}  // namespace
+
+extern "C" {
+
+int avbd_server_create(avbd_ctx* ctx, const avbd_server_desc* desc, avbd_server** out) {
+  API_BEGIN
+  REQUIRE(ctx && desc && out, "null argument");
+  REQUIRE(desc->budget_bytes > 0, "budget_bytes must be positive");
+  REQUIRE(desc->initial_bodies >= 0 && desc->initial_worlds >= 0, "negative initial capacity");
+  bind(ctx);
+  const int nb = std::max(desc->initial_bodies, 1024);
+  const int nw = std::max(desc->initial_worlds, 16);
+  auto* S = new avbd_server();
+  S->ctx = ctx;
+  S->budget = desc->budget_bytes;
+  try {
+    S->A = new Arena(ctx, nb, std::max(nb / 16, 64), Arena::initialPairCap(nb), nw);
+  } catch (...) {
+    delete S;
+    throw;
+  }
+  if (S->A->deviceBytes() > size_t(S->budget)) {
+    delete S->A;
+    delete S;
+    throw Error(AVBD_E_CAPACITY, "the initial capacities alone exceed budget_bytes");
+  }
+  ctx->owned.push_back(S->A);
+  // a pair region outgrowing the slot buffers mid-tick: stay within the budget by evicting idle
+  // worlds (never one being stepped: those have queued steps) before the buffers grow
+  S->A->onSlotPressure = [S](int slots) { S->makeRoom(0, 0, slots, -1, false); };
+  S->notePeak();
+  *out = S;
+  API_END
+}
+
+int avbd_server_destroy(avbd_server* s) {
+  API_BEGIN
+  if (!s) return AVBD_OK;
+  bind(s->ctx);
+  forget(s->ctx, s->A);
+  delete s->A;
+  dfree(s->segDev);
+  dfree(s->poseDev);
+  delete s;
+  API_END
+}
+
+int avbd_server_admit(avbd_server* s, const avbd_scene_desc* scene, const avbd_params* params, int64_t* world_id) {
+  API_BEGIN
+  REQUIRE(s && scene && params && world_id, "null argument");
+  Arena::validate(*scene, *params);
+  bind(s->ctx);
+  const int nb = scene->n_bodies, nj = Arena::jointsOf(*scene);
+  if (!s->makeRoom(nb, nj, Arena::initialPairCap(nb), -1)) {
+    s->rejected++;
+    throw Error(AVBD_E_CAPACITY, "world of " + std::to_string(nb) + " bodies does not fit in the device budget (" +
+                                     std::to_string(s->budget) + " bytes) with every idle world evicted");
+  }
+  const int slot = s->A->addWorld(*scene, *params);
+  const int64_t id = s->nextId++;
+  Served w;
+  w.slot = slot;
+  w.nBodies = nb;
+  w.lastUse = ++s->clock;
+  s->worlds.emplace(id, std::move(w));
+  s->admitted++;
+  s->notePeak();
+  *world_id = id;
+  API_END
+}
+
+int avbd_server_advance(avbd_server* s, int64_t world_id, int32_t steps, int64_t* ticket) {
+  API_BEGIN
+  REQUIRE(s && ticket, "null argument");
+  REQUIRE(steps >= 0, "steps must be non-negative");
+  Served& w = s->get(world_id);
+  const int64_t t = s->nextTicket++;
+  w.queued += steps;
+  w.lastUse = ++s->clock;
+  if (steps == 0 && w.tickets.empty()) {
+    s->completed.push_back(t);  // nothing to wait for
+    s->completedCount++;
+  } else {
+    w.tickets.push_back(Ticket{w.done + w.queued, t});
+  }
+  if (w.queued > 0) s->busy.insert(world_id);
+  *ticket = t;
+  API_END
+}
+
+int avbd_server_tick(avbd_server* s, int32_t* n_stepped) {
+  API_BEGIN
+  REQUIRE(s, "null server");
+  bind(s->ctx);
+  Arena& A = *s->A;
+  s->clock++;
+  // restore evicted worlds that have work, least recently used first, while room allows
+  std::vector<std::pair<unsigned long long, int64_t>> waiting;
+  for (int64_t id : s->busy) {
+    const Served& w = s->worlds.at(id);
+    if (!A.W[w.slot].resident) waiting.push_back({w.lastUse, id});
+  }
+  std::sort(waiting.begin(), waiting.end());
+  for (auto& e : waiting) {
+    Served& w = s->worlds.at(e.second);
+    const WorldRec& R = A.W[w.slot];
+    if (!s->makeRoom(R.nBodies, R.nJoints, A.restoreSlots(w.slot), w.slot, false)) break;
+    A.restore(w.slot);
+  }
+  std::vector<int> act;
+  std::vector<int64_t> ids;
+  for (int64_t id : s->busy) {
+    const Served& w = s->worlds.at(id);
+    if (A.W[w.slot].resident) {
+      act.push_back(w.slot);
+      ids.push_back(id);
+    }
+  }
+  if (!act.empty()) A.stepWorlds(act);
+  for (int64_t id : ids) {
+    Served& w = s->worlds.at(id);
+    w.queued--;
+    w.done++;
+    w.lastUse = s->clock;
+    s->bodySteps += w.nBodies;
+    while (!w.tickets.empty() && w.tickets.front().target <= w.done) {
+      s->completed.push_back(w.tickets.front().id);
+      s->completedCount++;
+      w.tickets.pop_front();
+    }
+    if (w.queued == 0) s->busy.erase(id);
+  }
+  s->ticks++;
+  s->notePeak();
+  if (n_stepped) *n_stepped = int32_t(act.size());
+  API_END
+}
+
+int avbd_server_completed(avbd_server* s, int64_t* tickets, int32_t cap, int32_t* n) {
+  API_BEGIN
+  REQUIRE(s && n && (cap == 0 || tickets), "null argument");
+  REQUIRE(cap >= 0, "negative capacity");
+  int k = 0;
+  while (k < cap && !s->completed.empty()) {
+    tickets[k++] = s->completed.front();
+    s->completed.pop_front();
+  }
+  *n = k;
+  API_END
+}
+
+int avbd_server_read_poses(avbd_server* s, const int64_t* world_ids, int32_t n, float* out) {
+  API_BEGIN
+  REQUIRE(s && (n == 0 || (world_ids && out)), "null argument");
+  REQUIRE(n >= 0, "negative count");
+  bind(s->ctx);
+  Arena& A = *s->A;
+  std::vector<int4> seg;
+  std::vector<std::pair<int, size_t>> hostRows;  // (slot, first output body) of evicted worlds
+  size_t total = 0;
+  for (int k = 0; k < n; k++) {
+    const Served& w = s->get(world_ids[k]);
+    const WorldRec& R = A.W[w.slot];
+    if (total + size_t(R.nBodies) > size_t(0x7fffffff)) throw Error(AVBD_E_CAPACITY, "too many bodies in one read");
+    if (R.resident) seg.push_back(make_int4(R.dev.bodyOff, R.nBodies, int(total), 0));
+    else {
+      seg.push_back(make_int4(0, 0, int(total), 0));
+      hostRows.push_back({w.slot, total});
+    }
+    total += size_t(R.nBodies);
+  }
+  if (total == 0) return AVBD_OK;
+  s->ensurePoseBuffers(seg.size(), total);
+  A.put(s->segDev, seg.data(), seg.size() * sizeof(int4));
+  int blocks = grid_blocks((long long)total, 256);
+  if (blocks > 152 * 8) blocks = 152 * 8;
+  k_gather_poses<<<blocks, 256, 0, A.s>>>(A.B, s->segDev, int(seg.size()), int(total), s->poseDev); note_launches(1);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(out, s->poseDev, total * 2 * sizeof(float4), cudaMemcpyDeviceToHost, A.s));
+  A.flush();
+  for (auto& h : hostRows) {
+    const WorldRec& R = A.W[h.first];
+    const Snapshot& S = *R.snap;
+    for (int i = 0; i < R.nBodies; i++) {
+      float* o = out + (h.second + size_t(i)) * 8;
+      const float4 p = S.body[0][i], q = S.body[1][i], sz = S.body[9][i];
+      o[0] = p.x; o[1] = p.y; o[2] = p.z; o[3] = sz.w;
+      o[4] = q.x; o[5] = q.y; o[6] = q.z; o[7] = q.w;
+    }
+  }
+  API_END
+}
+
+int avbd_server_read_state(avbd_server* s, int64_t world_id, float* position, float* rotation, float* velocity, float* angular,
+                           float* prev_velocity) {
+  API_BEGIN
+  REQUIRE(s, "null server");
+  bind(s->ctx);
+  const Served& w = s->get(world_id);
+  const WorldRec& R = s->A->W[w.slot];
+  if (R.resident) {
+    s->A->readState(w.slot, position, rotation, velocity, angular, prev_velocity);
+    return AVBD_OK;
+  }
+  const Snapshot& S = *R.snap;
+  auto put3 = [&](float* o, const std::vector<float4>& v) {
+    if (!o) return;
+    for (int i = 0; i < R.nBodies; i++) { o[3 * i] = v[i].x; o[3 * i + 1] = v[i].y; o[3 * i + 2] = v[i].z; }
+  };
+  put3(position, S.body[0]);
+  put3(velocity, S.body[6]);
+  put3(angular, S.body[7]);
+  put3(prev_velocity, S.body[8]);
+  if (rotation)
+    for (int i = 0; i < R.nBodies; i++) {
+      const float4 q = S.body[1][i];
+      rotation[4 * i] = q.x; rotation[4 * i + 1] = q.y; rotation[4 * i + 2] = q.z; rotation[4 * i + 3] = q.w;
+    }
+  API_END
+}
+
+int avbd_server_world_info(avbd_server* s, int64_t world_id, int32_t* n_bodies, int64_t* queued, int64_t* steps_done,
+                           int32_t* resident) {
+  API_BEGIN
+  REQUIRE(s, "null server");
+  const Served& w = s->get(world_id);
+  if (n_bodies) *n_bodies = w.nBodies;
+  if (queued) *queued = w.queued;
+  if (steps_done) *steps_done = w.done;
+  if (resident) *resident = s->A->W[w.slot].resident ? 1 : 0;
+  API_END
+}
+
+int avbd_server_evict(avbd_server* s, int64_t world_id) {
+  API_BEGIN
+  REQUIRE(s, "null server");
+  bind(s->ctx);
+  const Served& w = s->get(world_id);
+  if (!s->A->W[w.slot].resident) return AVBD_OK;
+  s->A->evict(w.slot);
+  API_END
+}
+
+int avbd_server_release(avbd_server* s, int64_t world_id) {
+  API_BEGIN
+  REQUIRE(s, "null server");
+  bind(s->ctx);
+  const Served& w = s->get(world_id);
+  s->A->removeWorld(w.slot);
+  s->busy.erase(world_id);
+  s->worlds.erase(world_id);
+  API_END
+}
+
+int avbd_server_read_stats(avbd_server* s, avbd_server_stats* out) {
+  API_BEGIN
+  REQUIRE(s && out, "null argument");
+  std::memset(out, 0, sizeof(*out));
+  out->budget_bytes = s->budget;
+  out->device_bytes = int64_t(s->deviceBytes());
+  out->peak_device_bytes = int64_t(s->peak);
+  out->live_worlds = int64_t(s->worlds.size());
+  for (auto& kv : s->worlds) {
+    const WorldRec& R = s->A->W[kv.second.slot];
+    if (R.resident) {
+      out->resident_worlds++;
+      out->resident_bodies += R.nBodies;
+    } else {
+      out->evicted_worlds++;
+    }
+  }
+  out->pending_worlds = int64_t(s->busy.size());
+  out->admitted = s->admitted;
+  out->rejected = s->rejected;
+  out->evictions = s->A->evictions;
+  out->restores = s->A->restores;
+  out->ticks = s->ticks;
+  out->body_steps = s->bodySteps;
+  out->completed = s->completedCount;
+  API_END
+}
+
+}  // extern "C"

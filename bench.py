@@ -49,10 +49,15 @@ def args_parse():
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    p.add_argument("--workload", choices=["world_mix", "box_pile"], default="world_mix")
+    p.add_argument("--workload", choices=["world_mix", "box_pile", "served"], default="world_mix")
+    p.add_argument("--requests", type=int, default=20_000, help="served: requests per stream")
+    p.add_argument("--rates", default="2000,10000,50000", help="served: Poisson arrival rates (req/s)")
+    p.add_argument("--serve-rate", type=float, default=10_000.0, help="rate of the served stream in the default line")
+    p.add_argument("--budget-gb", type=float, default=120.0, help="served: device-memory budget")
+    p.add_argument("--no-serve", action="store_true")
     p.add_argument("--worlds", type=int, default=4096)
     p.add_argument("--plain-sample", type=int, default=128, help="worlds timed on the plain path")
-    p.add_argument("--cpu-sample", type=int, default=64, help="worlds timed on the CPU path")
+    p.add_argument("--cpu-sample", type=int, default=256, help="worlds timed on the CPU path")
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-plain", action="store_true")
@@ -175,7 +180,7 @@ def cpu_baseline(worlds, warm, steps, seconds, threads=0):
     bodies = sum(w.n_bodies for w in worlds)
     done, t0 = 0, time.perf_counter()
     used = 1
-    while done < steps:
+    while done < steps or time.perf_counter() - t0 < seconds:
         used = oracle.step_parallel(ws, 1, threads)
         done += 1
         if time.perf_counter() - t0 > seconds:
@@ -200,6 +205,111 @@ def load_traffic():
         return json.load(open(p))
     except Exception:
         return {}
+
+
+def served_stream(pipe, args, rate, seed):
+    """One Poisson request stream through the world server (the serving configuration: 20,000
+    requests, creates of log-normal size and advances by K in {1, 4, 16}, continuous batching,
+    budgeted admission with LRU eviction). Latency of a request = arrival to its reply: a create
+    replies once the world is admitted; an advance once its steps have run and the world's poses
+    are read back (one batched pose read per tick for the worlds whose requests completed)."""
+    from avbd_gb300 import _lib as L
+    from avbd_gb300 import workloads
+    r = workloads.request_stream(args.requests, rate, seed)
+    creates = np.nonzero(r["create"])[0]
+    packed = {int(i): L.PackedScene(workloads.lattice_pile(int(r["count"][i]), int(r["world_seed"][i]))) for i in creates}
+    server = pipe.createServer(budgetBytes=int(args.budget_gb * 1e9), initialBodies=1 << 20, initialWorlds=4096)
+    n = args.requests
+    world_of_create = {}  # creation order -> world id
+    created = 0
+    ticket_info = {}
+    lat_create, lat_adv, tick_ms = [], [], []
+    rejected = 0
+    h2d = d2h = 0
+    i = 0
+    arrival = r["arrival"]
+    pipe.synchronize()
+    t0 = time.perf_counter()
+    while i < n or ticket_info:
+        now = time.perf_counter() - t0
+        if i < n and arrival[i] > now and not ticket_info:
+            time.sleep(min(arrival[i] - now, 0.001))
+            continue
+        while i < n and arrival[i] <= now:
+            if r["create"][i]:
+                pk = packed[i]
+                try:
+                    wid = server.admit(pk)
+                    world_of_create[created] = wid
+                    h2d += sum(a.nbytes for a in pk.keep)
+                except L.AvbdError:
+                    rejected += 1
+                    world_of_create[created] = None
+                created += 1
+                lat_create.append(time.perf_counter() - t0 - arrival[i])
+            else:
+                wid = world_of_create.get(int(r["target"][i]))
+                if wid is not None:
+                    ticket_info[server.advance(wid, int(r["steps"][i]))] = (arrival[i], wid)
+                else:
+                    lat_adv.append(time.perf_counter() - t0 - arrival[i])  # refused at once
+            i += 1
+        if ticket_info:
+            a = time.perf_counter()
+            server.tick()
+            done = server.completed()
+            if done:
+                ids = sorted({ticket_info[t][1] for t in done})
+                poses = server.readPoses(ids)  # replies: poses of the worlds whose requests completed
+                d2h += poses.nbytes
+            else:
+                pipe.synchronize()
+            b = time.perf_counter()
+            tick_ms.append((b - a) * 1000.0)
+            for t in done:
+                arr, _ = ticket_info.pop(t)
+                lat_adv.append(b - t0 - arr)
+    wall = time.perf_counter() - t0
+    st = server.stats()
+    server.destroy()
+    lat = np.array(lat_create + lat_adv) * 1000.0
+    la = np.array(lat_adv) * 1000.0
+    pct = lambda x, q: round(float(np.percentile(x, q)), 3) if len(x) else None  # noqa: E731
+    return {"rate_req_s": rate, "requests": n, "creates": int(len(creates)), "wall_s": round(wall, 3),
+            "body_steps_per_s": st["body_steps"] / wall, "body_steps": st["body_steps"],
+            "latency_ms": {"p50": pct(lat, 50), "p95": pct(lat, 95), "p99": pct(lat, 99)},
+            "advance_latency_ms": {"p50": pct(la, 50), "p95": pct(la, 95), "p99": pct(la, 99)},
+            "tick_ms": {"p50": pct(tick_ms, 50), "p95": pct(tick_ms, 95), "p99": pct(tick_ms, 99), "ticks": len(tick_ms)},
+            "admitted_worlds": st["admitted"], "rejected_worlds": rejected, "evictions": st["evictions"],
+            "restores": st["restores"], "peak_device_gb": round(st["peak_device_bytes"] / 1e9, 2),
+            "budget_gb": args.budget_gb, "h2d_bytes": int(h2d), "d2h_bytes": int(d2h),
+            "stream": f"seed {seed}, Poisson arrivals, first 256 requests create, then 10% creates; counts log-normal "
+                      f"median 256 sigma 1.2078 clipped [16, 65536]; advances K in {{1, 4, 16}} to a uniform earlier world"}
+
+
+def run_served(args, dist):
+    import torch
+    from avbd_gb300 import createSolverPipeline, workloads
+    dev = dist.local
+    torch.cuda.set_device(dev)
+    pipe = createSolverPipeline("gb300", device=dev)
+    lines = []
+    with Clocks(dev) as clk:
+        for k, rate in enumerate(float(x) for x in args.rates.split(",")):
+            log(f"served stream at {rate:.0f} req/s")
+            lines.append(served_stream(pipe, args, rate, workloads.SEED_BASE + 4 + 1000 * dist.rank))
+            log(json.dumps(lines[-1]))
+    pipe.destroy()
+    if dist.rank != 0:
+        return
+    best = max(lines, key=lambda x: x["body_steps_per_s"])
+    line = {"metric": METRIC, "value": best["body_steps_per_s"], "unit": UNIT, "n_gpus": args.gpus,
+            "steps": None, "warmup": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "served_poisson", "requests": args.requests, "budget_gb": args.budget_gb,
+                       "rates": args.rates},
+            "served": lines, "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
 
 
 # ------------------------------------------------------------------ arms
@@ -325,6 +435,11 @@ def run_ours(args, dist):
     if dist.rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(sample_worlds(worlds, args.cpu_sample), args.warmup, args.steps, args.cpu_seconds)
     log("cpu baseline done")
+    served = None
+    if not args.no_serve and args.workload == "world_mix":
+        from avbd_gb300 import workloads
+        served = served_stream(pipe, args, args.serve_rate, workloads.SEED_BASE + 4 + 1000 * dist.rank)
+        log("served stream done")
     pipe.destroy()
     if dist.rank != 0:
         return
@@ -334,7 +449,7 @@ def run_ours(args, dist):
             "tick_ms": {"p50": round(float(np.percentile(ticks, 50)), 3), "p95": round(float(np.percentile(ticks, 95)), 3),
                         "p99": round(float(np.percentile(ticks, 99)), 3)},
             "plain_gpu": plain, "stage_ms_per_step": breakdown, "roofline": roof, "cpu_baseline": cpu,
-            "e2e": e2e, "gpu_launches": int(launches), "clocks": clk.summary()}
+            "e2e": e2e, "gpu_launches": int(launches), "clocks": clk.summary(), "served": served}
     print(json.dumps(line), flush=True)
 
 
@@ -343,6 +458,8 @@ def main():
     dist = Dist()
     if args.impl == "reference":
         run_reference(args, dist)
+    elif args.workload == "served":
+        run_served(args, dist)
     else:
         run_ours(args, dist)
 

@@ -209,6 +209,58 @@ int avbd_world_profile_read(avbd_world* w, avbd_profile* out);
 int avbd_batch_profile(avbd_batch* b, int32_t enable);
 int avbd_batch_profile_read(avbd_batch* b, avbd_profile* out);
 
+/* ---------------------------------------------------------------- serving */
+
+/* A world server: worlds are admitted and released at any time, advance requests queue steps,
+ * and each tick steps every world with queued steps in one launch sequence (continuous
+ * batching). Device memory is held under a byte budget: when a new or restored world does not
+ * fit, the least recently used idle world (no queued steps) is evicted to host memory and
+ * restored when work for it arrives. A world's results do not depend on what else is served,
+ * on ticks it waits, or on eviction: K steps give the same bits as avbd_world_step(w, K) on
+ * the same scene. No counterpart in the reference (one solver per world, stepped by its owner:
+ * src/native/pipeline.js:52-81, src/native/runtime.js:255-272). World ids and tickets are
+ * positive and never reused. */
+typedef struct avbd_server avbd_server;
+
+typedef struct avbd_server_desc {
+  int64_t budget_bytes;   /* device bytes the server's arrays may occupy (> 0) */
+  int32_t initial_bodies; /* initial capacities (grown on demand within the budget) */
+  int32_t initial_worlds;
+} avbd_server_desc;
+
+typedef struct avbd_server_stats {
+  int64_t budget_bytes, device_bytes, peak_device_bytes;
+  int64_t live_worlds, resident_worlds, evicted_worlds, pending_worlds;
+  int64_t resident_bodies, admitted, rejected, evictions, restores, ticks, body_steps, completed;
+} avbd_server_stats;
+
+int avbd_server_create(avbd_ctx* ctx, const avbd_server_desc* desc, avbd_server** out);
+int avbd_server_destroy(avbd_server* s);
+/* Admit a world (as avbd_world_create). AVBD_E_CAPACITY when it cannot fit in the budget even
+ * after evicting every idle world; nothing changes then. */
+int avbd_server_admit(avbd_server* s, const avbd_scene_desc* scene, const avbd_params* params, int64_t* world_id);
+/* Queue `steps` steps of a world; *ticket completes once they have run. */
+int avbd_server_advance(avbd_server* s, int64_t world_id, int32_t steps, int64_t* ticket);
+/* One step of every world with queued steps (evicted ones are restored first, room
+ * permitting). *n_stepped = worlds stepped (may be 0). */
+int avbd_server_tick(avbd_server* s, int32_t* n_stepped);
+/* Drain up to `cap` completed tickets (oldest first); *n = number written. */
+int avbd_server_completed(avbd_server* s, int64_t* tickets, int32_t cap, int32_t* n);
+/* Poses of every body of each listed world, 8 floats each (pos.xyz, friction, quat), world
+ * after world in list order; evicted worlds are read from their host copy. */
+int avbd_server_read_poses(avbd_server* s, const int64_t* world_ids, int32_t n, float* out);
+/* Full state of one world (as avbd_world_read_state); any pointer may be null. */
+int avbd_server_read_state(avbd_server* s, int64_t world_id, float* position, float* rotation, float* velocity,
+                           float* angular, float* prev_velocity);
+/* World facts: bodies, queued steps, steps done, resident (1) or evicted (0). */
+int avbd_server_world_info(avbd_server* s, int64_t world_id, int32_t* n_bodies, int64_t* queued, int64_t* steps_done,
+                           int32_t* resident);
+/* Evict a world now (its queued steps wait for a restore). */
+int avbd_server_evict(avbd_server* s, int64_t world_id);
+/* Drop a world; its outstanding tickets never complete. */
+int avbd_server_release(avbd_server* s, int64_t world_id);
+int avbd_server_read_stats(avbd_server* s, avbd_server_stats* out);
+
 #ifdef __cplusplus
 }
 #endif
