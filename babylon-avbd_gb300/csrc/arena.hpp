@@ -292,6 +292,9 @@ class Arena {
     G.cellCount = dalloc<int>(size_t(table) + 1);
     G.cellFill = dalloc<int>(table);
     G.cellBodies = dalloc<int>(N);
+    G.cellKey = dalloc<int4>(N);
+    G.cellPos = dalloc<float4>(N);
+    G.pairTmp = dalloc<uint32_t>(N * PAIR_TMP);
     G.bodyBucket = dalloc<int>(N);
     G.large = dalloc<int>(size_t(nw) * MAX_LARGE);
     T.adjStart = dalloc<int>(N + 1);
@@ -318,8 +321,8 @@ class Arena {
     void* ptrs[] = {B.pos, B.rot, B.pos0, B.rot0, B.posY, B.rotY, B.vel, B.ang, B.vprev, B.size, B.mass, B.meta, J.ab, J.rA,
                     J.rB, J.stiff, J.penLin, J.penAng, J.lamLin, J.lamAng, J.C0Lin, J.C0Ang, J.restQ, J.broken, worlds,
                     which, pairN, wover, wactive, active, activeBodies, activeJoints, pairPrefix, pairCount, G.cellCount,
-                    G.cellFill, G.cellBodies, G.bodyBucket, G.large, T.adjStart, T.adjFill, T.activeIndex, T.color, T.won,
-                    T.pending, T.colorBodies, T.itemStart, T.itemRef, T.contrib, ctr, NC.keys, NC.jid, scanTemp, traffic,
+                    G.cellFill, G.cellBodies, G.cellKey, G.cellPos, G.pairTmp, G.bodyBucket, G.large, T.adjStart, T.adjFill, T.activeIndex, T.color, T.won,
+                    T.pending, T.colorBodies, T.itemStart, T.itemRef, ctr, NC.keys, NC.jid, scanTemp, traffic,
                     poseStage, P.pair, P.count, P.basis, P.ct, NS.sat, NS.boxList, NS.sphereList, NS.ctr, activePairs,
                     T.adjList};
     for (void* p : ptrs) dfree(p);
@@ -413,6 +416,9 @@ class Arena {
     rescratch(T.pending, N);
     CK(cudaMemset(T.pending, 0, N));
     for (int** p : {&T.activeIndex, &T.won, &T.colorBodies, &activeBodies, &G.cellBodies, &G.bodyBucket}) rescratch(*p, N);
+    rescratch(G.cellKey, N);
+    rescratch(G.cellPos, N);
+    rescratch(G.pairTmp, N * PAIR_TMP);
     for (int** p : {&T.itemStart, &T.adjStart, &pairCount}) rescratch(*p, N + 1);
     rescratch(T.adjFill, std::max<size_t>(N + 1, MAX_COLORS));
     const uint32_t table = tableFor(N);
@@ -478,11 +484,11 @@ class Arena {
 
   // Device bytes of an arena with these capacities: the arrays above and the pair-slot buffers.
   // The per-tick work-item scratch (scratchBytes) comes on top; it grows with the contacts of
-  // the worlds being stepped (about 0.5 KB per body in settled piles, hence the reserve).
-  size_t scratchBytes() const { return itemCap * sizeof(int2) + size_t(T.contribCap) * 7 * sizeof(float4); }
-  static size_t scratchReserve(long long nb) { return size_t(nb) * 1024; }
+  // the worlds being stepped (about 0.2 KB per body in settled piles; the reserve doubles that).
+  size_t scratchBytes() const { return itemCap * sizeof(int4); }
+  static size_t scratchReserve(long long nb) { return size_t(nb) * 512; }
   size_t footprint(long long nb, long long nj, long long slots, long long nw) const {
-    const size_t perBody = 12 * 16 + 2 * 4 + 1 + 11 * 4;
+    const size_t perBody = 12 * 16 + 2 * 4 + 1 + 11 * 4 + 32 + 4 * PAIR_TMP;
     const size_t perJoint = 8 + 10 * 16 + 4 + 4 + 8;
     const size_t perSlot = 2 * (8 + 4 + 3 * 16 + MAX_CONTACTS * 64) + 16 + 3 * 4 + 8;
     const size_t perWorld = sizeof(WorldDev) + 4 * 4 + 16 + 4 + MAX_LARGE * 4;
@@ -990,23 +996,13 @@ class Arena {
   // ------------------------------------------------------------------ ticks
   void ensureItems() {
     const size_t need = size_t(std::max(ctrHost->itemsTotal, 1));
-    int maxColor = 1;
-    for (int c = 0; c < MAX_COLORS; c++) maxColor = std::max(maxColor, ctrHost->colorItems[c]);
     if (need > itemCap) {
       CK(cudaStreamSynchronize(s));
       const size_t cap = need + need / 4 + 1024;
       dfree(T.itemRef);
       T.itemRef = nullptr;
-      T.itemRef = dalloc<int2>(cap);
+      T.itemRef = dalloc<int4>(cap);
       itemCap = cap;
-    }
-    if (maxColor > T.contribCap) {
-      CK(cudaStreamSynchronize(s));
-      const int ccap = maxColor + maxColor / 4 + 1024;
-      dfree(T.contrib);
-      T.contrib = nullptr;
-      T.contrib = dalloc<float4>(size_t(ccap) * 7);
-      T.contribCap = ccap;
     }
   }
 
@@ -1071,7 +1067,7 @@ class Arena {
     const int pairBudget = int(std::min<long long>(budget, slotCap));
     Tick t = tick(na, nb, nj);
     ensureItems();
-    launch_items_fill(P, t, T, ctr, s);
+    launch_items_fill(B, worlds, P, t, T, ctr, s);
     cudaEvent_t o0 = prof ? mark() : nullptr;
     launch_joint_warmstart(B, worlds, J, t, s);
     launch_body_warmstart(B, worlds, t, s);
@@ -1085,12 +1081,14 @@ class Arena {
         launch_primal(B, worlds, J, P, t, T, ctr, c, it, cnt, ctrHost->colorItems[c], s);
         if (prof) {
           span(P_PRIMAL, a, mark());
-          profPrimalLaunches += ctrHost->colorItems[c] > 0 ? 2 : 1;
+          profPrimalLaunches += 1;
         }
       }
-      cudaEvent_t d = prof ? mark() : nullptr;
-      launch_dual(B, worlds, J, P, t, ctr, pairBudget, it, s);
-      if (prof) span(P_DUAL, d, mark());
+      if (nj) {
+        cudaEvent_t d = prof ? mark() : nullptr;
+        launch_dual_joints(B, worlds, J, t, it, s);
+        if (prof) span(P_DUAL, d, mark());
+      }
     }
     cudaEvent_t v0 = prof ? mark() : nullptr;
     launch_velocities(B, worlds, t, s);

@@ -95,14 +95,22 @@ __global__ void k_grid_count(const float4* __restrict__ pos, const int4* __restr
   }
 }
 
-__global__ void k_grid_scatter(const int* __restrict__ bodyBucket, Tick t, const int* __restrict__ cellStart,
-                               int* __restrict__ cellFill, int* __restrict__ cellBodies) {
+// Bucket the small bodies; each bucket entry also records its body's cell and position, so the
+// pair passes read candidates from contiguous memory and skip bodies of other cells or worlds
+// that share a hash bucket.
+__global__ void k_grid_scatter(const float4* __restrict__ pos, const int4* __restrict__ meta, const WorldDev* __restrict__ worlds,
+                               Tick t, Grid g) {
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < t.nBodies; k += gridDim.x * blockDim.x) {
     const int i = t.bodies[k];
-    const int b = bodyBucket[i];
+    const int b = g.bodyBucket[i];
     if (b < 0) continue;
-    const int slot = cellStart[b] + atomicAdd(&cellFill[b], 1);
-    cellBodies[slot] = i;
+    const float4 p = pos[i];
+    const int w = meta[i].x;
+    const float cell = worlds[w].cell;
+    const int slot = g.cellCount[b] + atomicAdd(&g.cellFill[b], 1);
+    g.cellBodies[slot] = i;
+    g.cellKey[slot] = make_int4(cell_coord(p.x, cell), cell_coord(p.y, cell), cell_coord(p.z, cell), w);
+    g.cellPos[slot] = p;
   }
 }
 
@@ -119,7 +127,7 @@ void launch_grid_build(const BodyPtrs& b, const WorldDev* worlds, Tick t, Grid g
   if (t.nBodies == 0) return;
   k_grid_count<<<grid_blocks(t.nBodies, 256), 256, 0, s>>>(b.pos, b.meta, worlds, t, g.tableMask, g.cellCount, g.bodyBucket); note_launches(1);
   scan_exclusive(g.cellCount, table + 1, nullptr, scanTemp, s);
-  k_grid_scatter<<<grid_blocks(t.nBodies, 256), 256, 0, s>>>(g.bodyBucket, t, g.cellCount, g.cellFill, g.cellBodies); note_launches(1);
+  k_grid_scatter<<<grid_blocks(t.nBodies, 256), 256, 0, s>>>(b.pos, b.meta, worlds, t, g); note_launches(1);
 }
 
 // ------------------------------------------------------------------ pair predicate
@@ -147,16 +155,17 @@ __device__ __forceinline__ bool linked(const NoCollide& nc, const int* jbroken, 
   return false;
 }
 
-// cpuPhysics3D.js:319-343 pair(): A = hi, B = lo
-__device__ __forceinline__ bool pair_test(const PairCtx& c, int hi, int lo, float4 pA, float mA, int4 metaA) {
-  const float4 pB = c.pos[lo];
-  const float mB = c.mass[lo].x;
-  if (mA <= 0.f && mB <= 0.f) return false;
-  const int4 metaB = c.meta[lo];
-  if (!(uint32_t(metaA.z) & uint32_t(metaB.w)) || !(uint32_t(metaB.z) & uint32_t(metaA.w))) return false;
+// cpuPhysics3D.js:319-343 pair(): A = hi, B = lo. The conditions are independent, so the cheap
+// distance test (on the partner's position pB) runs first.
+__device__ __forceinline__ bool pair_test(const PairCtx& c, int hi, int lo, float4 pA, float4 pB, float mA, int4 metaA) {
   const float r = pA.w + pB.w;
   const V3 d = v3(pA) - v3(pB);
   if (!(dot(d, d) <= r * r)) return false;
+  const float mB = c.mass[lo].x;
+  if (mA <= 0.f && mB <= 0.f) return false;
+  const int4 metaB = c.meta[lo];
+  if (metaB.x != metaA.x) return false;
+  if (!(uint32_t(metaA.z) & uint32_t(metaB.w)) || !(uint32_t(metaB.z) & uint32_t(metaA.w))) return false;
   if (c.nc.n > 0 && linked(c.nc, c.jbroken, hi, lo)) return false;
   return true;
 }
@@ -172,33 +181,37 @@ __device__ __forceinline__ void for_each_partner(const PairCtx& c, const WorldDe
   const bool small = !(pA.w > W.largeR);
   if (small) {
     const int cx = cell_coord(pA.x, W.cell), cy = cell_coord(pA.y, W.cell), cz = cell_coord(pA.z, W.cell);
-    uint32_t seen[27];
-    int nseen = 0;
     for (int dz = -1; dz <= 1; dz++)
       for (int dy = -1; dy <= 1; dy++)
         for (int dx = -1; dx <= 1; dx++) {
-          uint32_t b = cell_hash(w, cx + dx, cy + dy, cz + dz) & g.tableMask;
-          bool dup = false;
-          for (int k = 0; k < nseen; k++) dup |= seen[k] == b;
-          if (dup) continue;
-          seen[nseen++] = b;
+          const int nx = cx + dx, ny = cy + dy, nz = cz + dz;
+          const uint32_t b = cell_hash(w, nx, ny, nz) & g.tableMask;
           const int s0 = g.cellCount[b], s1 = g.cellCount[b + 1];
           for (int s = s0; s < s1; s++) {
             const int j = g.cellBodies[s];
-            if (j >= i || c.meta[j].x != w) continue;
-            if (pair_test(c, i, j, pA, mA, metaA)) emit(j);
+            if (j >= i) continue;
+            const float4 pB = g.cellPos[s];
+            const float r = pA.w + pB.w;
+            const V3 d = v3(pA) - v3(pB);
+            if (!(dot(d, d) <= r * r)) continue;
+            // only the entries of this very cell: a bucket shared by several neighbour cells (or
+            // worlds) is scanned once per cell, and each body counts in its own cell only
+            const int4 key = g.cellKey[s];
+            if (key.x != nx || key.y != ny || key.z != nz || key.w != w) continue;
+            if (pair_test(c, i, j, pA, pB, mA, metaA)) emit(j);
           }
         }
   }
   for (int k = 0; k < W.largeCount; k++) {
     const int L = g.large[W.largeOff + k];
     if (L >= i) break;
-    if (pair_test(c, i, L, pA, mA, metaA)) emit(L);
+    if (pair_test(c, i, L, pA, c.pos[L], mA, metaA)) emit(L);
   }
   if (!small) {
     for (int j = W.bodyOff; j < i; j++) {
-      if (c.pos[j].w > W.largeR) continue;  // large partners came from the list above
-      if (pair_test(c, i, j, pA, mA, metaA)) emit(j);
+      const float4 pB = c.pos[j];
+      if (pB.w > W.largeR) continue;  // large partners came from the list above
+      if (pair_test(c, i, j, pA, pB, mA, metaA)) emit(j);
     }
   }
 }
@@ -209,7 +222,13 @@ __device__ __forceinline__ void for_each_partner(const PairCtx& c, const WorldDe
 __global__ void k_pair_count(PairCtx c, const WorldDev* __restrict__ worlds, Grid g, Tick t, int* __restrict__ pairCount) {
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k <= t.nBodies; k += gridDim.x * blockDim.x) {
     int cnt = 0;
-    if (k < t.nBodies) for_each_partner(c, worlds, g, t.bodies[k], [&](int) { cnt++; });
+    if (k < t.nBodies) {
+      uint32_t* keep = g.pairTmp + k;  // column layout: partner m at keep[m * nBodies]
+      for_each_partner(c, worlds, g, t.bodies[k], [&](int j) {
+        if (cnt < PAIR_TMP) keep[size_t(cnt) * t.nBodies] = uint32_t(j);
+        cnt++;
+      });
+    }
     pairCount[k] = cnt;
   }
 }
@@ -242,11 +261,18 @@ __global__ void k_pair_write(PairCtx c, const WorldDev* __restrict__ worlds, Gri
     const int local = pairStart[k] - pairStart[e.y];
     const int cap = W.pairCap;
     uint2* out = pairs + (size_t)(1 - t.which[w]) * t.slotStride + W.pairOff;
+    const int total = pairStart[k + 1] - pairStart[k];
     int n = 0;
-    for_each_partner(c, worlds, g, i, [&](int j) {
-      const int slot = local + n++;
-      if (slot < cap) out[slot] = make_uint2(uint32_t(i), uint32_t(j));
-    });
+    if (total <= PAIR_TMP) {  // the partners kept by the counting pass
+      const uint32_t* keep = g.pairTmp + k;
+      for (; n < total; n++)
+        if (local + n < cap) out[local + n] = make_uint2(uint32_t(i), keep[size_t(n) * t.nBodies]);
+    } else {
+      for_each_partner(c, worlds, g, i, [&](int j) {
+        const int slot = local + n++;
+        if (slot < cap) out[slot] = make_uint2(uint32_t(i), uint32_t(j));
+      });
+    }
     // insertion sort of this body's range by partner (a body has a few dozen partners at most)
     const int end = min(local + n, cap);
     for (int a = local + 1; a < end; a++) {
@@ -576,18 +602,28 @@ __device__ __forceinline__ V3 unitv(V3 a) {
 
 __device__ __forceinline__ void box_geo(BoxGeo& g, float4 p, float4 q, float4 size) {
   const V3 c = v3(p);
+#pragma unroll
   for (int i = 0; i < 8; i++) {
     V3 l{(size.x / 2) * ((i & 1) ? 1.f : -1.f), (size.y / 2) * ((i & 2) ? 1.f : -1.f), (size.z / 2) * ((i & 4) ? 1.f : -1.f)};
     g.v[i] = c + rotate(q, l);
   }
+#pragma unroll
   for (int f = 0; f < 6; f++) g.n[f] = rotate(q, V3{kNormals[f][0], kNormals[f][1], kNormals[f][2]});
 }
 
+// first vertex of greatest dot(v, n) (the running best is kept by value, not by index)
 __device__ __forceinline__ V3 box_support(const BoxGeo& g, V3 n) {
-  int best = 0;
-  for (int i = 0; i < 8; i++)
-    if (dot(g.v[i], n) > dot(g.v[best], n)) best = i;
-  return g.v[best];
+  V3 best = g.v[0];
+  float bestDot = dot(g.v[0], n);
+#pragma unroll
+  for (int i = 1; i < 8; i++) {
+    const float d = dot(g.v[i], n);
+    if (d > bestDot) {
+      best = g.v[i];
+      bestDot = d;
+    }
+  }
+  return best;
 }
 
 // support of a sphere (both spine points coincide): first of the two, pushed out by r
@@ -685,14 +721,22 @@ __device__ int collide(float4 pA, float4 qA, float4 sA, int shA, float4 pB, floa
       n = v;
     }
   };
+  // The gap only grows, and a positive final gap means no contact: stop at the first positive one.
   if (!roundA)
-    for (int f = 0; f < 6; f++) consider(box.n[f]);
+    for (int f = 0; f < 6; f++) {
+      consider(box.n[f]);
+      if (gap > 0) return 0;
+    }
   if (!roundB)
-    for (int f = 0; f < 6; f++) consider(box.n[f]);
+    for (int f = 0; f < 6; f++) {
+      consider(box.n[f]);
+      if (gap > 0) return 0;
+    }
   if (roundA && roundB) {
     V3 pa, pb;
     closest_seg(spA, spA, spB, spB, pa, pb);
     consider(pa - pb);
+    if (gap > 0) return 0;
   }
   // [round, poly] = [A, B] then [B, A]
   for (int k = 0; k < 2; k++) {
@@ -709,11 +753,13 @@ __device__ int collide(float4 pA, float4 qA, float4 sA, int shA, float4 pB, floa
       float t = dot(ap, e) / (ee != 0.f ? ee : 1.f);
       t = fmaxf(0.f, fminf(1.f, t));
       consider(box.v[i] - madd(sp, e, t));
+      if (gap > 0) return 0;
     }
     for (int i = 0; i < 12; i++) {
       V3 pa, pb;
       closest_seg(sp, sp, box.v[kEdges[i][0]], box.v[kEdges[i][1]], pa, pb);
       consider(pa - pb);
+      if (gap > 0) return 0;
     }
   }
   if (gap == -INFINITY) consider(cA - cB);
@@ -771,8 +817,8 @@ __device__ __forceinline__ void finish_pair(const BodyPtrs& bd, const WorldDev& 
   const float friction = sqrtf(sA.w * sB.w);
   cur.count[p] = n;
   cur.basis[3 * p + 0] = f4(basis.r0, friction);
-  cur.basis[3 * p + 1] = f4(basis.r1, 0.f);
-  cur.basis[3 * p + 2] = f4(basis.r2, 0.f);
+  cur.basis[3 * p + 1] = f4(basis.r1, W.alpha);  // the world's constants the solver kernels need
+  cur.basis[3 * p + 2] = f4(basis.r2, W.betaLin);
   if (n == 0) return;
   // the world's previous pairs: its region in the buffer it holds its last state in
   const int pw = t.which[w];

@@ -10,8 +10,9 @@
 //   pairs    a region of pair slots, present in two buffers (slot + k * slotStride, k = 0, 1): the
 //            world's previous state lives in buffer which[w], a step writes the other buffer and
 //            flips which[w]. Per slot: (hi, lo) sorted ascending within the world, contact count,
-//            basis rows n(w: friction), t1, t2, and 8 contact slots of 4 float4: rA(xyz,
-//            feature|stick) rB(xyz, C0.n) pen(xyz, C0.t1) lam(xyz, C0.t2).
+//            basis rows n(w: friction), t1(w: the world's alpha), t2(w: its beta_lin), and 8
+//            contact slots of 4 float4: rA(xyz, feature|stick) rB(xyz, C0.n) pen(xyz, C0.t1)
+//            lam(xyz, C0.t2).
 //   colours  two buffers of per-body colour state, selected like the pairs.
 // A step (a "tick") runs over an explicit list of active worlds: the bodies, joints and pair slots
 // of those worlds only. Worlds not stepped keep their state untouched, so a world evolves the
@@ -106,13 +107,18 @@ struct Counters {
   int colorItems[MAX_COLORS];
 };
 
+constexpr int PAIR_TMP = 16;  // partners a body keeps from the enumerating pass (more: enumerated again)
+
 struct Grid {
   uint32_t tableMask;  // hash table size - 1 (power of two)
   int* cellCount;      // table + 1 (scanned in place to starts)
   int* cellFill;
   int* cellBodies;     // small bodies bucketed
+  int4* cellKey;       // per bucketed entry: its cell (x, y, z, world)
+  float4* cellPos;     // per bucketed entry: position and bounding radius
   int* bodyBucket;     // per body (-1: large)
   int* large;          // MAX_LARGE slots per world: its large bodies, ascending
+  uint32_t* pairTmp;   // PAIR_TMP partners per active body: partner m of list position k at m * nBodies + k
 };
 
 // Narrowphase scratch (per tick), indexed by position q in the tick's active pair list: SAT
@@ -143,9 +149,7 @@ struct Topo {
   int* colorBodies;  // active indices k, bucketed by colour
   // manifold-contact work items of the dynamic bodies, bucket order (see launch_primal):
   int* itemStart;  // per bucket slot, nBodies + 1 (exclusive scan of item counts)
-  int2* itemRef;   // item -> (pair slot, contact | side << 3)
-  float4* contrib; // per item of the current colour: 7 planes of `contribCap` float4
-  int contribCap;
+  int4* itemRef;   // item -> (pair slot, item code (item_code), body A, body B)
 };
 
 // ---------------------------------------------------------------- launchers
@@ -175,13 +179,26 @@ void launch_adjacency(const BodyPtrs& b, JointPtrs j, PairPtrs P, Tick t, const 
 void launch_coloring(const BodyPtrs& b, const WorldDev* worlds, JointPtrs j, PairPtrs P, Tick t, Topo topo, int rounds,
                      Counters* ctr, cudaStream_t s);
 // Per tick, before the counter readback: per-body manifold-contact item counts, their scan and
-// the per-colour item totals. After the readback (with itemRef/contrib large enough): fill.
+// the per-colour item totals. After the readback (with itemRef large enough): fill.
 void launch_items_count(PairPtrs P, Tick t, Topo topo, Counters* ctr, void* scanTemp, cudaStream_t s);
-void launch_items_fill(PairPtrs P, Tick t, Topo topo, const Counters* ctr, cudaStream_t s);
+void launch_items_fill(const BodyPtrs& b, const WorldDev* worlds, PairPtrs P, Tick t, Topo topo, const Counters* ctr,
+                       cudaStream_t s);
+
+// Work-item code: contact index (3 bits), side (0: body A, 1: body B), whether this item runs the
+// contact's dual update (the item of the body solved last in an iteration: the other body is
+// static or has a lower colour; side 0 breaks a tie), and the world's iteration count (the solver
+// kernels need no world lookup).
+__host__ __device__ __forceinline__ int item_code(int contact, int side, bool dualOwner, int iterations) {
+  return contact | (side << 3) | (dualOwner ? 16 : 0) | (iterations << 5);
+}
+__host__ __device__ __forceinline__ int item_contact(int code) { return code & 7; }
+__host__ __device__ __forceinline__ int item_side(int code) { return (code >> 3) & 1; }
+__host__ __device__ __forceinline__ bool item_dual_owner(int code) { return (code & 16) != 0; }
+__host__ __device__ __forceinline__ int item_iterations(int code) { return code >> 5; }
 void launch_primal(const BodyPtrs& b, const WorldDev* worlds, JointPtrs j, PairPtrs P, Tick t, Topo topo, const Counters* ctr,
                    int color, int iteration, int nBodiesColor, int nItemsColor, cudaStream_t s);
-void launch_dual(const BodyPtrs& b, const WorldDev* worlds, JointPtrs j, PairPtrs P, Tick t, const Counters* ctr, int pairBudget,
-                 int iteration, cudaStream_t s);
+// Joint duals of one iteration (contact duals run inside launch_primal, see k_primal).
+void launch_dual_joints(const BodyPtrs& b, const WorldDev* worlds, JointPtrs j, Tick t, int iteration, cudaStream_t s);
 void launch_velocities(const BodyPtrs& b, const WorldDev* worlds, Tick t, cudaStream_t s);
 void launch_tick_end(Tick t, cudaStream_t s);
 void launch_count_active(JointPtrs j, PairPtrs P, const int* slots, int nSlots, const int* joints, int nJoints, Counters* out,
