@@ -4,7 +4,7 @@ Each CUDA translation unit is compiled in parallel with nvcc (one ``-gencode``),
 with ``-shared``. The collision and solve units are compiled with ``-fmad=false`` so their
 float arithmetic is rounded operation by operation, as the reference's is.
 
-Usage: python babylon-avbd_gb300/build.py [--force]
+Usage: python babylon-avbd_gb300/build.py [--force]   (AVBD_DEFINES="NAME=VALUE ..." adds -D flags)
 """
 from __future__ import annotations
 
@@ -56,9 +56,12 @@ def build(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
     cc = nvcc()
 
+    # extra -D definitions (tuning parameters of the kernels, e.g. AVBD_PRIMAL_TILE=512)
+    defines = ["-D" + d for d in os.environ.get("AVBD_DEFINES", "").split()]
+
     def compile_unit(name):
         obj = os.path.join(BUILD, name + ".o")
-        cmd = [cc, *ARCH, *COMMON, *UNITS[name], "-c", os.path.join(CSRC, name), "-o", obj]
+        cmd = [cc, *ARCH, *COMMON, *UNITS[name], *defines, "-c", os.path.join(CSRC, name), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed for {name}:\n{r.stderr}")
