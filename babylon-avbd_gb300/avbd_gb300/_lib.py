@@ -22,7 +22,8 @@ class Params(C.Structure):
     _fields_ = [("dt", C.c_float), ("gravity", C.c_float), ("up", C.c_float * 3),
                 ("iterations", C.c_int32), ("alpha", C.c_float), ("beta_lin", C.c_float),
                 ("beta_ang", C.c_float), ("gamma", C.c_float), ("mass_penalty", C.c_int32),
-                ("face_bias", C.c_int32), ("color_rounds", C.c_int32)]
+                ("face_bias", C.c_int32), ("color_rounds", C.c_int32), ("broadphase", C.c_int32),
+                ("bvh_rebuild", C.c_int32)]
 
 
 class SceneDesc(C.Structure):
@@ -108,6 +109,7 @@ SIGNATURES = [
 
 # include/avbd_gb300.h
 AVBD_E_CAPACITY = -5
+BROADPHASE = {"grid": 0, "hploc": 1, "auto": 2}
 NOALLOC_MAX_SELECTED = 8192
 
 _lib = None
@@ -174,6 +176,6 @@ class PackedScene:
         p = s.params
         self.params = Params(p.dt, p.gravity, (C.c_float * 3)(*p.up), p.iterations, p.alpha,
                              p.beta_lin, p.beta_ang, p.gamma, int(p.mass_penalty), int(p.face_bias),
-                             int(p.color_rounds))
+                             int(p.color_rounds), BROADPHASE[p.broadphase], int(p.bvh_rebuild))
         self.n_bodies = s.n_bodies
         self.n_joints = int(np.sum(s.kind != 2)) if s.n_cons else 0

@@ -18,6 +18,28 @@ from . import _lib as L
 from .scene import AvbdScene3D, SceneArrays
 
 
+def _with_options(arrays: SceneArrays, options) -> SceneArrays:
+    import copy
+    p = copy.copy(arrays.params)
+    if "broadphase" in options:
+        if options["broadphase"] not in L.BROADPHASE:
+            raise ValueError("broadphase must be 'grid', 'hploc' or 'auto'")
+        p.broadphase = options["broadphase"]
+    if "bvh" in options:
+        r = (options["bvh"] or {}).get("rebuildInterval", p.bvh_rebuild)
+        if int(r) != r or r < 1:
+            raise ValueError("BVH rebuildInterval must be a positive integer")
+        p.bvh_rebuild = int(r)
+    if "colorRounds" in options:
+        r = options["colorRounds"]
+        if int(r) != r or r < 1:
+            raise ValueError("colorRounds must be a positive integer")
+        p.color_rounds = int(r)
+    out = copy.copy(arrays)
+    out.params = p
+    return out
+
+
 def _arrays(scene) -> SceneArrays:
     if isinstance(scene, AvbdScene3D):
         scene.created = True
@@ -55,12 +77,17 @@ class SolverPipeline:
         L.check(L.lib().avbd_ctx_synchronize(self._h))
 
     def createSolver(self, scene, options=None) -> "World":
+        """``pipeline.createSolver(scene, options)``; options ``broadphase`` ("auto", "grid",
+        "hploc"), ``bvh: {rebuildInterval}`` and ``colorRounds`` as in AvbdGpuOptions
+        (``src/native/scenes.d.ts:288-310``)."""
         self._live()
+        arrays = _arrays(scene)
         if options:
-            unknown = set(options) - {"spatialSort"}
+            unknown = set(options) - {"spatialSort", "broadphase", "bvh", "colorRounds"}
             if unknown:
                 raise ValueError(f"unsupported solver options {sorted(unknown)}")
-        w = World(self, _arrays(scene))
+            arrays = _with_options(arrays, options)
+        w = World(self, arrays)
         self._children.append(w)
         return w
 

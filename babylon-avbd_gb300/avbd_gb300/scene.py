@@ -44,6 +44,8 @@ class SolverParams:
     mass_penalty: bool = True
     face_bias: bool = True
     color_rounds: int = 64
+    broadphase: str = "auto"  # "grid", "hploc" (the tree of gpuHploc.js) or "auto"; same pairs
+    bvh_rebuild: int = 16     # steps between tree rebuilds; refit in between
 
 
 @dataclass

@@ -29,6 +29,7 @@ UNITS = {
     "solve.cu": ["-fmad=false"],
     "engine.cu": ["-fmad=false"],
     "server.cu": [],
+    "bvh.cu": [],
 }
 
 

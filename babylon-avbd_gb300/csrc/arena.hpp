@@ -152,6 +152,11 @@ struct WorldRec {
   long long pending = 0;
   unsigned long long lastUse = 0;
   std::unique_ptr<Snapshot> snap;
+  // broadphase tree (FLAG_BVH): node range in the arena's pool, rebuilt every bvhRebuild steps
+  bool bvh = false;
+  BvhLayout tree;
+  int bvhOff = 0, bvhRebuild = 16, sinceBuild = 0;
+  bool built = false;
 };
 
 class Arena {
@@ -160,6 +165,11 @@ class Arena {
   cudaStream_t s;
   int bodyCap = 0, jointCap = 0, slotCap = 0, maxWorlds = 0;
   RangeAlloc bodyA, jointA, slotA;
+  // tree pool of the worlds with FLAG_BVH, and the build scratch (sized for the largest tree)
+  RangeAlloc bvhA;
+  int bvhCap = 0;
+  BvhScratch bsc{};
+  size_t bscKeys = 0, bscHist = 0, bscClusters = 0, bscBounds = 0;
   std::vector<int> freeSlots;
   std::vector<WorldRec> W;
   // device
@@ -324,7 +334,8 @@ class Arena {
                     G.cellFill, G.cellBodies, G.cellKey, G.cellPos, G.pairTmp, G.bodyBucket, G.large, T.adjStart, T.adjFill, T.activeIndex, T.color, T.won,
                     T.pending, T.colorBodies, T.itemStart, T.itemRef, ctr, NC.keys, NC.jid, scanTemp, traffic,
                     poseStage, P.pair, P.count, P.basis, P.ct, NS.sat, NS.boxList, NS.sphereList, NS.ctr, activePairs,
-                    T.adjList};
+                    T.adjList, G.bvh.node, G.bvh.parent, G.bvh.escape, G.bvh.minIdx, bsc.keys[0], bsc.keys[1], bsc.hist,
+                    bsc.clusters, bsc.bounds};
     for (void* p : ptrs) dfree(p);
     if (ctrHost) cudaFreeHost(ctrHost);
     if (activeHost) cudaFreeHost(activeHost);
@@ -493,7 +504,8 @@ class Arena {
     const size_t perSlot = 2 * (8 + 4 + 3 * 16 + MAX_CONTACTS * 64) + 16 + 3 * 4 + 8;
     const size_t perWorld = sizeof(WorldDev) + 4 * 4 + 16 + 4 + MAX_LARGE * 4;
     return size_t(nb) * perBody + size_t(tableFor(size_t(nb))) * 8 + size_t(nj) * perJoint + size_t(slots) * perSlot +
-           size_t(nw) * perWorld + size_t(ncCap) * 12 + scanBytes;
+           size_t(nw) * perWorld + size_t(ncCap) * 12 + scanBytes + size_t(bvhCap) * (32 + 12) +
+           (2 * bscKeys * sizeof(uint2) + bscHist * 4 + bscClusters * 4 + bscBounds * 16);
   }
   size_t deviceBytes() const { return footprint(bodyCap, jointCap, slotCap, maxWorlds) + scratchBytes(); }
 
@@ -625,6 +637,10 @@ class Arena {
     R.nBodies = d.n_bodies;
     R.nJoints = jointsOf(d);
     Wd.jointCount = R.nJoints;
+    R.bvh = p.broadphase == AVBD_BROADPHASE_HPLOC || (p.broadphase == AVBD_BROADPHASE_AUTO && treeSuits(d, R.nJoints, Wd.cell));
+    if (R.bvh) Wd.flags |= FLAG_BVH;
+    R.bvhRebuild = p.bvh_rebuild > 0 ? p.bvh_rebuild : 16;
+    Wd.bvhRoot = -1;
     R.nc.clear();
     int j = 0;
     for (int c = 0; c < d.n_cons; c++) {
@@ -633,6 +649,90 @@ class Arena {
       const int a = d.cons_a[c], b = d.cons_b[c];
       if (a >= 0) R.nc.push_back({(unsigned long long)(uint32_t)std::max(a, b) << 32 | (uint32_t)std::min(a, b), jid});
     }
+  }
+
+  // "auto" broadphase (src/gpu/appGpuSolver3D.js:333-398): the tree for >= 10,000 bodies when the
+  // grid cell is at least 4x twice the median radius, or for a jointed sheet of thin plates.
+  static bool treeSuits(const avbd_scene_desc& d, int joints, float cell) {
+    const int n = d.n_bodies;
+    if (n < 10000) return false;
+    std::vector<float> radii;
+    radii.reserve(n);
+    int dynamicCount = 0, thin = 0;
+    for (int i = 0; i < n; i++) {
+      if (d.radius[i] > 0.f) radii.push_back(d.radius[i]);
+      if (!(d.mass[i] > 0.f)) continue;
+      dynamicCount++;
+      const float a = d.size[3 * i], b = d.size[3 * i + 1], c = d.size[3 * i + 2];
+      const float lo = std::min(a, std::min(b, c)), hi = std::max(a, std::max(b, c)), mid = a + b + c - lo - hi;
+      if (d.shape[i] == AVBD_SHAPE_BOX && lo <= 0.4f * mid && mid >= 0.5f * hi) thin++;
+    }
+    float median = 1.f;
+    if (!radii.empty()) {
+      std::nth_element(radii.begin(), radii.begin() + radii.size() / 2, radii.end());
+      median = radii[radii.size() / 2];
+    }
+    const double cellRatio = double(cell) / (2.0 * double(median));
+    const bool sheet = joints >= n && dynamicCount > 0 && double(thin) / dynamicCount >= 0.25;
+    return cellRatio >= 4.0 || sheet;
+  }
+
+  // ------------------------------------------------------------------ trees
+  void growBvhPool(int cap) {
+    if (cap <= bvhCap) return;
+    flush();
+    const size_t o = size_t(bvhCap), N = size_t(cap);
+    regrow(G.bvh.node, 2 * o, 2 * N);
+    regrow(G.bvh.parent, o, N);
+    regrow(G.bvh.escape, o, N);
+    regrow(G.bvh.minIdx, o, N);
+    if (bvhCap == 0) bvhA.init(cap);
+    else bvhA.grow(cap);
+    bvhCap = cap;
+  }
+  void ensureBvhScratch(const WorldRec& R) {
+    const int n = R.nBodies;
+    if (bvh_scratch_keys(n) > bscKeys) {
+      bscKeys = bvh_scratch_keys(n);
+      rescratch(bsc.keys[0], bscKeys);
+      rescratch(bsc.keys[1], bscKeys);
+    }
+    if (bvh_scratch_hist(n) > bscHist) {
+      bscHist = bvh_scratch_hist(n);
+      rescratch(bsc.hist, bscHist);
+    }
+    if (size_t(R.tree.clusters) > bscClusters) {
+      bscClusters = size_t(R.tree.clusters);
+      rescratch(bsc.clusters, bscClusters);
+    }
+    if (bvh_scratch_bounds(n) > bscBounds) {
+      bscBounds = bvh_scratch_bounds(n);
+      rescratch(bsc.bounds, bscBounds);
+    }
+    const size_t need = scan_temp_bytes(int(bscHist) + 2);
+    if (need > scanBytes) {
+      rescratch(reinterpret_cast<char*&>(scanTemp), need);
+      scanBytes = need;
+    }
+  }
+  void placeBvh(WorldRec& R) {
+    if (!R.bvh) return;
+    bvh_layout(R.nBodies, R.tree);
+    const int need = std::max(R.tree.nodes, 1);
+    int off = bvhA.alloc(need);
+    if (off < 0) {
+      growBvhPool(std::max(bvhCap + need, bvhCap + bvhCap / 2));
+      off = bvhA.alloc(need);
+    }
+    if (off < 0) throw Error(AVBD_E_NOMEM, "tree pool exhausted");
+    R.bvhOff = off;
+    R.dev.bvhNodeOff = off;
+    R.dev.bvhRoot = R.tree.root == BVH_END ? -1 : int(R.tree.root);
+    R.built = false;
+    R.sinceBuild = 0;
+  }
+  void freeBvh(WorldRec& R) {
+    if (R.bvh) bvhA.release(R.bvhOff, std::max(R.tree.nodes, 1));
   }
 
   int takeSlot() {
@@ -707,11 +807,15 @@ class Arena {
     ensureRoom(d.n_bodies, jointsOf(d), initialPairCap(d.n_bodies));  // may move W: before any reference into it
     const int w = takeSlot();
     WorldRec& R = W[w];
+    bool placed = false;
     try {
       worldParams(d, p, R);
       R.dev.largeOff = w * MAX_LARGE;
       placeRanges(R, initialPairCap(d.n_bodies));
+      placed = true;
+      placeBvh(R);
     } catch (...) {
+      if (placed) freeRanges(R);
       R = WorldRec();
       freeSlots.push_back(w);
       throw;
@@ -798,12 +902,17 @@ class Arena {
     jointA.release(R.dev.jointOff, R.nJoints);
     slotA.release(R.dev.pairOff, R.dev.pairCap);
   }
+  // everything a resident world holds in the arena
+  void freeResident(WorldRec& R) {
+    freeRanges(R);
+    freeBvh(R);
+  }
 
   void removeWorld(int w) {
     if (w < 0 || w >= maxWorlds || !W[w].live) throw Error(AVBD_E_INVALID, "no such world");
     CK(cudaStreamSynchronize(s));
     WorldRec& R = W[w];
-    if (R.resident) freeRanges(R);
+    if (R.resident) freeResident(R);
     R = WorldRec();
     freeSlots.push_back(w);
     rebuildNoCollide();
@@ -853,7 +962,7 @@ class Arena {
     getRange(S->counts, P.count, base, np);
     getRange(S->basis, P.basis, 3 * base, 3 * size_t(np));
     getRange(S->ct, P.ct, 32 * base, 32 * size_t(np));
-    freeRanges(R);
+    freeResident(R);
     R.resident = false;
     R.snap = std::move(S);
     evictions++;
@@ -873,6 +982,7 @@ class Arena {
     Snapshot& S = *R.snap;
     const int np = int(S.pairs.size());
     placeRanges(R, restoreSlots(w));
+    placeBvh(R);  // the tree is rebuilt at the next step (it only shapes the candidate search)
     const size_t off = R.dev.bodyOff, joff = R.dev.jointOff;
     float4* bdst[11] = {B.pos, B.rot, B.pos0, B.rot0, B.posY, B.rotY, B.vel, B.ang, B.vprev, B.size, B.mass};
     for (int k = 0; k < 11; k++) putRange(bdst[k], off, S.body[k]);
@@ -1027,6 +1137,26 @@ class Arena {
     if (na) CK(cudaMemcpyAsync(active, activeHost, sizeof(int4) * na, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(wactive, wactiveHost, sizeof(int) * maxWorlds, cudaMemcpyHostToDevice, s));
     lastActive = act;
+    // broadphase trees: rebuild every bvhRebuild steps, refit in between (before the pair passes;
+    // an overflow re-run below reuses them, the poses being unchanged)
+    {
+      cudaEvent_t b0 = nullptr;
+      for (int w : act) {
+        WorldRec& R = W[w];
+        if (!R.bvh || R.nBodies == 0) continue;
+        if (prof && !b0) b0 = mark();
+        if (!R.built || R.sinceBuild >= R.bvhRebuild) {
+          ensureBvhScratch(R);
+          launch_bvh_build(B, R.dev.bodyOff, R.nBodies, G.bvh, R.bvhOff, R.tree, bsc, scanTemp, s);
+          R.built = true;
+          R.sinceBuild = 0;
+        } else {
+          launch_bvh_refit(B, R.dev.bodyOff, R.nBodies, G.bvh, R.bvhOff, R.tree, s);
+        }
+        R.sinceBuild++;
+      }
+      if (b0) span(P_COLLIDE, b0, mark());
+    }
     long long budget = 0;
     for (int attempt = 0;; attempt++) {
       budget = 0;

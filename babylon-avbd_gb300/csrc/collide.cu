@@ -85,7 +85,7 @@ __global__ void k_grid_count(const float4* __restrict__ pos, const int4* __restr
     const float4 p = pos[i];
     const int w = meta[i].x;
     const WorldDev& W = worlds[w];
-    if (p.w > W.largeR) {
+    if (p.w > W.largeR || (W.flags & FLAG_BVH)) {  // large, or found through the world's tree
       bodyBucket[i] = -1;
       continue;
     }
@@ -170,6 +170,42 @@ __device__ __forceinline__ bool pair_test(const PairCtx& c, int hi, int lo, floa
   return true;
 }
 
+// Lower-index partners from the world's tree: stackless traversal along escape links of every
+// node whose box meets body i's (bounding sphere box, widened by a margin far above the rounding
+// of the boxes) and whose subtree holds a lower index.
+template <class Emit>
+__device__ __forceinline__ void tree_partners(const PairCtx& c, const WorldDev& W, const Grid& g, int i, float4 pA, float mA, int4 metaA,
+                                              Emit emit) {
+  if (W.bvhRoot < 0) return;
+  const uint32_t local = uint32_t(i - W.bodyOff);
+  const float eps = 1e-3f + 1e-6f * (fabsf(pA.x) + fabsf(pA.y) + fabsf(pA.z));
+  const float r = pA.w + eps;
+  const float lx = pA.x - r, ly = pA.y - r, lz = pA.z - r, hx = pA.x + r, hy = pA.y + r, hz = pA.z + r;
+  const float4* node = g.bvh.node + 2 * size_t(W.bvhNodeOff);
+  const uint32_t* escape = g.bvh.escape + W.bvhNodeOff;
+  const uint32_t* minIdx = g.bvh.minIdx + W.bvhNodeOff;
+  uint32_t at = uint32_t(W.bvhRoot);
+  // every node is entered at most once; the bound only guards against a damaged tree
+  for (int guard = 4 * W.bodyCount + 8; at != BVH_END && guard > 0; guard--) {
+    if (minIdx[at] >= local) {
+      at = escape[at];
+      continue;
+    }
+    const float4 lo = node[2 * size_t(at)], hi = node[2 * size_t(at) + 1];
+    if (hi.x < lx || hi.y < ly || hi.z < lz || lo.x > hx || lo.y > hy || lo.z > hz) {
+      at = escape[at];
+      continue;
+    }
+    if (__float_as_uint(hi.w) == BVH_END) {  // leaf
+      const int j = W.bodyOff + int(__float_as_uint(lo.w));
+      if (pair_test(c, i, j, pA, c.pos[j], mA, metaA)) emit(j);
+      at = escape[at];
+    } else {
+      at = __float_as_uint(lo.w);
+    }
+  }
+}
+
 // Enumerate the lower-index partners of body i; emit(j) for each pair (i, j).
 template <class Emit>
 __device__ __forceinline__ void for_each_partner(const PairCtx& c, const WorldDev* __restrict__ worlds, const Grid& g, int i, Emit emit) {
@@ -178,6 +214,10 @@ __device__ __forceinline__ void for_each_partner(const PairCtx& c, const WorldDe
   const int4 metaA = c.meta[i];
   const int w = metaA.x;
   const WorldDev W = worlds[w];
+  if (W.flags & FLAG_BVH) {
+    tree_partners(c, W, g, i, pA, mA, metaA, emit);
+    return;
+  }
   const bool small = !(pA.w > W.largeR);
   if (small) {
     const int cx = cell_coord(pA.x, W.cell), cy = cell_coord(pA.y, W.cell), cz = cell_coord(pA.z, W.cell);

@@ -21,6 +21,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <vector>
+
 #include "avbd_math.cuh"
 
 namespace avbd {
@@ -41,6 +43,7 @@ constexpr int KIND_SPRING = 1;
 
 constexpr int FLAG_MASS_PENALTY = 1;
 constexpr int FLAG_FACE_BIAS = 2;
+constexpr int FLAG_BVH = 4;  // broadphase by the world's bounding-volume hierarchy (bvh.cu)
 
 // Per-world parameters and ranges (96 bytes).
 struct WorldDev {
@@ -50,7 +53,7 @@ struct WorldDev {
   int iterations;
   int flags, bodyOff, bodyCount, largeOff;
   int largeCount, jointOff, jointCount, pairOff;
-  int pairCap, pad0, pad1, pad2;
+  int pairCap, bvhNodeOff, bvhRoot, pad0;  // bvhRoot: local node id (-1: empty tree)
 };
 
 struct BodyPtrs {
@@ -109,6 +112,19 @@ struct Counters {
 
 constexpr int PAIR_TMP = 16;  // partners a body keeps from the enumerating pass (more: enumerated again)
 
+// Bounding-volume hierarchies of the worlds that use one, in one pool of nodes (each world a
+// range starting at WorldDev::bvhNodeOff; node ids below are local to the range). A node is two
+// float4: (lo.xyz, left) and (hi.xyz, right); a leaf has right == BVH_END and left = its body's
+// local index.
+constexpr uint32_t BVH_END = 0xffffffffu;
+constexpr int BVH_WIDTH = 16;  // clusters per treelet
+struct BvhPool {
+  float4* node;      // 2 per node
+  uint32_t* parent;  // per node (BVH_END: root or unused)
+  uint32_t* escape;  // per node: where traversal continues after its subtree (BVH_END: done)
+  uint32_t* minIdx;  // per node: least local body index below it
+};
+
 struct Grid {
   uint32_t tableMask;  // hash table size - 1 (power of two)
   int* cellCount;      // table + 1 (scanned in place to starts)
@@ -119,6 +135,7 @@ struct Grid {
   int* bodyBucket;     // per body (-1: large)
   int* large;          // MAX_LARGE slots per world: its large bodies, ascending
   uint32_t* pairTmp;   // PAIR_TMP partners per active body: partner m of list position k at m * nBodies + k
+  BvhPool bvh;         // trees of the worlds with FLAG_BVH
 };
 
 // Narrowphase scratch (per tick), indexed by position q in the tick's active pair list: SAT
@@ -169,6 +186,30 @@ void launch_pairs(const BodyPtrs& b, const WorldDev* worlds, Tick t, Grid g, NoC
                   PairPtrs P, Counters* ctr, void* scanTemp, cudaStream_t s);
 void launch_narrowphase(const BodyPtrs& b, const WorldDev* worlds, Tick t, PairPtrs P, NarrowScratch ns, const Counters* ctr,
                         int pairBudget, cudaStream_t s);
+
+// bvh.cu
+struct BvhLevel {
+  int inputCount, nodeBase, inputOffset, outputOffset, blocks;
+};
+struct BvhLayout {
+  std::vector<BvhLevel> levels;
+  uint32_t root = BVH_END;
+  int nodes = 0;     // node ids in use: [0, nodes)
+  int clusters = 0;  // cluster-list entries the build needs
+};
+struct BvhScratch {
+  uint2* keys[2];     // Morton keys, ping-pong
+  int* hist;          // radix digit counts
+  uint32_t* clusters;
+  float4* bounds;     // per-block bounds, then the scene bounds
+};
+void bvh_layout(int n, BvhLayout& L);
+size_t bvh_scratch_keys(int n);
+size_t bvh_scratch_hist(int n);
+size_t bvh_scratch_bounds(int n);
+void launch_bvh_build(const BodyPtrs& b, int bodyOff, int n, BvhPool pool, int nodeOff, const BvhLayout& L, BvhScratch sc,
+                      void* scanTemp, cudaStream_t s);
+void launch_bvh_refit(const BodyPtrs& b, int bodyOff, int n, BvhPool pool, int nodeOff, const BvhLayout& L, cudaStream_t s);
 
 // solve.cu
 void launch_joint_prepare(const BodyPtrs& b, JointPtrs j, int j0, int j1, cudaStream_t s);

@@ -49,7 +49,7 @@ def args_parse():
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    p.add_argument("--workload", choices=["world_mix", "box_pile", "served"], default="world_mix")
+    p.add_argument("--workload", choices=["world_mix", "box_pile", "cloth_wall", "served"], default="world_mix")
     p.add_argument("--requests", type=int, default=20_000, help="served: requests per stream")
     p.add_argument("--rates", default="2000,10000,50000", help="served: Poisson arrival rates (req/s)")
     p.add_argument("--serve-rate", type=float, default=10_000.0, help="rate of the served stream in the default line")
@@ -156,7 +156,14 @@ class Clocks:
 def build_worlds(args, rank):
     from avbd_gb300 import workloads
     if args.workload == "box_pile":
-        return [workloads.box_pile_c0()], {"workload": "box_pile_c0", "bodies": 1001}
+        return [workloads.box_pile_c0()], {"workload": "box_pile_c0", "bodies": 1001, "iterations": 10,
+                                           "l2": "one 1,001-body world: L2-resident (launch-bound)"}
+    if args.workload == "cloth_wall":
+        w = workloads.cloth_wall()
+        return [w], {"workload": "cloth_wall", "bodies": int(w.n_bodies), "joints": int(w.n_cons), "iterations": 15,
+                     "cloth": "256x256 boxes of 0.1 m, ball joints, two corners pinned, over a static 5 m sphere",
+                     "wall": "100x2x50 bricks of 1x0.5x0.5 m hit by a 2 m sphere at 40 m/s",
+                     "l2": "inputs larger than L2 (no flush needed)"}
     seed = workloads.SEED_BASE + 3 + 1000 * rank
     worlds, counts, sigma = workloads.world_mix(args.worlds, target=int(2_100_000 * args.worlds / 4096), seed=seed)
     cfg = {"workload": f"world_mix_{args.worlds}", "worlds": args.worlds, "bodies": int(counts.sum() + len(counts)),

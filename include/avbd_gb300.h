@@ -51,7 +51,17 @@ typedef struct avbd_params {
   int32_t mass_penalty; /* contact normal penalty floor min(mA, mB)/dt^2 */
   int32_t face_bias;    /* prefer face axes in box-box SAT (cpuBoxContacts3D.ts:457-466) */
   int32_t color_rounds; /* Jones-Plassmann round budget per step */
+  int32_t broadphase;   /* options.broadphase (src/native/scenes.d.ts:299-300): AVBD_BROADPHASE_* */
+  int32_t bvh_rebuild;  /* options.bvh.rebuildInterval: steps between tree rebuilds; <= 0: 16 */
 } avbd_params;
+
+/* Candidate search. Both give the same pair set; the tree (hierarchical PLOC, src/gpu/gpuHploc.js)
+ * suits large worlds whose grid cells would be large against most bodies. AUTO follows
+ * src/gpu/appGpuSolver3D.js:333-398: the tree for >= 10,000 bodies when the grid cell is >= 4x
+ * twice the median radius or the world is a jointed sheet of thin plates. */
+#define AVBD_BROADPHASE_GRID 0
+#define AVBD_BROADPHASE_HPLOC 1
+#define AVBD_BROADPHASE_AUTO 2
 
 /* A built scene as flat structure-of-arrays in creation order (what AvbdScene3D holds,
  * src/native/scenes.js:107-698). Optional arrays may be NULL (defaults in brackets). */
