@@ -131,7 +131,8 @@ namespace avbd {
 
 // World state kept on the host while a world is evicted (all indices world-local).
 struct Snapshot {
-  std::vector<float4> body[11];  // pos rot pos0 rot0 posY rotY vel ang vprev size mass
+  std::vector<float4> pose, pose0, poseY;          // (pos, rot) pairs
+  std::vector<float4> vel, ang, vprev, size, mass;  // one per body
   std::vector<int4> meta;
   std::vector<int2> jab;
   std::vector<float4> joint[10];  // rA rB stiff penLin penAng lamLin lamAng C0Lin C0Ang restQ
@@ -272,8 +273,8 @@ class Arena {
     W.resize(nw);
     for (int w = nw - 1; w >= 0; w--) freeSlots.push_back(w);
     const size_t N = size_t(nb), NJ = size_t(nj);
-    for (float4** p : {&B.pos, &B.rot, &B.pos0, &B.rot0, &B.posY, &B.rotY, &B.vel, &B.ang, &B.vprev, &B.size, &B.mass})
-      *p = dalloc<float4>(N);
+    for (float4** p : {&B.pose, &B.pose0, &B.poseY}) *p = dalloc<float4>(2 * N);
+    for (float4** p : {&B.vel, &B.ang, &B.vprev, &B.size, &B.mass}) *p = dalloc<float4>(N);
     B.meta = dalloc<int4>(N);
     J.ab = dalloc<int2>(NJ);
     for (float4** p : {&J.rA, &J.rB, &J.stiff, &J.penLin, &J.penAng, &J.lamLin, &J.lamAng, &J.C0Lin, &J.C0Ang, &J.restQ})
@@ -328,7 +329,7 @@ class Arena {
   }
 
   void release() {
-    void* ptrs[] = {B.pos, B.rot, B.pos0, B.rot0, B.posY, B.rotY, B.vel, B.ang, B.vprev, B.size, B.mass, B.meta, J.ab, J.rA,
+    void* ptrs[] = {B.pose, B.pose0, B.poseY, B.vel, B.ang, B.vprev, B.size, B.mass, B.meta, J.ab, J.rA,
                     J.rB, J.stiff, J.penLin, J.penAng, J.lamLin, J.lamAng, J.C0Lin, J.C0Ang, J.restQ, J.broken, worlds,
                     which, pairN, wover, wactive, active, activeBodies, activeJoints, pairPrefix, pairCount, G.cellCount,
                     G.cellFill, G.cellBodies, G.cellKey, G.cellPos, G.pairTmp, G.bodyBucket, G.large, T.adjStart, T.adjFill, T.activeIndex, T.color, T.won,
@@ -415,8 +416,8 @@ class Arena {
     if (nb <= bodyCap) return;
     flush();
     const size_t o = size_t(bodyCap), N = size_t(nb);
-    for (float4** p : {&B.pos, &B.rot, &B.pos0, &B.rot0, &B.posY, &B.rotY, &B.vel, &B.ang, &B.vprev, &B.size, &B.mass})
-      regrow(*p, o, N);
+    for (float4** p : {&B.pose, &B.pose0, &B.poseY}) regrow(*p, 2 * o, 2 * N);
+    for (float4** p : {&B.vel, &B.ang, &B.vprev, &B.size, &B.mass}) regrow(*p, o, N);
     regrow(B.meta, o, N);
     int* c = dalloc<int>(2 * N);  // both colour buffers, stride = capacity
     CK(cudaMemcpyAsync(c, T.color, o * 4, cudaMemcpyDeviceToDevice, s));
@@ -845,10 +846,15 @@ class Arena {
         const uint32_t grp = d.group ? d.group[i] : 0xffffffffu, msk = d.collides_with ? d.collides_with[i] : 0xffffffffu;
         meta[i] = make_int4(w, d.shape[i], int(grp), int(msk));
       }
-      const float4* src[11] = {pos.data(), rot.data(), pos.data(), rot.data(), pos.data(), rot.data(), vel.data(), ang.data(),
-                               vprev.data(), size.data(), mass.data()};
-      float4* dst[11] = {B.pos, B.rot, B.pos0, B.rot0, B.posY, B.rotY, B.vel, B.ang, B.vprev, B.size, B.mass};
-      for (int k = 0; k < 11; k++) put(dst[k] + off, src[k], n * 16);
+      std::vector<float4> pose(2 * n);
+      for (size_t i = 0; i < n; i++) {
+        pose[2 * i] = pos[i];
+        pose[2 * i + 1] = rot[i];
+      }
+      for (float4* d : {B.pose, B.pose0, B.poseY}) put(d + 2 * off, pose.data(), 2 * n * 16);
+      const float4* src[5] = {vel.data(), ang.data(), vprev.data(), size.data(), mass.data()};
+      float4* dst[5] = {B.vel, B.ang, B.vprev, B.size, B.mass};
+      for (int k = 0; k < 5; k++) put(dst[k] + off, src[k], n * 16);
       put(B.meta + off, meta.data(), n * 16);
       std::vector<int> minus(n, -1);
       put(T.color + off, minus.data(), n * 4);
@@ -940,8 +946,14 @@ class Arena {
     CK(cudaStreamSynchronize(s));
     auto S = std::make_unique<Snapshot>();
     const size_t off = R.dev.bodyOff, n = R.nBodies, joff = R.dev.jointOff, nj = R.nJoints;
-    const float4* bsrc[11] = {B.pos, B.rot, B.pos0, B.rot0, B.posY, B.rotY, B.vel, B.ang, B.vprev, B.size, B.mass};
-    for (int k = 0; k < 11; k++) getRange(S->body[k], bsrc[k], off, n);
+    getRange(S->pose, B.pose, 2 * off, 2 * n);
+    getRange(S->pose0, B.pose0, 2 * off, 2 * n);
+    getRange(S->poseY, B.poseY, 2 * off, 2 * n);
+    getRange(S->vel, B.vel, off, n);
+    getRange(S->ang, B.ang, off, n);
+    getRange(S->vprev, B.vprev, off, n);
+    getRange(S->size, B.size, off, n);
+    getRange(S->mass, B.mass, off, n);
     getRange(S->meta, B.meta, off, n);
     getRange(S->jab, J.ab, joff, nj);
     for (auto& ab : S->jab) {
@@ -984,8 +996,14 @@ class Arena {
     placeRanges(R, restoreSlots(w));
     placeBvh(R);  // the tree is rebuilt at the next step (it only shapes the candidate search)
     const size_t off = R.dev.bodyOff, joff = R.dev.jointOff;
-    float4* bdst[11] = {B.pos, B.rot, B.pos0, B.rot0, B.posY, B.rotY, B.vel, B.ang, B.vprev, B.size, B.mass};
-    for (int k = 0; k < 11; k++) putRange(bdst[k], off, S.body[k]);
+    putRange(B.pose, 2 * off, S.pose);
+    putRange(B.pose0, 2 * off, S.pose0);
+    putRange(B.poseY, 2 * off, S.poseY);
+    putRange(B.vel, off, S.vel);
+    putRange(B.ang, off, S.ang);
+    putRange(B.vprev, off, S.vprev);
+    putRange(B.size, off, S.size);
+    putRange(B.mass, off, S.mass);
     putRange(B.meta, off, S.meta);
     for (auto& ab : S.jab) {
       if (ab.x >= 0) ab.x += int(off);
@@ -1285,13 +1303,16 @@ class Arena {
       auto h = fetch(d, off, n);
       for (size_t i = 0; i < n; i++) { out[3 * i] = h[i].x; out[3 * i + 1] = h[i].y; out[3 * i + 2] = h[i].z; }
     };
-    put3(position, B.pos);
     put3(velocity, B.vel);
     put3(angular, B.ang);
     put3(prevVel, B.vprev);
-    if (rotation) {
-      auto h = fetch(B.rot, off, n);
-      for (size_t i = 0; i < n; i++) { rotation[4 * i] = h[i].x; rotation[4 * i + 1] = h[i].y; rotation[4 * i + 2] = h[i].z; rotation[4 * i + 3] = h[i].w; }
+    if (position || rotation) {
+      auto h = fetch(B.pose, 2 * off, 2 * n);
+      for (size_t i = 0; i < n; i++) {
+        const float4 p = h[2 * i], q = h[2 * i + 1];
+        if (position) { position[3 * i] = p.x; position[3 * i + 1] = p.y; position[3 * i + 2] = p.z; }
+        if (rotation) { rotation[4 * i] = q.x; rotation[4 * i + 1] = q.y; rotation[4 * i + 2] = q.z; rotation[4 * i + 3] = q.w; }
+      }
     }
   }
 

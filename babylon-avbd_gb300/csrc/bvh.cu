@@ -43,13 +43,13 @@ __device__ __forceinline__ void store_node(float4* node, uint32_t id, float3 lo,
 }
 
 // Leaf boxes (bounding sphere of each body) and per-block scene bounds.
-__global__ void k_bvh_leaves(const float4* __restrict__ pos, int bodyOff, int n, BvhPool b, int nodeOff, float4* blockBounds,
+__global__ void k_bvh_leaves(const float4* __restrict__ pose, int bodyOff, int n, BvhPool b, int nodeOff, float4* blockBounds,
                              int withBounds) {
   __shared__ float3 slo[256], shi[256];
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   float3 lo = make_float3(3.402823e38f, 3.402823e38f, 3.402823e38f), hi = make_float3(-3.402823e38f, -3.402823e38f, -3.402823e38f);
   if (i < n) {
-    const float4 p = pos[bodyOff + i];
+    const float4 p = pose[2 * size_t(bodyOff + i)];
     lo = make_float3(p.x - p.w, p.y - p.w, p.z - p.w);
     hi = make_float3(p.x + p.w, p.y + p.w, p.z + p.w);
     store_node(b.node, uint32_t(nodeOff + i), lo, uint32_t(i), hi, BVH_END);
@@ -326,7 +326,7 @@ void launch_bvh_build(const BodyPtrs& bd, int bodyOff, int n, BvhPool b, int nod
   const int lb = blocks_of(n, 256);
   k_bvh_init_links<<<blocks_of(L.nodes, 256) > 152 * 8 ? 152 * 8 : blocks_of(L.nodes, 256), 256, 0, s>>>(b, nodeOff, L.nodes);
   float4* bounds = sc.bounds + 2 * size_t(lb);
-  k_bvh_leaves<<<lb, 256, 0, s>>>(bd.pos, bodyOff, n, b, nodeOff, sc.bounds, 1);
+  k_bvh_leaves<<<lb, 256, 0, s>>>(bd.pose, bodyOff, n, b, nodeOff, sc.bounds, 1);
   k_bvh_bounds<<<1, 256, 0, s>>>(sc.bounds, lb, bounds);
   k_bvh_morton<<<lb, 256, 0, s>>>(b, nodeOff, n, bounds, sc.keys[0]);
   note_launches(4);
@@ -353,7 +353,7 @@ void launch_bvh_build(const BodyPtrs& bd, int bodyOff, int n, BvhPool b, int nod
 
 void launch_bvh_refit(const BodyPtrs& bd, int bodyOff, int n, BvhPool b, int nodeOff, const BvhLayout& L, cudaStream_t s) {
   if (n <= 0) return;
-  k_bvh_leaves<<<blocks_of(n, 256), 256, 0, s>>>(bd.pos, bodyOff, n, b, nodeOff, nullptr, 0);
+  k_bvh_leaves<<<blocks_of(n, 256), 256, 0, s>>>(bd.pose, bodyOff, n, b, nodeOff, nullptr, 0);
   note_launches(1);
   for (const BvhLevel& v : L.levels) {
     k_bvh_refit_treelets<<<blocks_of(v.blocks, 64), 64, 0, s>>>(b, nodeOff, v.inputCount, v.nodeBase);

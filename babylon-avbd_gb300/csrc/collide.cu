@@ -78,11 +78,11 @@ __global__ void k_tick_lists(Tick t, const WorldDev* __restrict__ worlds, Topo t
   }
 }
 
-__global__ void k_grid_count(const float4* __restrict__ pos, const int4* __restrict__ meta, const WorldDev* __restrict__ worlds,
+__global__ void k_grid_count(const float4* __restrict__ pose, const int4* __restrict__ meta, const WorldDev* __restrict__ worlds,
                              Tick t, uint32_t mask, int* __restrict__ cellCount, int* __restrict__ bodyBucket) {
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < t.nBodies; k += gridDim.x * blockDim.x) {
     const int i = t.bodies[k];
-    const float4 p = pos[i];
+    const float4 p = pose[2 * size_t(i)];
     const int w = meta[i].x;
     const WorldDev& W = worlds[w];
     if (p.w > W.largeR || (W.flags & FLAG_BVH)) {  // large, or found through the world's tree
@@ -98,13 +98,13 @@ __global__ void k_grid_count(const float4* __restrict__ pos, const int4* __restr
 // Bucket the small bodies; each bucket entry also records its body's cell and position, so the
 // pair passes read candidates from contiguous memory and skip bodies of other cells or worlds
 // that share a hash bucket.
-__global__ void k_grid_scatter(const float4* __restrict__ pos, const int4* __restrict__ meta, const WorldDev* __restrict__ worlds,
+__global__ void k_grid_scatter(const float4* __restrict__ pose, const int4* __restrict__ meta, const WorldDev* __restrict__ worlds,
                                Tick t, Grid g) {
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < t.nBodies; k += gridDim.x * blockDim.x) {
     const int i = t.bodies[k];
     const int b = g.bodyBucket[i];
     if (b < 0) continue;
-    const float4 p = pos[i];
+    const float4 p = pose[2 * size_t(i)];
     const int w = meta[i].x;
     const float cell = worlds[w].cell;
     const int slot = g.cellCount[b] + atomicAdd(&g.cellFill[b], 1);
@@ -125,15 +125,16 @@ void launch_grid_build(const BodyPtrs& b, const WorldDev* worlds, Tick t, Grid g
   cudaMemsetAsync(g.cellCount, 0, sizeof(int) * (table + 1), s);
   cudaMemsetAsync(g.cellFill, 0, sizeof(int) * table, s);
   if (t.nBodies == 0) return;
-  k_grid_count<<<grid_blocks(t.nBodies, 256), 256, 0, s>>>(b.pos, b.meta, worlds, t, g.tableMask, g.cellCount, g.bodyBucket); note_launches(1);
+  k_grid_count<<<grid_blocks(t.nBodies, 256), 256, 0, s>>>(b.pose, b.meta, worlds, t, g.tableMask, g.cellCount, g.bodyBucket); note_launches(1);
   scan_exclusive(g.cellCount, table + 1, nullptr, scanTemp, s);
-  k_grid_scatter<<<grid_blocks(t.nBodies, 256), 256, 0, s>>>(b.pos, b.meta, worlds, t, g); note_launches(1);
+  k_grid_scatter<<<grid_blocks(t.nBodies, 256), 256, 0, s>>>(b.pose, b.meta, worlds, t, g); note_launches(1);
 }
 
 // ------------------------------------------------------------------ pair predicate
 
 struct PairCtx {
-  const float4* __restrict__ pos;
+  const float4* __restrict__ pose;  // (pos, rot) pairs
+  __device__ __forceinline__ float4 pos(int i) const { return pose[2 * size_t(i)]; }
   const float4* __restrict__ mass;
   const int4* __restrict__ meta;
   NoCollide nc;
@@ -198,7 +199,7 @@ __device__ __forceinline__ void tree_partners(const PairCtx& c, const WorldDev& 
     }
     if (__float_as_uint(hi.w) == BVH_END) {  // leaf
       const int j = W.bodyOff + int(__float_as_uint(lo.w));
-      if (pair_test(c, i, j, pA, c.pos[j], mA, metaA)) emit(j);
+      if (pair_test(c, i, j, pA, c.pos(j), mA, metaA)) emit(j);
       at = escape[at];
     } else {
       at = __float_as_uint(lo.w);
@@ -209,7 +210,7 @@ __device__ __forceinline__ void tree_partners(const PairCtx& c, const WorldDev& 
 // Enumerate the lower-index partners of body i; emit(j) for each pair (i, j).
 template <class Emit>
 __device__ __forceinline__ void for_each_partner(const PairCtx& c, const WorldDev* __restrict__ worlds, const Grid& g, int i, Emit emit) {
-  const float4 pA = c.pos[i];
+  const float4 pA = c.pos(i);
   const float mA = c.mass[i].x;
   const int4 metaA = c.meta[i];
   const int w = metaA.x;
@@ -245,11 +246,11 @@ __device__ __forceinline__ void for_each_partner(const PairCtx& c, const WorldDe
   for (int k = 0; k < W.largeCount; k++) {
     const int L = g.large[W.largeOff + k];
     if (L >= i) break;
-    if (pair_test(c, i, L, pA, c.pos[L], mA, metaA)) emit(L);
+    if (pair_test(c, i, L, pA, c.pos(L), mA, metaA)) emit(L);
   }
   if (!small) {
     for (int j = W.bodyOff; j < i; j++) {
-      const float4 pB = c.pos[j];
+      const float4 pB = c.pos(j);
       if (pB.w > W.largeR) continue;  // large partners came from the list above
       if (pair_test(c, i, j, pA, pB, mA, metaA)) emit(j);
     }
@@ -344,7 +345,7 @@ __global__ void k_pair_slots(const WorldDev* __restrict__ worlds, Tick t, const 
 
 void launch_pairs(const BodyPtrs& b, const WorldDev* worlds, Tick t, Grid g, NoCollide nc, const int* jbroken, int* pairCount,
                   PairPtrs P, Counters* ctr, void* scanTemp, cudaStream_t s) {
-  PairCtx c{b.pos, b.mass, b.meta, nc, jbroken};
+  PairCtx c{b.pose, b.mass, b.meta, nc, jbroken};
   cudaMemsetAsync(ctr, 0, 2 * sizeof(int), s);  // activePairs, overflowWorlds
   if (t.nActive == 0) return;
   k_pair_count<<<grid_blocks(t.nBodies + 1, 128), 128, 0, s>>>(c, worlds, g, t, pairCount); note_launches(1);
@@ -938,7 +939,7 @@ __global__ void __launch_bounds__(256) k_np_classify(BodyPtrs bd, const WorldDev
       } else {
         const WorldDev& W = worlds[bd.meta[a].x];
         box::Sat best;
-        if (box::sat(bd.pos[a], bd.rot[a], bd.size[a], bd.pos[b], bd.rot[b], bd.size[b], (W.flags & FLAG_FACE_BIAS) != 0, best)) {
+        if (box::sat(bd.pos(a), bd.rot(a), bd.size[a], bd.pos(b), bd.rot(b), bd.size[b], (W.flags & FLAG_FACE_BIAS) != 0, best)) {
           boxHit = true;
           ns.sat[q] = make_float4(best.n.x, best.n.y, best.n.z, __int_as_float(best.type | ((best.ia & 0xff) << 8) | ((best.ib & 0xff) << 16)));
         } else {
@@ -960,8 +961,8 @@ __global__ void __launch_bounds__(128) k_np_box(BodyPtrs bd, const WorldDev* __r
     const int p = t.pairs[q];
     const uint2 key = cur.pair[p];
     const int a = int(key.x), b = int(key.y);
-    const float4 pA = bd.pos[a], qA = bd.rot[a], sA = bd.size[a];
-    const float4 pB = bd.pos[b], qB = bd.rot[b], sB = bd.size[b];
+    const float4 pA = bd.pos(a), qA = bd.rot(a), sA = bd.size[a];
+    const float4 pB = bd.pos(b), qB = bd.rot(b), sB = bd.size[b];
     const WorldDev& W = worlds[bd.meta[a].x];
     const float4 sr = ns.sat[q];
     const int code = __float_as_int(sr.w);
@@ -992,8 +993,8 @@ __global__ void __launch_bounds__(128) k_np_sphere(BodyPtrs bd, const WorldDev* 
     const int p = ns.sphereList[k];
     const uint2 key = cur.pair[p];
     const int a = int(key.x), b = int(key.y);
-    const float4 pA = bd.pos[a], qA = bd.rot[a], sA = bd.size[a];
-    const float4 pB = bd.pos[b], qB = bd.rot[b], sB = bd.size[b];
+    const float4 pA = bd.pos(a), qA = bd.rot(a), sA = bd.size[a];
+    const float4 pB = bd.pos(b), qB = bd.rot(b), sB = bd.size[b];
     const int shA = bd.meta[a].y, shB = bd.meta[b].y;
     const WorldDev& W = worlds[bd.meta[a].x];
     M33 basis{V3{0, 0, 0}, V3{0, 0, 0}, V3{0, 0, 0}};

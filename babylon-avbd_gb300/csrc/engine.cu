@@ -32,7 +32,7 @@ __global__ void k_read_selected(BodyPtrs bd, const WorldDev* __restrict__ worlds
                                 int posesOnly, float* __restrict__ out) {
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
     const int i = off + int(idx[k]);
-    const float4 p = bd.pos[i], q = bd.rot[i], sz = bd.size[i];
+    const float4 p = bd.pos(i), q = bd.rot(i), sz = bd.size[i];
     if (posesOnly) {
       float* o = out + size_t(k) * 8;
       o[0] = p.x; o[1] = p.y; o[2] = p.z; o[3] = sz.w;
@@ -40,7 +40,7 @@ __global__ void k_read_selected(BodyPtrs bd, const WorldDev* __restrict__ worlds
       continue;
     }
     float* o = out + size_t(k) * 40;
-    const float4 p0 = bd.pos0[i], q0 = bd.rot0[i], m = bd.mass[i], py = bd.posY[i], qy = bd.rotY[i];
+    const float4 p0 = bd.pos0(i), q0 = bd.rot0(i), m = bd.mass[i], py = bd.posY(i), qy = bd.rotY(i);
     const float4 v = bd.vel[i], w = bd.ang[i], vp = bd.vprev[i];
     const int4 meta = bd.meta[i];
     const WorldDev& W = worlds[meta.x];
@@ -61,9 +61,9 @@ __global__ void k_set_poses(BodyPtrs bd, const uint32_t* __restrict__ idx, int n
                             const float* __restrict__ rot) {
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
     const int i = off + int(idx[k]);
-    const float r = bd.pos[i].w;
-    bd.pos[i] = make_float4(pos[3 * k], pos[3 * k + 1], pos[3 * k + 2], r);
-    if (rot) bd.rot[i] = qnormalize(make_float4(rot[4 * k], rot[4 * k + 1], rot[4 * k + 2], rot[4 * k + 3]));
+    const float r = bd.pos(i).w;
+    bd.pos(i) = make_float4(pos[3 * k], pos[3 * k + 1], pos[3 * k + 2], r);
+    if (rot) bd.rot(i) = qnormalize(make_float4(rot[4 * k], rot[4 * k + 1], rot[4 * k + 2], rot[4 * k + 3]));
   }
 }
 
@@ -76,12 +76,11 @@ __global__ void k_set_velocities(BodyPtrs bd, const uint32_t* __restrict__ idx, 
   }
 }
 
-__global__ void k_read_poses(const float4* __restrict__ pos, const float4* __restrict__ rot, const float4* __restrict__ size, int n,
-                             float4* __restrict__ out) {
+__global__ void k_read_poses(const float4* __restrict__ pose, const float4* __restrict__ size, int n, float4* __restrict__ out) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const float4 p = pos[i];
-    out[2 * i] = make_float4(p.x, p.y, p.z, size[i].w);
-    out[2 * i + 1] = rot[i];
+    const float4 p = pose[2 * size_t(i)];
+    out[2 * size_t(i)] = make_float4(p.x, p.y, p.z, size[i].w);
+    out[2 * size_t(i) + 1] = pose[2 * size_t(i) + 1];
   }
 }
 
@@ -549,7 +548,7 @@ int avbd_batch_read_poses(avbd_batch* b, float* out) {
   if (!A.poseStage) A.poseStage = dalloc<float4>(size_t(n) * 2);
   int blocks = grid_blocks(n, 256);
   if (blocks > 152 * 8) blocks = 152 * 8;
-  k_read_poses<<<blocks, 256, 0, A.s>>>(A.B.pos, A.B.rot, A.B.size, n, A.poseStage); note_launches(1);
+  k_read_poses<<<blocks, 256, 0, A.s>>>(A.B.pose, A.B.size, n, A.poseStage); note_launches(1);
   CK(cudaMemcpyAsync(out, A.poseStage, size_t(n) * 32, cudaMemcpyDeviceToHost, A.s));
   CK(cudaStreamSynchronize(A.s));
   API_END

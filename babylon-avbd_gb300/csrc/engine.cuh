@@ -2,9 +2,9 @@
 // and the host orchestration (engine.cu). Not part of the C ABI.
 //
 // Every world is a self-contained segment of one arena in HBM:
-//   bodies   a contiguous range of the body arrays (structure of arrays, one float4 per field):
-//            pos(xyz, bounding radius) rot pos0(x-) rot0 posY(inertial) rotY vel ang vprev
-//            size(xyz, friction) mass(m, Ix, Iy, Iz) meta(world, shape, group, mask)
+//   bodies   a contiguous range of the body arrays: poses as (pos(xyz, bounding radius), rot)
+//            pairs for the current, step-start (x-) and inertial poses, then one float4 per field:
+//            vel ang vprev size(xyz, friction) mass(m, Ix, Iy, Iz) meta(world, shape, group, mask)
 //   joints   a contiguous range of the joint arrays: body pair, rA(xyz, kind) rB(xyz, rest)
 //            stiff(lin, ang, fracture, torqueArm) penLin penAng lamLin lamAng C0Lin C0Ang restQ, broken
 //   pairs    a region of pair slots, present in two buffers (slot + k * slotStride, k = 0, 1): the
@@ -56,9 +56,18 @@ struct WorldDev {
   int pairCap, bvhNodeOff, bvhRoot, pad0;  // bvhRoot: local node id (-1: empty tree)
 };
 
+// Poses are stored as interleaved pairs (pos, rot) of 32 bytes: a gather of a body's pose, or of
+// its pose and step-start pose, touches one (two) 32-byte sectors instead of two (four).
 struct BodyPtrs {
-  float4 *pos, *rot, *pos0, *rot0, *posY, *rotY, *vel, *ang, *vprev, *size, *mass;
+  float4 *pose, *pose0, *poseY;  // (pos, rot) at [2i], [2i + 1]: current, step start (x-), inertial
+  float4 *vel, *ang, *vprev, *size, *mass;
   int4* meta;
+  __host__ __device__ __forceinline__ float4& pos(int i) const { return pose[2 * size_t(i)]; }
+  __host__ __device__ __forceinline__ float4& rot(int i) const { return pose[2 * size_t(i) + 1]; }
+  __host__ __device__ __forceinline__ float4& pos0(int i) const { return pose0[2 * size_t(i)]; }
+  __host__ __device__ __forceinline__ float4& rot0(int i) const { return pose0[2 * size_t(i) + 1]; }
+  __host__ __device__ __forceinline__ float4& posY(int i) const { return poseY[2 * size_t(i)]; }
+  __host__ __device__ __forceinline__ float4& rotY(int i) const { return poseY[2 * size_t(i) + 1]; }
 };
 
 struct JointPtrs {

@@ -46,9 +46,9 @@ __global__ void k_gather_poses(BodyPtrs bd, const int4* __restrict__ seg, int ns
     const int k = i - e.z;
     if (k >= e.y) continue;  // output rows of evicted worlds (filled on the host)
     const int body = e.x + k;
-    const float4 p = bd.pos[body];
+    const float4 p = bd.pos(body);
     out[2 * size_t(i)] = make_float4(p.x, p.y, p.z, bd.size[body].w);
-    out[2 * size_t(i) + 1] = bd.rot[body];
+    out[2 * size_t(i) + 1] = bd.rot(body);
   }
 }
 
@@ -334,7 +334,7 @@ int avbd_server_read_poses(avbd_server* s, const int64_t* world_ids, int32_t n, 
     const Snapshot& S = *R.snap;
     for (int i = 0; i < R.nBodies; i++) {
       float* o = out + (h.second + size_t(i)) * 8;
-      const float4 p = S.body[0][i], q = S.body[1][i], sz = S.body[9][i];
+      const float4 p = S.pose[2 * size_t(i)], q = S.pose[2 * size_t(i) + 1], sz = S.size[i];
       o[0] = p.x; o[1] = p.y; o[2] = p.z; o[3] = sz.w;
       o[4] = q.x; o[5] = q.y; o[6] = q.z; o[7] = q.w;
     }
@@ -358,13 +358,17 @@ int avbd_server_read_state(avbd_server* s, int64_t world_id, float* position, fl
     if (!o) return;
     for (int i = 0; i < R.nBodies; i++) { o[3 * i] = v[i].x; o[3 * i + 1] = v[i].y; o[3 * i + 2] = v[i].z; }
   };
-  put3(position, S.body[0]);
-  put3(velocity, S.body[6]);
-  put3(angular, S.body[7]);
-  put3(prev_velocity, S.body[8]);
+  put3(velocity, S.vel);
+  put3(angular, S.ang);
+  put3(prev_velocity, S.vprev);
+  if (position)
+    for (int i = 0; i < R.nBodies; i++) {
+      const float4 p = S.pose[2 * size_t(i)];
+      position[3 * i] = p.x; position[3 * i + 1] = p.y; position[3 * i + 2] = p.z;
+    }
   if (rotation)
     for (int i = 0; i < R.nBodies; i++) {
-      const float4 q = S.body[1][i];
+      const float4 q = S.pose[2 * size_t(i) + 1];
       rotation[4 * i] = q.x; rotation[4 * i + 1] = q.y; rotation[4 * i + 2] = q.z; rotation[4 * i + 3] = q.w;
     }
   API_END
