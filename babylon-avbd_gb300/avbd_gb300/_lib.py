@@ -105,6 +105,10 @@ SIGNATURES = [
     ("avbd_server_evict", C.c_int, [C.c_void_p, C.c_int64]),
     ("avbd_server_release", C.c_int, [C.c_void_p, C.c_int64]),
     ("avbd_server_read_stats", C.c_int, [C.c_void_p, C.POINTER(ServerStats)]),
+    ("avbd_world_edit", C.c_int, [C.c_void_p, _up, C.c_int32]),
+    ("avbd_world_flush_edits", C.c_int, [C.c_void_p]),
+    ("avbd_batch_edit", C.c_int, [C.c_void_p, C.c_int32, _up, C.c_int32]),
+    ("avbd_server_edit", C.c_int, [C.c_void_p, C.c_int64, _up, C.c_int32]),
 ]
 
 # include/avbd_gb300.h

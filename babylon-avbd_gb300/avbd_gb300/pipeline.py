@@ -130,6 +130,68 @@ def createSolverPipeline(backend: str = "gb300", device: int = 0) -> SolverPipel
     return SolverPipeline(device)
 
 
+# Body command kinds in the order of the reference's command shaders (src/native/runtime.js:36-44);
+# kind 4 is the teleport.
+_EDIT_KEYS = ["linearVelocity", "angularVelocity", "impulse", "force", "", "angularImpulse", "torque"]
+
+
+def _components(value, count, name):
+    try:
+        a = [float(x) for x in (value.tolist() if isinstance(value, np.ndarray) else value)]
+    except TypeError:
+        raise ValueError(f"{name} requires {count} finite components") from None
+    if len(a) != count or not all(math.isfinite(x) for x in a):
+        raise ValueError(f"{name} requires {count} finite components")
+    return a
+
+
+def stage_edits(edits, body_count: int, dt: float) -> np.ndarray:
+    """``editBodies(edits)`` records (``src/native/runtime.js:62-167``): the whole batch is
+    validated before anything is queued; per edit the teleport comes first, then velocity
+    replacements, impulses and forces in kind order. Returns (n, 12) uint32 words."""
+    words = []
+    unsupported = {"isTrigger", "restitution", "allowSleep", "group", "collidesWith"}
+
+    def record(index, kind, value, point):
+        w = np.zeros(12, dtype=np.uint32)
+        f = w.view(np.float32)
+        w[0], w[1], w[2] = index, kind, int(point is not None)
+        f[4:4 + len(value)] = value
+        if point is not None:
+            f[8:8 + len(point)] = point
+        if kind in (3, 6):
+            f[7] = dt
+        return w
+
+    for edit in edits:
+        index = edit.get("body")
+        if not isinstance(index, (int, np.integer)) or not 0 <= int(index) < body_count:
+            raise ValueError("A live body index is required")
+        index = int(index)
+        bad = unsupported & set(edit)
+        if bad:
+            raise ValueError(f"body property edits {sorted(bad)} are not part of this engine")
+        point = None if edit.get("worldPoint") is None else _components(edit["worldPoint"], 3, "worldPoint")
+        if edit.get("position") is not None:
+            p = _components(edit["position"], 3, "position")
+            q = None
+            if edit.get("rotation") is not None:
+                q = _components(edit["rotation"], 4, "rotation")
+                ln = math.hypot(*q)
+                if not ln:
+                    raise ValueError("rotation must be nonzero")
+                q = [v / ln for v in q]
+            words.append(record(index, 4, p, q))
+        elif edit.get("rotation") is not None:
+            raise ValueError("A rotation edit requires position; use teleport for a full pose")
+        for kind, key in enumerate(_EDIT_KEYS):
+            if kind == 4 or edit.get(key) is None:
+                continue
+            v = _components(edit[key], 3, key)
+            words.append(record(index, kind, v, point if kind in (2, 3) else None))
+    return np.stack(words) if words else np.zeros((0, 12), dtype=np.uint32)
+
+
 def _indices(indices, n):
     idx = np.ascontiguousarray(np.asarray(indices, dtype=np.int64).reshape(-1))
     if idx.size and (idx.min() < 0 or idx.max() >= n):
@@ -202,6 +264,49 @@ class World:
 
     def readBodies(self) -> np.ndarray:
         return self.readSelectedBodies(np.arange(self.bodyCount))
+
+    # ---- body commands (src/native/runtime.js:46-167, src/native/cpu/world.js:145-166)
+    def editBodies(self, edits):
+        """Queue a validated batch of body edits for the next step."""
+        self._live()
+        rec = stage_edits(edits, self.bodyCount, self.dt)
+        if len(rec):
+            L.check(L.lib().avbd_world_edit(self._h, L.uptr(rec), int(rec.shape[0])))
+        return self
+
+    def editRecords(self, records):
+        """Queue already-staged command records (n x 12 uint32 words, see ``stage_edits``)."""
+        self._live()
+        rec = np.ascontiguousarray(records, dtype=np.uint32).reshape(-1, 12)
+        if len(rec):
+            L.check(L.lib().avbd_world_edit(self._h, L.uptr(rec), int(rec.shape[0])))
+        return self
+
+    def flushEdits(self):
+        self._live()
+        L.check(L.lib().avbd_world_flush_edits(self._h))
+        return self
+
+    def setLinearVelocity(self, index, value):
+        return self.editBodies([{"body": index, "linearVelocity": value}])
+
+    def setAngularVelocity(self, index, value):
+        return self.editBodies([{"body": index, "angularVelocity": value}])
+
+    def applyImpulse(self, index, value, worldPoint=None):
+        return self.editBodies([{"body": index, "impulse": value, "worldPoint": worldPoint}])
+
+    def applyForce(self, index, value, worldPoint=None):
+        return self.editBodies([{"body": index, "force": value, "worldPoint": worldPoint}])
+
+    def applyAngularImpulse(self, index, value):
+        return self.editBodies([{"body": index, "angularImpulse": value}])
+
+    def applyTorque(self, index, value):
+        return self.editBodies([{"body": index, "torque": value}])
+
+    def teleport(self, index, position, rotation=None):
+        return self.editBodies([{"body": index, "position": position, "rotation": rotation}])
 
     def readCounters(self) -> dict:
         self._live()
@@ -316,6 +421,7 @@ class Batch:
         self._h = h
         self.worldCount = len(arrays_list)
         self.bodyCounts = [a.n_bodies for a in arrays_list]
+        self._dts = [float(a.params.dt) for a in arrays_list]
         self.bodyCount = int(sum(self.bodyCounts))
 
     def step(self, steps: int = 1):
@@ -358,6 +464,15 @@ class Batch:
                 raise ValueError("velocities must be finite")
         L.check(L.lib().avbd_batch_set_velocities(self._h, L.uptr(idx), idx.size, L.fptr(v), L.fptr(a)))
 
+    def editBodies(self, world: int, edits):
+        """Body edits (world-local indices) of world ``world``, applied at the next step."""
+        if not 0 <= world < self.worldCount:
+            raise ValueError("world index out of range")
+        rec = stage_edits(edits, self.bodyCounts[world], self._dts[world])
+        if len(rec):
+            L.check(L.lib().avbd_batch_edit(self._h, int(world), L.uptr(rec), int(rec.shape[0])))
+        return self
+
     def profile(self, enable: bool = True):
         L.check(L.lib().avbd_batch_profile(self._h, int(bool(enable))))
 
@@ -392,7 +507,7 @@ class Server:
         L.check(L.lib().avbd_server_create(pipe._h, C.byref(desc), C.byref(h)))
         self._h = h
         self._counts = {}
-        self._packed = None
+        self._dts = {}
 
     def _live(self):
         if self._h is None:
@@ -405,7 +520,18 @@ class Server:
         wid = C.c_int64()
         L.check(L.lib().avbd_server_admit(self._h, C.byref(packed.desc), C.byref(packed.params), C.byref(wid)))
         self._counts[wid.value] = packed.n_bodies
+        self._dts[wid.value] = float(packed.params.dt)
         return wid.value
+
+    def editBodies(self, world: int, edits):
+        """Body edits of a served world, applied before its next step."""
+        self._live()
+        if int(world) not in self._counts:
+            raise ValueError(f"no such world {world}")
+        rec = stage_edits(edits, self._counts[int(world)], self._dts[int(world)])
+        if len(rec):
+            L.check(L.lib().avbd_server_edit(self._h, int(world), L.uptr(rec), int(rec.shape[0])))
+        return self
 
     def advance(self, world: int, steps: int = 1) -> int:
         self._live()

@@ -158,6 +158,7 @@ struct WorldRec {
   BvhLayout tree;
   int bvhOff = 0, bvhRebuild = 16, sinceBuild = 0;
   bool built = false;
+  std::vector<uint32_t> edits;  // body command records waiting for the next step (12 words each)
 };
 
 class Arena {
@@ -336,7 +337,7 @@ class Arena {
                     T.pending, T.colorBodies, T.itemStart, T.itemRef, ctr, NC.keys, NC.jid, scanTemp, traffic,
                     poseStage, P.pair, P.count, P.basis, P.ct, NS.sat, NS.boxList, NS.sphereList, NS.ctr, activePairs,
                     T.adjList, G.bvh.node, G.bvh.parent, G.bvh.escape, G.bvh.minIdx, bsc.keys[0], bsc.keys[1], bsc.hist,
-                    bsc.clusters, bsc.bounds};
+                    bsc.clusters, bsc.bounds, editRec, editRanges, editTele};
     for (void* p : ptrs) dfree(p);
     if (ctrHost) cudaFreeHost(ctrHost);
     if (activeHost) cudaFreeHost(activeHost);
@@ -1068,6 +1069,71 @@ class Arena {
     regrowths++;
   }
 
+  // ------------------------------------------------------------------ body commands
+  uint32_t* editRec = nullptr;
+  int2* editRanges = nullptr;
+  uint32_t* editTele = nullptr;
+  size_t editCap = 0;
+
+  // Validate n 12-word records (src/native/runtime.js:59-167 stages the same checks) and queue
+  // them for world w's next step.
+  void queueEdits(int w, const uint32_t* rec, int n) {
+    if (w < 0 || w >= maxWorlds || !W[w].live) throw Error(AVBD_E_INVALID, "no such world");
+    if (n < 0) throw Error(AVBD_E_INVALID, "negative record count");
+    const WorldRec& R = W[w];
+    for (int k = 0; k < n; k++) {
+      const uint32_t* u = rec + 12 * size_t(k);
+      if (u[0] >= uint32_t(R.nBodies)) throw Error(AVBD_E_INVALID, "body index out of range");
+      if (u[1] > 6u) throw Error(AVBD_E_INVALID, "unknown body command kind");
+      float f[8];
+      std::memcpy(f, u + 4, sizeof(f));
+      for (int i = 0; i < 8; i++)
+        if (!std::isfinite(f[i])) throw Error(AVBD_E_INVALID, "body command values must be finite");
+      if (u[1] == 4u && u[2] != 0u && f[4] == 0.f && f[5] == 0.f && f[6] == 0.f && f[7] == 0.f)
+        throw Error(AVBD_E_INVALID, "rotation must be nonzero");
+    }
+    W[w].edits.insert(W[w].edits.end(), rec, rec + 12 * size_t(n));
+  }
+
+  // Apply world w's queued records (the reference applies them at its next step, or at
+  // flushEdits): grouped by body in record order, one thread per body; teleported bodies lose
+  // the warm start of their pairs.
+  void flushEdits(int w) {
+    WorldRec& R = W[w];
+    if (R.edits.empty()) return;
+    if (!R.resident) throw Error(AVBD_E_STATE, "world is evicted");
+    const int n = int(R.edits.size() / 12);
+    std::vector<int> order(n);
+    for (int k = 0; k < n; k++) order[k] = k;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return R.edits[12 * size_t(a)] < R.edits[12 * size_t(b)]; });
+    std::vector<uint32_t> sorted(R.edits.size());
+    std::vector<int2> ranges;
+    std::vector<uint32_t> tele;
+    for (int k = 0; k < n; k++) {
+      const uint32_t* u = R.edits.data() + 12 * size_t(order[k]);
+      std::memcpy(sorted.data() + 12 * size_t(k), u, 48);
+      if (ranges.empty() || sorted[12 * size_t(ranges.back().x)] != u[0]) ranges.push_back(make_int2(k, 0));
+      ranges.back().y++;
+      if (u[1] == 4u && (tele.empty() || tele.back() != u[0])) tele.push_back(u[0]);
+    }
+    if (size_t(n) > editCap) {
+      editCap = size_t(n) + size_t(n) / 2 + 64;
+      rescratch(editRec, 12 * editCap);
+      rescratch(editRanges, editCap);
+      rescratch(editTele, editCap);
+    }
+    put(editRec, sorted.data(), sorted.size() * 4);
+    put(editRanges, ranges.data(), ranges.size() * sizeof(int2));
+    launch_apply_edits(B, editRec, editRanges, int(ranges.size()), R.dev.bodyOff, s);
+    if (!tele.empty()) {
+      put(editTele, tele.data(), tele.size() * 4);
+      const int np = prevPairs(w);
+      launch_drop_contacts(P, size_t(R.which) * slotCap + R.dev.pairOff, np, editTele, int(tele.size()), R.dev.bodyOff, s);
+    }
+    flush();
+    R.edits.clear();
+  }
+
   // ------------------------------------------------------------------ profiling
   cudaEvent_t event() {
     if (!pool.empty()) {
@@ -1140,6 +1206,7 @@ class Arena {
     act.erase(std::unique(act.begin(), act.end()), act.end());
     for (int w : act)
       if (w < 0 || w >= maxWorlds || !W[w].live || !W[w].resident) throw Error(AVBD_E_INVALID, "stepping a world that is not resident");
+    for (int w : act) flushEdits(w);  // queued body commands apply before the step
     for (int w : lastActive) wactiveHost[w] = -1;
     lastActive.clear();
     int nb = 0, nj = 0, maxIter = 0;

@@ -364,6 +364,21 @@ int avbd_world_counters(avbd_world* w, avbd_counters* out) {
   API_END
 }
 
+int avbd_world_edit(avbd_world* w, const uint32_t* records, int32_t n) {
+  API_BEGIN
+  REQUIRE(w && (n == 0 || records), "null argument");
+  w->A->queueEdits(w->w, records, n);
+  API_END
+}
+
+int avbd_world_flush_edits(avbd_world* w) {
+  API_BEGIN
+  REQUIRE(w, "null world");
+  bind(w->A->ctx);
+  w->A->flushEdits(w->w);
+  API_END
+}
+
 int avbd_world_pairs(avbd_world* w, uint32_t* out, int64_t cap, int64_t* n) {
   API_BEGIN
   REQUIRE(w && n, "null argument");
@@ -559,6 +574,14 @@ int avbd_batch_set_velocities(avbd_batch* b, const uint32_t* indices, int32_t n,
   REQUIRE(b, "null batch");
   bind(b->A->ctx);
   setVelocities(*b->A, 0, int(b->bodies), indices, n, velocity, angular);
+  API_END
+}
+
+int avbd_batch_edit(avbd_batch* b, int32_t world, const uint32_t* records, int32_t n) {
+  API_BEGIN
+  REQUIRE(b && (n == 0 || records), "null argument");
+  REQUIRE(world >= 0 && world < int32_t(b->worlds.size()), "world index out of range");
+  b->A->queueEdits(b->worlds[world], records, n);
   API_END
 }
 

@@ -250,6 +250,10 @@ void launch_primal(const BodyPtrs& b, const WorldDev* worlds, JointPtrs j, PairP
 // Joint duals of one iteration (contact duals run inside launch_primal, see k_primal).
 void launch_dual_joints(const BodyPtrs& b, const WorldDev* worlds, JointPtrs j, Tick t, int iteration, cudaStream_t s);
 void launch_velocities(const BodyPtrs& b, const WorldDev* worlds, Tick t, cudaStream_t s);
+// Body command records of one world (sorted by body, ranges per body; see k_apply_edits), and
+// the warm-start drop of teleported bodies (sorted local indices) in its last pair region.
+void launch_apply_edits(const BodyPtrs& b, const uint32_t* rec, const int2* ranges, int nranges, int bodyOff, cudaStream_t s);
+void launch_drop_contacts(PairPtrs P, size_t base, int np, const uint32_t* tele, int ntele, int bodyOff, cudaStream_t s);
 void launch_tick_end(Tick t, cudaStream_t s);
 void launch_count_active(JointPtrs j, PairPtrs P, const int* slots, int nSlots, const int* joints, int nJoints, Counters* out,
                          cudaStream_t s);

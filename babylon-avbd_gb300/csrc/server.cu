@@ -386,6 +386,14 @@ int avbd_server_world_info(avbd_server* s, int64_t world_id, int32_t* n_bodies, 
   API_END
 }
 
+int avbd_server_edit(avbd_server* s, int64_t world_id, const uint32_t* records, int32_t n) {
+  API_BEGIN
+  REQUIRE(s && (n == 0 || records), "null argument");
+  const Served& w = s->get(world_id);
+  s->A->queueEdits(w.slot, records, n);
+  API_END
+}
+
 int avbd_server_evict(avbd_server* s, int64_t world_id) {
   API_BEGIN
   REQUIRE(s, "null server");

@@ -174,6 +174,17 @@ int avbd_world_set_velocities(avbd_world* w, const uint32_t* indices, int32_t n,
 /* world.readCounters() (src/vendor/three-avbd-lib/solver3D.ts:1460-1463). */
 int avbd_world_counters(avbd_world* w, avbd_counters* out);
 
+/* Body commands: world.editBodies(edits) / flushEdits() (src/native/runtime.js:46-167,
+ * src/native/cpu/world.js:229-300). n records of 12 32-bit words, the layout of the reference's
+ * command staging (src/gpu/bodyCommands2D.js:46-55): word 0 body index, 1 kind, 2 has-point,
+ * 3 zero, 4-7 value (float), 8-11 point (float). Kinds: 0 set linear velocity, 1 set angular
+ * velocity, 2 impulse (at point when has-point), 3 force (value.w = dt), 4 teleport (value.xyz =
+ * position, point = unit quaternion when has-point; the body's contacts lose their warm start),
+ * 5 angular impulse, 6 torque (value.w = dt). Records are validated, queued, and applied in order
+ * at the next step (or at avbd_world_flush_edits). */
+int avbd_world_edit(avbd_world* w, const uint32_t* records, int32_t n);
+int avbd_world_flush_edits(avbd_world* w);
+
 /* Parity dumps (readPairs / readContactList, solver3D.ts:1466-1506). Each writes at most `cap`
  * records and stores the full count in *n. */
 /* Candidate pairs of the last step, sorted ascending by (hi, lo): 2 uint32 per pair. */
@@ -212,6 +223,8 @@ int avbd_batch_counters(avbd_batch* b, avbd_counters* out);
 int avbd_batch_read_poses(avbd_batch* b, float* out);
 /* setVelocities for bodies given by batch-global index (world offset + body index). */
 int avbd_batch_set_velocities(avbd_batch* b, const uint32_t* indices, int32_t n, const float* velocity, const float* angular);
+/* Body commands (as avbd_world_edit) for world `world` of the batch (world-local body indices). */
+int avbd_batch_edit(avbd_batch* b, int32_t world, const uint32_t* records, int32_t n);
 
 /* Profiling (see avbd_profile): enable resets the accumulators; read returns them. */
 int avbd_world_profile(avbd_world* w, int32_t enable);
@@ -265,6 +278,8 @@ int avbd_server_read_state(avbd_server* s, int64_t world_id, float* position, fl
 /* World facts: bodies, queued steps, steps done, resident (1) or evicted (0). */
 int avbd_server_world_info(avbd_server* s, int64_t world_id, int32_t* n_bodies, int64_t* queued, int64_t* steps_done,
                            int32_t* resident);
+/* Body commands (as avbd_world_edit), applied before the world's next step. */
+int avbd_server_edit(avbd_server* s, int64_t world_id, const uint32_t* records, int32_t n);
 /* Evict a world now (its queued steps wait for a restore). */
 int avbd_server_evict(avbd_server* s, int64_t world_id);
 /* Drop a world; its outstanding tickets never complete. */

@@ -992,6 +992,65 @@ template <class R> class Solver {
     stepSolve();
   }
   int forceCount() const { return int(forces.size()); }
+
+  // Body commands in the 12-word records of src/gpu/bodyCommands2D.js:46-55 (index, kind,
+  // hasPoint, 0, value[4], point[4]) with the semantics of src/native/cpu/world.js:229-300
+  // (flushEdits): 0 set linear velocity, 1 set angular velocity, 2 impulse (at point), 3 force
+  // (value.w = dt), 4 teleport (position, rotation = point; step-start and inertial poses follow;
+  // the body's manifolds are dropped), 5 angular impulse, 6 torque (value.w = dt).
+  void applyEdits(const uint32_t* rec, int n) {
+    for (int k = 0; k < n; k++) {
+      const uint32_t* u = rec + 12 * size_t(k);
+      float f[12];
+      std::memcpy(f, u, sizeof(f));
+      const int id = int(u[0]), kind = int(u[1]);
+      const bool point = u[2] != 0;
+      Body<R>& b = bodies[id];
+      auto angular = [&](const R* v) {
+        if (b.mass <= 0) return;
+        R c[4] = {-b.q[0], -b.q[1], -b.q[2], b.q[3]}, local[3], delta[3];
+        Mt::rotate(local, c, v);
+        for (int i = 0; i < 3; i++) local[i] = local[i] / std::max(R(1e-10), b.moment[i]);
+        Mt::rotate(delta, b.q, local);
+        for (int i = 0; i < 3; i++) b.w[i] += delta[i];
+      };
+      if (kind == 0) {
+        for (int i = 0; i < 3; i++) b.v[i] = R(f[4 + i]);
+      } else if (kind == 1) {
+        for (int i = 0; i < 3; i++) b.w[i] = R(f[4 + i]);
+      } else if (kind == 4) {
+        for (int i = 0; i < 3; i++) b.pos[i] = R(f[4 + i]);
+        if (point)
+          for (int i = 0; i < 4; i++) b.q[i] = R(f[8 + i]);
+        std::memcpy(b.x0, b.pos, sizeof(b.x0));
+        std::memcpy(b.y, b.pos, sizeof(b.y));
+        std::memcpy(b.q0, b.q, sizeof(b.q0));
+        std::memcpy(b.qy, b.q, sizeof(b.qy));
+        std::vector<int> kept;
+        for (int fid : forces) {
+          Force<R>& fo = *store[fid];
+          if (fo.type == F_MANIFOLD && (fo.a == id || fo.b == id)) unlinkFromBodies(fid);
+          else kept.push_back(fid);
+        }
+        forces.swap(kept);
+      } else if (kind == 2 || kind == 3) {
+        if (b.mass <= 0) continue;
+        R imp[3];
+        for (int i = 0; i < 3; i++) imp[i] = kind == 3 ? R(f[4 + i]) * R(f[7]) : R(f[4 + i]);
+        for (int i = 0; i < 3; i++) b.v[i] += imp[i] / b.mass;
+        if (point) {
+          R r[3], t[3];
+          for (int i = 0; i < 3; i++) r[i] = R(f[8 + i]) - b.pos[i];
+          Mt::cross(t, r, imp);
+          angular(t);
+        }
+      } else if (kind == 5 || kind == 6) {
+        R t[3];
+        for (int i = 0; i < 3; i++) t[i] = kind == 6 ? R(f[4 + i]) * R(f[7]) : R(f[4 + i]);
+        angular(t);
+      }
+    }
+  }
 };
 
 // ---------------------------------------------------------------- collide.ts (box-box)

@@ -74,6 +74,7 @@ def lib():
         L.oracle_world_candidate_pairs.argtypes = [C.c_void_p, _ip, C.c_int]
         L.oracle_world_collide.argtypes = [C.c_void_p, C.c_int, C.c_int, _dp, _up, _dp, _dp]
         L.oracle_world_import.argtypes = [C.c_void_p, C.POINTER(_State)]
+        L.oracle_world_edit.argtypes = [C.c_void_p, C.POINTER(C.c_uint32), C.c_int]
         L.oracle_worlds_step_parallel.argtypes = [C.POINTER(C.c_void_p), C.c_int, C.c_int, C.c_int]
         L.oracle_worlds_step_parallel.restype = C.c_int
         _lib = L
@@ -220,6 +221,12 @@ class OracleWorld:
                    i32(st["mcount"]), u32(st["cfeature"]), d(st["cra"]), d(st["crb"]),
                    d(st["cpen"]), d(st["clam"]), i32(st["cstick"]), i32(st.get("colors")))
         lib().oracle_world_import(self.h, C.byref(s))
+
+    def edit(self, records):
+        """Apply body command records (n x 12 uint32 words, ``src/gpu/bodyCommands2D.js``
+        layout) with the CPU world's flushEdits semantics (``src/native/cpu/world.js:229-300``)."""
+        r = np.ascontiguousarray(records, dtype=np.uint32).reshape(-1, 12)
+        lib().oracle_world_edit(self.h, r.ctypes.data_as(C.POINTER(C.c_uint32)), int(r.shape[0]))
 
 
 def step_parallel(worlds, steps, threads=0) -> int:

@@ -330,6 +330,9 @@ template <class R> static void import_state(Solver<R>& S, const oracle_state* st
 
 extern "C" void oracle_world_import(void* h, const oracle_state* st) { DISPATCH(h, import_state(S, st)); }
 
+// src/native/cpu/world.js:229-300 flushEdits over n 12-word body command records
+extern "C" void oracle_world_edit(void* h, const uint32_t* records, int n) { DISPATCH(h, S.applyEdits(records, n)); }
+
 // Step many independent worlds in parallel with OpenMP (the multi-world CPU baseline).
 // Returns the thread count used.
 extern "C" int oracle_worlds_step_parallel(void** hs, int n, int steps, int threads) {

@@ -28,8 +28,10 @@ def _err(gpu, cpu):
     return float(np.max(np.abs(g - c) / (np.abs(c) + 1.0)))
 
 
-def compare_step(world, scene, warm: int):
-    """Run the comparison on an engine world built from `scene`; returns a report dict."""
+def compare_step(world, scene, warm: int, edits=None):
+    """Run the comparison on an engine world built from `scene`; returns a report dict.
+    `edits` (body command records, n x 12 words) are queued on the engine world and applied to
+    the oracles before the compared step."""
     if warm:
         world.step(warm)
     st = world.exportState()
@@ -38,7 +40,11 @@ def compare_step(world, scene, warm: int):
     for name, fp64 in (("fp32", False), ("fp64", True)):
         o = O.OracleWorld(scene, fp64=fp64, app=True, colored=True)
         o.import_state(st)
+        if edits is not None and len(edits):
+            o.edit(edits)
         oracles[name] = o
+    if edits is not None and len(edits):
+        world.editRecords(edits)
     o32 = oracles["fp32"]
     cand = o32.candidate_pairs()
     world.step(1)

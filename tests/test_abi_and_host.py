@@ -153,3 +153,23 @@ def test_oracle_fp32_narrowphase_box_box_kat():
         else:
             misses += 1
     assert hits > 20 and misses > 20
+
+
+def test_stage_edits_layout_and_validation():
+    import numpy as np
+    import pytest as _pt
+    from avbd_gb300.pipeline import stage_edits
+    rec = stage_edits([{"body": 2, "position": [1, 2, 3], "rotation": [0, 0, 0, 2], "linearVelocity": [4, 5, 6],
+                        "force": [1, 0, 0], "worldPoint": [0, 1, 0], "torque": [0, 0, 3]}], 5, 0.5)
+    assert rec.shape == (4, 12)
+    f = rec.view(np.float32)
+    assert list(rec[:, 1]) == [4, 0, 3, 6]  # teleport first, then kinds in order
+    assert list(rec[:, 0]) == [2, 2, 2, 2]
+    assert rec[0, 2] == 1 and list(f[0, 4:7]) == [1, 2, 3] and list(f[0, 8:12]) == [0, 0, 0, 1]
+    assert rec[1, 2] == 0 and rec[2, 2] == 1 and f[2, 7] == 0.5 and f[3, 7] == 0.5
+    assert list(f[2, 8:11]) == [0, 1, 0]
+    for bad in ({"body": 5, "linearVelocity": [0, 0, 0]}, {"body": 0, "rotation": [0, 0, 0, 1]},
+                {"body": 0, "impulse": [0, float("nan"), 0]}, {"body": 0, "position": [0, 0, 0], "rotation": [0, 0, 0, 0]},
+                {"body": 0, "restitution": 0.5}):
+        with _pt.raises(ValueError):
+            stage_edits([bad], 5, 0.5)
