@@ -335,9 +335,9 @@ class Arena {
                     which, pairN, wover, wactive, active, activeBodies, activeJoints, pairPrefix, pairCount, G.cellCount,
                     G.cellFill, G.cellBodies, G.cellKey, G.cellPos, G.pairTmp, G.bodyBucket, G.large, T.adjStart, T.adjFill, T.activeIndex, T.color, T.won,
                     T.pending, T.colorBodies, T.itemStart, T.itemRef, ctr, NC.keys, NC.jid, scanTemp, traffic,
-                    poseStage, P.pair, P.count, P.basis, P.ct, NS.sat, NS.boxList, NS.sphereList, NS.ctr, activePairs,
+                    poseStage, P.pair, P.count, P.basis, P.ct, NS.sat, NS.boxList, NS.sphereList, NS.sphere2List, NS.ctr, activePairs,
                     T.adjList, G.bvh.node, G.bvh.parent, G.bvh.escape, G.bvh.minIdx, bsc.keys[0], bsc.keys[1], bsc.hist,
-                    bsc.clusters, bsc.bounds, editRec, editRanges, editTele};
+                    bsc.clusters, bsc.bounds, editRec, editRanges, editTele, io};
     for (void* p : ptrs) dfree(p);
     if (ctrHost) cudaFreeHost(ctrHost);
     if (activeHost) cudaFreeHost(activeHost);
@@ -363,13 +363,14 @@ class Arena {
       CK(cudaStreamSynchronize(s));
     }
     for (void* p : {(void*)P.pair, (void*)P.count, (void*)P.basis, (void*)P.ct, (void*)NS.sat, (void*)NS.boxList,
-                    (void*)NS.sphereList, (void*)NS.ctr, (void*)activePairs, (void*)T.adjList})
+                    (void*)NS.sphereList, (void*)NS.sphere2List, (void*)NS.ctr, (void*)activePairs, (void*)T.adjList})
       dfree(p);
     P = np;
     NS.sat = dalloc<float4>(cap);
     NS.boxList = dalloc<int>(cap);
     NS.sphereList = dalloc<int>(cap);
-    NS.ctr = dalloc<int>(2);
+    NS.sphere2List = dalloc<int>(cap);
+    NS.ctr = dalloc<int>(3);
     activePairs = dalloc<int>(cap);
     T.adjList = dalloc<uint32_t>(2 * (size_t(jointCap) + size_t(cap)) + 1);
     if (slotCap == 0) slotA.init(cap);
@@ -503,7 +504,7 @@ class Arena {
   size_t footprint(long long nb, long long nj, long long slots, long long nw) const {
     const size_t perBody = 12 * 16 + 2 * 4 + 1 + 11 * 4 + 32 + 4 * PAIR_TMP;
     const size_t perJoint = 8 + 10 * 16 + 4 + 4 + 8;
-    const size_t perSlot = 2 * (8 + 4 + 3 * 16 + MAX_CONTACTS * 64) + 16 + 3 * 4 + 8;
+    const size_t perSlot = 2 * (8 + 4 + 3 * 16 + MAX_CONTACTS * 64) + 16 + 4 * 4 + 8;
     const size_t perWorld = sizeof(WorldDev) + 4 * 4 + 16 + 4 + MAX_LARGE * 4;
     return size_t(nb) * perBody + size_t(tableFor(size_t(nb))) * 8 + size_t(nj) * perJoint + size_t(slots) * perSlot +
            size_t(nw) * perWorld + size_t(ncCap) * 12 + scanBytes + size_t(bvhCap) * (32 + 12) +
@@ -1068,6 +1069,22 @@ class Arena {
     flush();
     regrowths++;
   }
+
+  // ------------------------------------------------------------------ call scratch
+  // One grow-only device buffer for the arguments and results of the read/write entry points
+  // (indices, velocities, poses), so they allocate nothing once warm; uploads go through the
+  // pinned stager on the arena's stream, so a write returns without waiting for the device.
+  char* io = nullptr;
+  size_t ioCap = 0;
+  char* ioBuffer(size_t bytes) {
+    if (bytes > ioCap) {
+      CK(cudaStreamSynchronize(s));  // earlier calls may still read the old buffer
+      ioCap = bytes + bytes / 2 + 4096;
+      rescratch(io, ioCap);
+    }
+    return io;
+  }
+  static size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
   // ------------------------------------------------------------------ body commands
   uint32_t* editRec = nullptr;

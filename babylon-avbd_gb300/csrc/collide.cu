@@ -731,10 +731,12 @@ __device__ __forceinline__ V3 closest_surface(const BoxGeo& g, V3 p) {
   return best;
 }
 
-// At least one body is a sphere. Returns the contact count (0 or 1).
+// At least one body is a sphere (BOTH_ROUND: both are, and the box code compiles away). Returns
+// the contact count (0 or 1).
+template <bool BOTH_ROUND>
 __device__ int collide(float4 pA, float4 qA, float4 sA, int shA, float4 pB, float4 qB, float4 sB, int shB, M33& basis,
                        V3& rA, V3& rB) {
-  const bool roundA = shA == SHAPE_SPHERE, roundB = shB == SHAPE_SPHERE;
+  const bool roundA = BOTH_ROUND || shA == SHAPE_SPHERE, roundB = BOTH_ROUND || shB == SHAPE_SPHERE;
   BoxGeo box;
   const V3 cA = v3(pA), cB = v3(pB);
   // a sphere's spine is its centre (rotate of a zero offset adds +-0)
@@ -929,13 +931,14 @@ __global__ void __launch_bounds__(256) k_np_classify(BodyPtrs bd, const WorldDev
   for (int base = blockIdx.x * blockDim.x; base < np; base += gridDim.x * blockDim.x) {
     const int q = base + threadIdx.x;
     const int p = q < np ? t.pairs[q] : 0;
-    bool boxHit = false, sphere = false;
+    bool boxHit = false, sphere = false, bothRound = false;
     if (q < np) {
       const uint2 key = cur.pair[p];
       const int a = int(key.x), b = int(key.y);
       const int shA = bd.meta[a].y, shB = bd.meta[b].y;
       if (shA == SHAPE_SPHERE || shB == SHAPE_SPHERE) {
         sphere = true;
+        bothRound = shA == SHAPE_SPHERE && shB == SHAPE_SPHERE;
       } else {
         const WorldDev& W = worlds[bd.meta[a].x];
         box::Sat best;
@@ -948,7 +951,8 @@ __global__ void __launch_bounds__(256) k_np_classify(BodyPtrs bd, const WorldDev
       }
     }
     append(ns.boxList, &ns.ctr[0], q, boxHit);
-    append(ns.sphereList, &ns.ctr[1], p, sphere);
+    append(ns.sphereList, &ns.ctr[1], p, sphere && !bothRound);
+    append(ns.sphere2List, &ns.ctr[2], p, sphere && bothRound);
   }
 }
 
@@ -985,12 +989,15 @@ __global__ void __launch_bounds__(128) k_np_box(BodyPtrs bd, const WorldDev* __r
   }
 }
 
-// Pass 2b: pairs with a sphere (generic support-function SAT, one contact).
+// Pass 2b: pairs with a sphere (generic support-function SAT, one contact): sphere-box pairs,
+// then sphere-sphere pairs in a lighter instance of the same code.
+template <bool BOTH_ROUND>
 __global__ void __launch_bounds__(128) k_np_sphere(BodyPtrs bd, const WorldDev* __restrict__ worlds, PairPtrs cur, Tick t,
                                                    NarrowScratch ns) {
-  const int n = ns.ctr[1];
+  const int n = ns.ctr[BOTH_ROUND ? 2 : 1];
+  const int* list = BOTH_ROUND ? ns.sphere2List : ns.sphereList;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-    const int p = ns.sphereList[k];
+    const int p = list[k];
     const uint2 key = cur.pair[p];
     const int a = int(key.x), b = int(key.y);
     const float4 pA = bd.pos(a), qA = bd.rot(a), sA = bd.size[a];
@@ -1000,20 +1007,21 @@ __global__ void __launch_bounds__(128) k_np_sphere(BodyPtrs bd, const WorldDev* 
     M33 basis{V3{0, 0, 0}, V3{0, 0, 0}, V3{0, 0, 0}};
     uint32_t feat[1] = {1u};  // feature i + 1
     V3 rA[1], rB[1];
-    const int nc = gen::collide(pA, qA, sA, shA, pB, qB, sB, shB, basis, rA[0], rB[0]);
+    const int nc = gen::collide<BOTH_ROUND>(pA, qA, sA, shA, pB, qB, sB, shB, basis, rA[0], rB[0]);
     finish_pair(bd, W, t, bd.meta[a].x, cur, p, key, pA, qA, sA, pB, qB, sB, true, nc, basis, feat, rA, rB);
   }
 }
 
 void launch_narrowphase(const BodyPtrs& b, const WorldDev* worlds, Tick t, PairPtrs P, NarrowScratch ns, const Counters* ctr,
                         int pairBudget, cudaStream_t s) {
-  cudaMemsetAsync(ns.ctr, 0, 2 * sizeof(int), s);
+  cudaMemsetAsync(ns.ctr, 0, 3 * sizeof(int), s);
   if (t.nActive == 0) return;
   int blocks = grid_blocks(pairBudget, 256);
   if (blocks > 152 * 16) blocks = 152 * 16;
   k_np_classify<<<blocks, 256, 0, s>>>(b, worlds, P, t, ctr, ns); note_launches(1);
   k_np_box<<<152 * 16, 128, 0, s>>>(b, worlds, P, t, ns); note_launches(1);
-  k_np_sphere<<<152 * 16, 128, 0, s>>>(b, worlds, P, t, ns); note_launches(1);
+  k_np_sphere<false><<<152 * 16, 128, 0, s>>>(b, worlds, P, t, ns); note_launches(1);
+  k_np_sphere<true><<<152 * 16, 128, 0, s>>>(b, worlds, P, t, ns); note_launches(1);
 }
 
 }  // namespace avbd

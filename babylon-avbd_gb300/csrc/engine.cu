@@ -92,12 +92,6 @@ namespace {
 
 void bind(avbd_ctx* c) { CK(cudaSetDevice(c->device)); }
 
-// Stage host bytes into a temporary device buffer; freed by the caller via the returned pointer.
-template <class X> X* upload(const X* h, size_t n, cudaStream_t s) {
-  X* d = dalloc<X>(n);
-  CK(cudaMemcpyAsync(d, h, n * sizeof(X), cudaMemcpyHostToDevice, s));
-  return d;
-}
 
 void forget(avbd_ctx* ctx, Arena* A) {
   auto& v = ctx->owned;
@@ -132,14 +126,15 @@ void readSelected(Arena& A, int w, const uint32_t* indices, int n, int posesOnly
   for (int k = 0; k < n; k++) REQUIRE(indices[k] < uint32_t(R.nBodies), "body index out of range");
   if (n == 0) return;
   const int stride = posesOnly ? 8 : 40;
-  uint32_t* di = upload(indices, size_t(n), A.s);
-  float* dout = dalloc<float>(size_t(n) * stride);
+  const size_t ib = Arena::align256(size_t(n) * 4);
+  char* io = A.ioBuffer(ib + size_t(n) * stride * 4);
+  uint32_t* di = reinterpret_cast<uint32_t*>(io);
+  float* dout = reinterpret_cast<float*>(io + ib);
+  A.put(di, indices, size_t(n) * 4);
   k_read_selected<<<grid_blocks(n, 128), 128, 0, A.s>>>(A.B, A.worlds, di, n, R.dev.bodyOff, posesOnly, dout); note_launches(1);
-  cudaError_t e = cudaMemcpyAsync(out, dout, size_t(n) * stride * 4, cudaMemcpyDeviceToHost, A.s);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(A.s);
-  dfree(di);
-  dfree(dout);
-  if (e != cudaSuccess) throw Error(AVBD_E_CUDA, cudaGetErrorString(e));
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(out, dout, size_t(n) * stride * 4, cudaMemcpyDeviceToHost, A.s));
+  A.flush();
 }
 
 void setVelocities(Arena& A, int off, int limit, const uint32_t* indices, int n, const float* velocity, const float* angular) {
@@ -149,15 +144,16 @@ void setVelocities(Arena& A, int off, int limit, const uint32_t* indices, int n,
   for (int k = 0; velocity && k < 3 * n; k++) REQUIRE(std::isfinite(velocity[k]), "velocities must be finite");
   for (int k = 0; angular && k < 3 * n; k++) REQUIRE(std::isfinite(angular[k]), "velocities must be finite");
   if (n == 0 || (!velocity && !angular)) return;
-  uint32_t* di = upload(indices, size_t(n), A.s);
-  float* dv = velocity ? upload(velocity, size_t(n) * 3, A.s) : nullptr;
-  float* da = angular ? upload(angular, size_t(n) * 3, A.s) : nullptr;
+  const size_t ib = Arena::align256(size_t(n) * 4), vb = Arena::align256(size_t(n) * 12);
+  char* io = A.ioBuffer(ib + 2 * vb);
+  uint32_t* di = reinterpret_cast<uint32_t*>(io);
+  float* dv = velocity ? reinterpret_cast<float*>(io + ib) : nullptr;
+  float* da = angular ? reinterpret_cast<float*>(io + ib + vb) : nullptr;
+  A.put(di, indices, size_t(n) * 4);
+  if (dv) A.put(dv, velocity, size_t(n) * 12);
+  if (da) A.put(da, angular, size_t(n) * 12);
   k_set_velocities<<<grid_blocks(n, 128), 128, 0, A.s>>>(A.B, di, n, off, dv, da); note_launches(1);
-  cudaError_t e = cudaStreamSynchronize(A.s);
-  dfree(di);
-  dfree(dv);
-  dfree(da);
-  if (e != cudaSuccess) throw Error(AVBD_E_CUDA, cudaGetErrorString(e));
+  CK(cudaGetLastError());
 }
 
 }  // namespace
@@ -334,15 +330,16 @@ int avbd_world_set_poses(avbd_world* w, const uint32_t* indices, int32_t n, cons
               "rotations must be finite and nonzero");
     }
   if (n == 0) return AVBD_OK;
-  uint32_t* di = upload(indices, size_t(n), A.s);
-  float* dp = upload(position, size_t(n) * 3, A.s);
-  float* dr = rotation ? upload(rotation, size_t(n) * 4, A.s) : nullptr;
+  const size_t ib = Arena::align256(size_t(n) * 4), pb = Arena::align256(size_t(n) * 12);
+  char* io = A.ioBuffer(ib + pb + size_t(n) * 16);
+  uint32_t* di = reinterpret_cast<uint32_t*>(io);
+  float* dp = reinterpret_cast<float*>(io + ib);
+  float* dr = rotation ? reinterpret_cast<float*>(io + ib + pb) : nullptr;
+  A.put(di, indices, size_t(n) * 4);
+  A.put(dp, position, size_t(n) * 12);
+  if (dr) A.put(dr, rotation, size_t(n) * 16);
   k_set_poses<<<grid_blocks(n, 128), 128, 0, A.s>>>(A.B, di, n, R.dev.bodyOff, dp, dr); note_launches(1);
-  cudaError_t e = cudaStreamSynchronize(A.s);
-  dfree(di);
-  dfree(dp);
-  dfree(dr);
-  if (e != cudaSuccess) throw Error(AVBD_E_CUDA, cudaGetErrorString(e));
+  CK(cudaGetLastError());
   API_END
 }
 

@@ -149,11 +149,12 @@ struct Grid {
 
 // Narrowphase scratch (per tick), indexed by position q in the tick's active pair list: SAT
 // results of overlapping box pairs, the queued lists (box hits by q, sphere pairs by slot) and
-// their counts (ctr[0] box hits, ctr[1] sphere pairs).
+// their counts (ctr[0] box hits, ctr[1] sphere-box pairs, ctr[2] sphere-sphere pairs).
 struct NarrowScratch {
   float4* sat;
   int* boxList;
-  int* sphereList;
+  int* sphereList;   // pairs of a sphere and a box
+  int* sphere2List;  // pairs of two spheres
   int* ctr;
 };
 
