@@ -32,7 +32,7 @@ class SceneDesc(C.Structure):
                 ("mass", _fp), ("moment", _fp), ("friction", _fp), ("radius", _fp),
                 ("shape", _ip), ("group", _up), ("collides_with", _up), ("n_cons", C.c_int32),
                 ("cons_kind", _ip), ("cons_a", _ip), ("cons_b", _ip), ("cons_ra", _fp),
-                ("cons_rb", _fp), ("cons_p0", _fp), ("cons_p1", _fp), ("cons_p2", _fp)]
+                ("cons_rb", _fp), ("cons_p0", _fp), ("cons_p1", _fp), ("cons_p2", _fp), ("restitution", _fp)]
 
 
 class Counters(C.Structure):
@@ -170,13 +170,13 @@ class PackedScene:
         self.keep = [f32(s.pos), f32(s.quat), f32(s.size), f32(s.vel), f32(s.angvel), f32(s.prev_vel),
                      f32(s.mass), f32(s.moment), f32(s.friction), f32(s.radius), i32(s.shape),
                      u32(s.group), u32(s.mask), i32(s.kind), i32(s.ca), i32(s.cb), f32(s.ra),
-                     f32(s.rb), f32(s.p0), f32(s.p1), f32(s.p2)]
+                     f32(s.rb), f32(s.p0), f32(s.p1), f32(s.p2), f32(s.restitution_or_zero())]
         k = self.keep
         self.desc = SceneDesc(s.n_bodies, fptr(k[0]), fptr(k[1]), fptr(k[2]), fptr(k[3]), fptr(k[4]),
                               fptr(k[5]), fptr(k[6]), fptr(k[7]), fptr(k[8]), fptr(k[9]), iptr(k[10]),
                               uptr(k[11]), uptr(k[12]), s.n_cons, iptr(k[13]), iptr(k[14]),
                               iptr(k[15]), fptr(k[16]), fptr(k[17]), fptr(k[18]), fptr(k[19]),
-                              fptr(k[20]))
+                              fptr(k[20]), fptr(k[21]))
         p = s.params
         self.params = Params(p.dt, p.gravity, (C.c_float * 3)(*p.up), p.iterations, p.alpha,
                              p.beta_lin, p.beta_ang, p.gamma, int(p.mass_penalty), int(p.face_bias),

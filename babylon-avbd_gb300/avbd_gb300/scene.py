@@ -74,6 +74,10 @@ class SceneArrays:
     p1: np.ndarray
     p2: np.ndarray
     params: SolverParams = field(default_factory=SolverParams)
+    restitution: np.ndarray | None = None  # per body, 0..1 (None: all zero)
+
+    def restitution_or_zero(self) -> np.ndarray:
+        return self.restitution if self.restitution is not None else np.zeros(self.n_bodies, dtype=np.float64)
 
     @property
     def n_bodies(self) -> int:
@@ -86,7 +90,7 @@ class SceneArrays:
 
 class _Body:
     __slots__ = ("pos", "quat", "size", "vel", "angvel", "prev_vel", "mass", "moment",
-                 "friction", "radius", "shape", "group", "mask")
+                 "friction", "radius", "shape", "group", "mask", "restitution")
 
     def __init__(self, size, density, friction, position, velocity=(0.0, 0.0, 0.0)):
         # body.ts:32-54
@@ -107,6 +111,7 @@ class _Body:
         self.shape = SHAPE_BOX
         self.group = MASK_ALL
         self.mask = MASK_ALL
+        self.restitution = 0.0
 
 
 class SceneBuilder:
@@ -177,6 +182,7 @@ class SceneBuilder:
             cb=np.array([c[2] for c in self.cons], dtype=np.int32),
             ra=np.array([c[3] for c in self.cons], dtype=np.float64).reshape(m, 3),
             rb=np.array([c[4] for c in self.cons], dtype=np.float64).reshape(m, 3),
+            restitution=np.array([b.restitution for b in B], dtype=np.float64),
             p0=np.array([c[5] for c in self.cons], dtype=np.float64),
             p1=np.array([c[6] for c in self.cons], dtype=np.float64),
             p2=np.array([c[7] for c in self.cons], dtype=np.float64),
@@ -259,8 +265,10 @@ class AvbdScene3D:
         for k in options:
             if k not in allowed:
                 raise ValueError(f"unknown body option {k}")
-        if options.get("restitution", 0) != 0:
-            raise ValueError("restitution is not supported by the gb300 backend")
+        if "restitution" in options:
+            e = options["restitution"]
+            if not isinstance(e, (int, float)) or not math.isfinite(e) or e < 0 or e > 1:
+                raise ValueError("restitution must be between 0 and 1")
         if options.get("isTrigger", False):
             raise ValueError("triggers are not supported by the gb300 backend")
 
@@ -289,6 +297,7 @@ class AvbdScene3D:
         b = self._b.bodies[i]
         b.group = _mask(options.get("group", MASK_ALL))
         b.mask = _mask(options.get("collidesWith", MASK_ALL))
+        b.restitution = float(options.get("restitution", 0.0))
         if "mass" in options:
             mass = _positive(options["mass"], "mass", True)
             if b.mass == 0 and mass > 0:

@@ -134,6 +134,7 @@ struct Snapshot {
   std::vector<float4> pose, pose0, poseY;          // (pos, rot) pairs
   std::vector<float4> vel, ang, vprev, size, mass;  // one per body
   std::vector<int4> meta;
+  std::vector<float> restitution;
   std::vector<int2> jab;
   std::vector<float4> joint[10];  // rA rB stiff penLin penAng lamLin lamAng C0Lin C0Ang restQ
   std::vector<int> jbroken;
@@ -172,6 +173,8 @@ class Arena {
   int bvhCap = 0;
   BvhScratch bsc{};
   size_t bscKeys = 0, bscHist = 0, bscClusters = 0, bscBounds = 0;
+  BounceBufs BB{};  // bounce pass (FLAG_RESTITUTION), see ensureBounce
+  size_t bounceBodies = 0, bounceSlots = 0;
   std::vector<int> freeSlots;
   std::vector<WorldRec> W;
   // device
@@ -277,6 +280,7 @@ class Arena {
     for (float4** p : {&B.pose, &B.pose0, &B.poseY}) *p = dalloc<float4>(2 * N);
     for (float4** p : {&B.vel, &B.ang, &B.vprev, &B.size, &B.mass}) *p = dalloc<float4>(N);
     B.meta = dalloc<int4>(N);
+    B.restitution = dalloc<float>(N);
     J.ab = dalloc<int2>(NJ);
     for (float4** p : {&J.rA, &J.rB, &J.stiff, &J.penLin, &J.penAng, &J.lamLin, &J.lamAng, &J.C0Lin, &J.C0Ang, &J.restQ})
       *p = dalloc<float4>(NJ);
@@ -330,7 +334,8 @@ class Arena {
   }
 
   void release() {
-    void* ptrs[] = {B.pose, B.pose0, B.poseY, B.vel, B.ang, B.vprev, B.size, B.mass, B.meta, J.ab, J.rA,
+    void* ptrs[] = {B.pose, B.pose0, B.poseY, B.vel, B.ang, B.vprev, B.size, B.mass, B.meta, B.restitution, BB.inVel,
+                    BB.inAng, BB.ra, BB.rb, BB.nk, BB.delta, J.ab, J.rA,
                     J.rB, J.stiff, J.penLin, J.penAng, J.lamLin, J.lamAng, J.C0Lin, J.C0Ang, J.restQ, J.broken, worlds,
                     which, pairN, wover, wactive, active, activeBodies, activeJoints, pairPrefix, pairCount, G.cellCount,
                     G.cellFill, G.cellBodies, G.cellKey, G.cellPos, G.pairTmp, G.bodyBucket, G.large, T.adjStart, T.adjFill, T.activeIndex, T.color, T.won,
@@ -421,6 +426,7 @@ class Arena {
     for (float4** p : {&B.pose, &B.pose0, &B.poseY}) regrow(*p, 2 * o, 2 * N);
     for (float4** p : {&B.vel, &B.ang, &B.vprev, &B.size, &B.mass}) regrow(*p, o, N);
     regrow(B.meta, o, N);
+    regrow(B.restitution, o, N);
     int* c = dalloc<int>(2 * N);  // both colour buffers, stride = capacity
     CK(cudaMemcpyAsync(c, T.color, o * 4, cudaMemcpyDeviceToDevice, s));
     CK(cudaMemcpyAsync(c + N, T.color + o, o * 4, cudaMemcpyDeviceToDevice, s));
@@ -502,13 +508,14 @@ class Arena {
   size_t scratchBytes() const { return itemCap * sizeof(int4); }
   static size_t scratchReserve(long long nb) { return size_t(nb) * 512; }
   size_t footprint(long long nb, long long nj, long long slots, long long nw) const {
-    const size_t perBody = 12 * 16 + 2 * 4 + 1 + 11 * 4 + 32 + 4 * PAIR_TMP;
+    const size_t perBody = 12 * 16 + 2 * 4 + 1 + 12 * 4 + 32 + 4 * PAIR_TMP;
     const size_t perJoint = 8 + 10 * 16 + 4 + 4 + 8;
     const size_t perSlot = 2 * (8 + 4 + 3 * 16 + MAX_CONTACTS * 64) + 16 + 4 * 4 + 8;
     const size_t perWorld = sizeof(WorldDev) + 4 * 4 + 16 + 4 + MAX_LARGE * 4;
     return size_t(nb) * perBody + size_t(tableFor(size_t(nb))) * 8 + size_t(nj) * perJoint + size_t(slots) * perSlot +
            size_t(nw) * perWorld + size_t(ncCap) * 12 + scanBytes + size_t(bvhCap) * (32 + 12) +
-           (2 * bscKeys * sizeof(uint2) + bscHist * 4 + bscClusters * 4 + bscBounds * 16);
+           (2 * bscKeys * sizeof(uint2) + bscHist * 4 + bscClusters * 4 + bscBounds * 16) +
+           (bounceBodies * 32 + bounceSlots * 52);
   }
   size_t deviceBytes() const { return footprint(bodyCap, jointCap, slotCap, maxWorlds) + scratchBytes(); }
 
@@ -615,6 +622,12 @@ class Arena {
     Wd.up2 = p.up[2];
     Wd.iterations = p.iterations;
     Wd.flags = (p.mass_penalty ? FLAG_MASS_PENALTY : 0) | (p.face_bias ? FLAG_FACE_BIAS : 0);
+    if (d.restitution)
+      for (int i = 0; i < d.n_bodies; i++)
+        if (d.restitution[i] > 0.f) {
+          Wd.flags |= FLAG_RESTITUTION;
+          break;
+        }
     Wd.bodyCount = d.n_bodies;
     R.largeLocal.clear();
     float largeR = INFINITY;
@@ -833,6 +846,7 @@ class Arena {
     if (n) {
       std::vector<float4> pos(n), rot(n), vel(n), ang(n), vprev(n), size(n), mass(n);
       std::vector<int4> meta(n);
+      std::vector<float> rest(n);
       auto v3at = [&](const float* a, size_t k) { return a ? make_float4(a[3 * k], a[3 * k + 1], a[3 * k + 2], 0.f) : make_float4(0, 0, 0, 0); };
       for (size_t i = 0; i < n; i++) {
         pos[i] = v3at(d.position, i);
@@ -845,6 +859,7 @@ class Arena {
         size[i] = v3at(d.size, i);
         size[i].w = d.friction[i];
         mass[i] = make_float4(d.mass[i], d.moment[3 * i], d.moment[3 * i + 1], d.moment[3 * i + 2]);
+        rest[i] = d.restitution ? d.restitution[i] : 0.f;
         const uint32_t grp = d.group ? d.group[i] : 0xffffffffu, msk = d.collides_with ? d.collides_with[i] : 0xffffffffu;
         meta[i] = make_int4(w, d.shape[i], int(grp), int(msk));
       }
@@ -858,6 +873,7 @@ class Arena {
       float4* dst[5] = {B.vel, B.ang, B.vprev, B.size, B.mass};
       for (int k = 0; k < 5; k++) put(dst[k] + off, src[k], n * 16);
       put(B.meta + off, meta.data(), n * 16);
+      put(B.restitution + off, rest.data(), n * 4);
       std::vector<int> minus(n, -1);
       put(T.color + off, minus.data(), n * 4);
       put(T.color + bodyCap + off, minus.data(), n * 4);
@@ -957,6 +973,7 @@ class Arena {
     getRange(S->size, B.size, off, n);
     getRange(S->mass, B.mass, off, n);
     getRange(S->meta, B.meta, off, n);
+    getRange(S->restitution, B.restitution, off, n);
     getRange(S->jab, J.ab, joff, nj);
     for (auto& ab : S->jab) {
       if (ab.x >= 0) ab.x -= int(off);
@@ -1007,6 +1024,7 @@ class Arena {
     putRange(B.size, off, S.size);
     putRange(B.mass, off, S.mass);
     putRange(B.meta, off, S.meta);
+    putRange(B.restitution, off, S.restitution);
     for (auto& ab : S.jab) {
       if (ab.x >= 0) ab.x += int(off);
       ab.y += int(off);
@@ -1205,6 +1223,25 @@ class Arena {
   }
 
   // ------------------------------------------------------------------ ticks
+  // bounce-pass scratch (worlds with FLAG_RESTITUTION): incoming velocities per body, state per
+  // active pair; allocated on first use at the arena's capacities
+  void ensureBounce() {
+    if (bounceBodies < size_t(bodyCap)) {
+      CK(cudaStreamSynchronize(s));
+      rescratch(BB.inVel, size_t(bodyCap));
+      rescratch(BB.inAng, size_t(bodyCap));
+      bounceBodies = size_t(bodyCap);
+    }
+    if (bounceSlots < size_t(slotCap)) {
+      CK(cudaStreamSynchronize(s));
+      rescratch(BB.ra, size_t(slotCap));
+      rescratch(BB.rb, size_t(slotCap));
+      rescratch(BB.nk, size_t(slotCap));
+      rescratch(BB.delta, size_t(slotCap));
+      bounceSlots = size_t(slotCap);
+    }
+  }
+
   void ensureItems() {
     const size_t need = size_t(std::max(ctrHost->itemsTotal, 1));
     if (need > itemCap) {
@@ -1322,8 +1359,13 @@ class Arena {
         if (prof) span(P_DUAL, d, mark());
       }
     }
+    bool bounce = false;
+    for (int w : act) bounce |= (W[w].dev.flags & FLAG_RESTITUTION) != 0;
+    if (bounce) ensureBounce();
     cudaEvent_t v0 = prof ? mark() : nullptr;
+    if (bounce) launch_bounce_capture(B, t, BB, s);
     launch_velocities(B, worlds, t, s);
+    if (bounce) launch_bounce(B, P, t, T, ctr, pairBudget, BB, worlds, s);
     if (prof) span(P_OTHER, v0, mark());
     if (prof) {
       CK(cudaMemsetAsync(traffic, 0, 3 * sizeof(unsigned long long), s));

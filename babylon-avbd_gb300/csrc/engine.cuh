@@ -44,6 +44,7 @@ constexpr int KIND_SPRING = 1;
 constexpr int FLAG_MASS_PENALTY = 1;
 constexpr int FLAG_FACE_BIAS = 2;
 constexpr int FLAG_BVH = 4;  // broadphase by the world's bounding-volume hierarchy (bvh.cu)
+constexpr int FLAG_RESTITUTION = 8;  // some body has restitution > 0: run the bounce pass
 
 // Per-world parameters and ranges (96 bytes).
 struct WorldDev {
@@ -62,6 +63,7 @@ struct BodyPtrs {
   float4 *pose, *pose0, *poseY;  // (pos, rot) at [2i], [2i + 1]: current, step start (x-), inertial
   float4 *vel, *ang, *vprev, *size, *mass;
   int4* meta;
+  float* restitution;  // per body (0 for most)
   __host__ __device__ __forceinline__ float4& pos(int i) const { return pose[2 * size_t(i)]; }
   __host__ __device__ __forceinline__ float4& rot(int i) const { return pose[2 * size_t(i) + 1]; }
   __host__ __device__ __forceinline__ float4& pos0(int i) const { return pose0[2 * size_t(i)]; }
@@ -251,6 +253,17 @@ void launch_primal(const BodyPtrs& b, const WorldDev* worlds, JointPtrs j, PairP
 // Joint duals of one iteration (contact duals run inside launch_primal, see k_primal).
 void launch_dual_joints(const BodyPtrs& b, const WorldDev* worlds, JointPtrs j, Tick t, int iteration, cudaStream_t s);
 void launch_velocities(const BodyPtrs& b, const WorldDev* worlds, Tick t, cudaStream_t s);
+// Restitution (src/native/cpu/restitution.js): per active pair q the bounce state: ra (xyz,
+// target speed), rb (xyz, accumulated impulse), nk (normal, effective mass k; k == 0: inactive),
+// delta (this round's impulse change); incoming velocities per body.
+struct BounceBufs {
+  float4 *inVel, *inAng;
+  float4 *ra, *rb, *nk;
+  float* delta;
+};
+void launch_bounce_capture(const BodyPtrs& b, Tick t, BounceBufs bb, cudaStream_t s);
+void launch_bounce(const BodyPtrs& b, PairPtrs P, Tick t, Topo topo, const Counters* ctr, int pairBudget, BounceBufs bb,
+                   const WorldDev* worlds, cudaStream_t s);
 // Body command records of one world (sorted by body, ranges per body; see k_apply_edits), and
 // the warm-start drop of teleported bodies (sorted local indices) in its last pair region.
 void launch_apply_edits(const BodyPtrs& b, const uint32_t* rec, const int2* ranges, int nranges, int bodyOff, cudaStream_t s);

@@ -89,6 +89,8 @@ typedef struct avbd_scene_desc {
   const float* cons_p0;          /* joint: linear stiffness (INFINITY = hard); spring: stiffness */
   const float* cons_p1;          /* joint: angular stiffness; spring: rest length (-1: current) */
   const float* cons_p2;          /* joint: fracture threshold on |lambda_ang| */
+  const float* restitution;      /* n [0] restitution 0..1 (addBox/addSphere option; the velocity
+                                    bounce pass of src/native/cpu/restitution.js runs when > 0) */
 } avbd_scene_desc;
 
 /* readCounters() of src/vendor/three-avbd-lib/solver3D.ts:1460-1463 plus engine state. */

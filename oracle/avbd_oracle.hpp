@@ -217,7 +217,7 @@ template <class R> struct Body {
   R y[3] = {0, 0, 0}, qy[4] = {0, 0, 0, 1};
   R v[3] = {0, 0, 0}, w[3] = {0, 0, 0}, vprev[3] = {0, 0, 0};
   R size[3] = {1, 1, 1};
-  R mass = 0, moment[3] = {0, 0, 0}, friction = 0, radius = 0;
+  R mass = 0, moment[3] = {0, 0, 0}, friction = 0, radius = 0, restitution = 0;
   int shape = SHAPE_BOX;
   uint32_t group = 0xffffffffu, mask = 0xffffffffu;
   std::vector<int> forces;  // force ids, in link order (newest last)
@@ -907,9 +907,125 @@ template <class R> class Solver {
     }
     forces.swap(kept);
   }
+  // Velocity-level restitution after the solve (src/native/cpu/restitution.js, with the GPU
+  // backend's arrangement, src/gpu/restitution.js: manifold centroids summed then divided, an
+  // impact threshold of 1 m/s, 12 Jacobi rounds relaxed by the larger constraint-list length of
+  // the two bodies, each body's velocity change summed in its constraint-list order). Constraint
+  // lists hold dynamic bodies only, as the GPU backend's adjacency does, so a static body's
+  // degree is 0 (the CPU world counts a static body's forces too).
+  struct Bounce {
+    int a, b;
+    R n[3], ra[3], rb[3], k, target, impulse, delta;
+  };
+  R invMass(int i) const { return bodies[i].mass > 0 ? R(1) / bodies[i].mass : R(0); }
+  void invInertia(R* o, int i, const R* t) const {
+    const Body<R>& bd = bodies[i];
+    if (!(bd.mass > 0)) {
+      Mt::set3(o, 0, 0, 0);
+      return;
+    }
+    R c[4] = {-bd.q[0], -bd.q[1], -bd.q[2], bd.q[3]}, local[3];
+    Mt::rotate(local, c, t);
+    for (int k = 0; k < 3; k++) local[k] = bd.moment[k] > 0 ? local[k] / bd.moment[k] : R(0);
+    Mt::rotate(o, bd.q, local);
+  }
+  static void pointVelocity(R* o, const R* v, const R* w, const R* r) {
+    R c[3];
+    Mt::cross(c, w, r);
+    Mt::add3(o, v, c);
+  }
+  void bounce(const std::vector<R>& inV, const std::vector<R>& inW, const std::vector<std::vector<int>>& lists) {
+    std::vector<int> slot(store.size(), -1);
+    std::vector<Bounce> bs;
+    for (int id : forces) {
+      const Force<R>& f = *store[id];
+      if (f.type != F_MANIFOLD || f.contacts.empty()) continue;
+      const R e = std::max(bodies[f.a].restitution, bodies[f.b].restitution);
+      if (!(e > 0)) continue;
+      Bounce B;
+      B.a = f.a;
+      B.b = f.b;
+      for (int k = 0; k < 3; k++) B.n[k] = f.basis[k];
+      R sa[3] = {0, 0, 0}, sb[3] = {0, 0, 0}, t[3];
+      for (const Contact<R>& c : f.contacts) {
+        Mt::rotate(t, bodies[f.a].q, c.rA);
+        Mt::add3(sa, sa, t);
+        Mt::rotate(t, bodies[f.b].q, c.rB);
+        Mt::add3(sb, sb, t);
+      }
+      const R cnt = R(f.contacts.size());
+      for (int k = 0; k < 3; k++) { B.ra[k] = sa[k] / cnt; B.rb[k] = sb[k] / cnt; }
+      R pa[3], pb[3], d[3];
+      pointVelocity(pa, &inV[3 * f.a], &inW[3 * f.a], B.ra);
+      pointVelocity(pb, &inV[3 * f.b], &inW[3 * f.b], B.rb);
+      Mt::sub3(d, pa, pb);
+      const R vn = Mt::dot(B.n, d);
+      if (vn >= R(-1)) continue;
+      R ta[3], tb[3], ia[3], ib[3];
+      Mt::cross(ta, B.ra, B.n);
+      Mt::cross(tb, B.rb, B.n);
+      invInertia(ia, f.a, ta);
+      invInertia(ib, f.b, tb);
+      B.k = ((invMass(f.a) + invMass(f.b)) + Mt::dot(ta, ia)) + Mt::dot(tb, ib);
+      if (!(B.k > 0)) continue;
+      B.target = -e * vn;
+      B.impulse = 0;
+      B.delta = 0;
+      slot[id] = int(bs.size());
+      bs.push_back(B);
+    }
+    if (bs.empty()) return;
+    auto degree = [&](int i) { return bodies[i].mass > 0 ? int(lists[i].size()) : 0; };
+    for (int round = 0; round < 12; round++) {
+      for (Bounce& B : bs) {
+        R pa[3], pb[3], d[3];
+        pointVelocity(pa, bodies[B.a].v, bodies[B.a].w, B.ra);
+        pointVelocity(pb, bodies[B.b].v, bodies[B.b].w, B.rb);
+        Mt::sub3(d, pa, pb);
+        const R vn = Mt::dot(B.n, d);
+        const int deg = std::max(1, std::max(degree(B.a), degree(B.b)));
+        const R imp = std::max(R(0), B.impulse + (B.target - vn) / (B.k * R(deg)));
+        B.delta = imp - B.impulse;
+        B.impulse = imp;
+      }
+      std::vector<R> dvs(3 * bodies.size(), R(0)), dws(3 * bodies.size(), R(0));
+      for (int i = 0; i < int(bodies.size()); i++) {
+        if (!(bodies[i].mass > 0)) continue;
+        R dv[3] = {0, 0, 0}, dw[3] = {0, 0, 0};
+        for (int id : lists[i]) {
+          if (id >= int(slot.size()) || slot[id] < 0) continue;
+          const Bounce& B = bs[slot[id]];
+          const bool isA = i == B.a;
+          R imp[3], t[3], di[3];
+          for (int k = 0; k < 3; k++) imp[k] = (B.n[k] * B.delta) * (isA ? R(1) : R(-1));
+          for (int k = 0; k < 3; k++) dv[k] += imp[k] * invMass(i);
+          Mt::cross(t, isA ? B.ra : B.rb, imp);
+          invInertia(di, i, t);
+          Mt::add3(dw, dw, di);
+        }
+        for (int k = 0; k < 3; k++) { dvs[3 * i + k] = dv[k]; dws[3 * i + k] = dw[k]; }
+      }
+      for (int i = 0; i < int(bodies.size()); i++) {
+        if (!(bodies[i].mass > 0)) continue;
+        for (int k = 0; k < 3; k++) { bodies[i].v[k] += dvs[3 * i + k]; bodies[i].w[k] += dws[3 * i + k]; }
+      }
+    }
+  }
+
   // Step part 2: body warm start, iterations, velocities.
   void stepSolve() {
     const int n = int(bodies.size());
+    bool bounceOn = false;
+    for (const Body<R>& b : bodies) bounceOn |= b.restitution > 0;
+    std::vector<R> inV, inW;
+    std::vector<std::vector<int>> bounceLists;
+    if (bounceOn) {
+      inV.resize(3 * size_t(n));
+      inW.resize(3 * size_t(n));
+      for (int b = 0; b < n; b++)
+        for (int k = 0; k < 3; k++) { inV[3 * b + k] = bodies[b].v[k]; inW[3 * b + k] = bodies[b].w[k]; }
+      canonicalLists(bounceLists);
+    }
     for (int b = n - 1; b >= 0; b--) {
       Body<R>& body = bodies[b];
       R t[3], accel[3];
@@ -986,6 +1102,7 @@ template <class R> class Solver {
         Mt::div3(body.w, t, dt);
       }
     }
+    if (bounceOn) bounce(inV, inW, bounceLists);
   }
   void step() {
     stepCollide();

@@ -25,7 +25,7 @@ class _Scene(C.Structure):
                 ("angvel", _dp), ("prev_vel", _dp), ("mass", _dp), ("moment", _dp),
                 ("friction", _dp), ("radius", _dp), ("shape", _ip), ("group", _up), ("mask", _up),
                 ("n_cons", C.c_int), ("kind", _ip), ("ca", _ip), ("cb", _ip), ("ra", _dp),
-                ("rb", _dp), ("p0", _dp), ("p1", _dp), ("p2", _dp)]
+                ("rb", _dp), ("p0", _dp), ("p1", _dp), ("p2", _dp), ("restitution", _dp)]
 
 
 class _Params(C.Structure):
@@ -115,7 +115,8 @@ class OracleWorld:
                    d(scene.angvel), d(scene.prev_vel), d(scene.mass), d(scene.moment),
                    d(scene.friction), d(scene.radius), i32(scene.shape), u32(scene.group),
                    u32(scene.mask), scene.n_cons, i32(scene.kind), i32(scene.ca), i32(scene.cb),
-                   d(scene.ra), d(scene.rb), d(scene.p0), d(scene.p1), d(scene.p2))
+                   d(scene.ra), d(scene.rb), d(scene.p0), d(scene.p1), d(scene.p2),
+                   d(scene.restitution_or_zero()))
         prm = _Params(p.dt, p.gravity, (C.c_double * 3)(*p.up), p.iterations, p.alpha, p.beta_lin,
                       p.beta_ang, p.gamma, int(app), int(p.mass_penalty), int(p.face_bias),
                       int(colored), int(p.color_rounds))

@@ -39,6 +39,7 @@ struct oracle_scene {
   const double* p0;  // joint: linear stiffness; spring: stiffness
   const double* p1;  // joint: angular stiffness; spring: rest (-1: current distance)
   const double* p2;  // joint: fracture
+  const double* restitution;  // n (null: 0)
 };
 
 struct oracle_params {
@@ -87,6 +88,7 @@ template <class R> static Solver<R>* build(const oracle_scene* s, const oracle_p
     b.shape = s->shape[i];
     b.group = s->group ? s->group[i] : 0xffffffffu;
     b.mask = s->mask ? s->mask[i] : 0xffffffffu;
+    b.restitution = s->restitution ? R(s->restitution[i]) : R(0);
     w->addBody(b);
   }
   for (int c = 0; c < s->n_cons; c++) {
