@@ -23,7 +23,8 @@ class Params(C.Structure):
                 ("iterations", C.c_int32), ("alpha", C.c_float), ("beta_lin", C.c_float),
                 ("beta_ang", C.c_float), ("gamma", C.c_float), ("mass_penalty", C.c_int32),
                 ("face_bias", C.c_int32), ("color_rounds", C.c_int32), ("broadphase", C.c_int32),
-                ("bvh_rebuild", C.c_int32)]
+                ("bvh_rebuild", C.c_int32), ("sleeping", C.c_int32), ("sleep_speed", C.c_float),
+                ("sleep_time", C.c_float)]
 
 
 class SceneDesc(C.Structure):
@@ -32,7 +33,8 @@ class SceneDesc(C.Structure):
                 ("mass", _fp), ("moment", _fp), ("friction", _fp), ("radius", _fp),
                 ("shape", _ip), ("group", _up), ("collides_with", _up), ("n_cons", C.c_int32),
                 ("cons_kind", _ip), ("cons_a", _ip), ("cons_b", _ip), ("cons_ra", _fp),
-                ("cons_rb", _fp), ("cons_p0", _fp), ("cons_p1", _fp), ("cons_p2", _fp), ("restitution", _fp)]
+                ("cons_rb", _fp), ("cons_p0", _fp), ("cons_p1", _fp), ("cons_p2", _fp), ("restitution", _fp),
+                ("allow_sleep", _ip)]
 
 
 class Counters(C.Structure):
@@ -109,6 +111,13 @@ SIGNATURES = [
     ("avbd_world_flush_edits", C.c_int, [C.c_void_p]),
     ("avbd_batch_edit", C.c_int, [C.c_void_p, C.c_int32, _up, C.c_int32]),
     ("avbd_server_edit", C.c_int, [C.c_void_p, C.c_int64, _up, C.c_int32]),
+    ("avbd_world_set_sleeping", C.c_int, [C.c_void_p, C.c_int32, C.c_float, C.c_float]),
+    ("avbd_world_set_sleep_enabled", C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
+    ("avbd_world_wake_all", C.c_int, [C.c_void_p]),
+    ("avbd_world_sleep_state", C.c_int, [C.c_void_p, _ip, _fp, _ip]),
+    ("avbd_world_import_sleep_state", C.c_int, [C.c_void_p, _ip, _fp]),
+    ("avbd_batch_sleep_state", C.c_int, [C.c_void_p, C.c_int32, _ip, _fp, _ip]),
+    ("avbd_server_sleep_state", C.c_int, [C.c_void_p, C.c_int64, _ip, _fp, _ip]),
 ]
 
 # include/avbd_gb300.h
@@ -170,16 +179,18 @@ class PackedScene:
         self.keep = [f32(s.pos), f32(s.quat), f32(s.size), f32(s.vel), f32(s.angvel), f32(s.prev_vel),
                      f32(s.mass), f32(s.moment), f32(s.friction), f32(s.radius), i32(s.shape),
                      u32(s.group), u32(s.mask), i32(s.kind), i32(s.ca), i32(s.cb), f32(s.ra),
-                     f32(s.rb), f32(s.p0), f32(s.p1), f32(s.p2), f32(s.restitution_or_zero())]
+                     f32(s.rb), f32(s.p0), f32(s.p1), f32(s.p2), f32(s.restitution_or_zero()),
+                     i32(s.allow_sleep_or_one())]
         k = self.keep
         self.desc = SceneDesc(s.n_bodies, fptr(k[0]), fptr(k[1]), fptr(k[2]), fptr(k[3]), fptr(k[4]),
                               fptr(k[5]), fptr(k[6]), fptr(k[7]), fptr(k[8]), fptr(k[9]), iptr(k[10]),
                               uptr(k[11]), uptr(k[12]), s.n_cons, iptr(k[13]), iptr(k[14]),
                               iptr(k[15]), fptr(k[16]), fptr(k[17]), fptr(k[18]), fptr(k[19]),
-                              fptr(k[20]), fptr(k[21]))
+                              fptr(k[20]), fptr(k[21]), iptr(k[22]))
         p = s.params
         self.params = Params(p.dt, p.gravity, (C.c_float * 3)(*p.up), p.iterations, p.alpha,
                              p.beta_lin, p.beta_ang, p.gamma, int(p.mass_penalty), int(p.face_bias),
-                             int(p.color_rounds), BROADPHASE[p.broadphase], int(p.bvh_rebuild))
+                             int(p.color_rounds), BROADPHASE[p.broadphase], int(p.bvh_rebuild),
+                             int(bool(p.sleeping)), float(p.sleep_speed), float(p.sleep_time))
         self.n_bodies = s.n_bodies
         self.n_joints = int(np.sum(s.kind != 2)) if s.n_cons else 0

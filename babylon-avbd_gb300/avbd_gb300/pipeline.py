@@ -35,9 +35,27 @@ def _with_options(arrays: SceneArrays, options) -> SceneArrays:
         if int(r) != r or r < 1:
             raise ValueError("colorRounds must be a positive integer")
         p.color_rounds = int(r)
+    if options.get("sleeping"):
+        p.sleeping = True
+        p.sleep_speed, p.sleep_time = _sleep_thresholds(options["sleeping"], p)
     out = copy.copy(arrays)
     out.params = p
     return out
+
+
+def _sleep_thresholds(opt, p):
+    """(speed, time) of a sleeping option: true or {speedThreshold, timeThreshold}
+    (src/native/cpu/sleeping.js:3-10)."""
+    if opt is True:
+        return 0.08, 0.6
+    if not isinstance(opt, dict):
+        raise ValueError("sleeping must be true or an options object")
+    speed = opt.get("speedThreshold", 0.08)
+    time = opt.get("timeThreshold", 0.6)
+    for v in (speed, time):
+        if not isinstance(v, (int, float)) or not np.isfinite(v) or v <= 0:
+            raise ValueError("Sleep thresholds must be positive and finite")
+    return float(speed), float(time)
 
 
 def _arrays(scene) -> SceneArrays:
@@ -384,7 +402,58 @@ class World:
         b = self.readBodyState()
         st.update(pos=b["position"], quat=b["rotation"], vel=b["velocity"], angvel=b["angular"],
                   prev_vel=b["prev_velocity"], colors=self.readColors())
+        st["asleep"], st["sleep_time"] = self.readSleepState()
         return st
+
+    # sleeping (src/native/cpu/world.js:859-890) ------------------------------
+    def enableSleeping(self, options=None):
+        """Island sleeping with {speedThreshold, timeThreshold} (defaults 0.08 m/s, 0.6 s)."""
+        self._live()
+        speed, time = _sleep_thresholds(True if options is None else options, None)
+        L.check(L.lib().avbd_world_set_sleeping(self._h, 1, speed, time))
+        return self
+
+    def disableSleeping(self):
+        self._live()
+        L.check(L.lib().avbd_world_set_sleeping(self._h, 0, 0.0, 0.0))
+        return self
+
+    def setSleepEnabled(self, index, enabled):
+        self._live()
+        if not isinstance(enabled, bool):
+            raise ValueError("Sleep flag must be boolean")
+        L.check(L.lib().avbd_world_set_sleep_enabled(self._h, int(index), int(enabled)))
+        return self
+
+    def wakeAll(self):
+        self._live()
+        L.check(L.lib().avbd_world_wake_all(self._h))
+        return self
+
+    def wakeUp(self, index):
+        if not 0 <= int(index) < self.bodyCount:
+            raise ValueError("A live body index is required")
+        return self.wakeAll()
+
+    def readSleepStats(self) -> dict:
+        self._live()
+        n = C.c_int32()
+        L.check(L.lib().avbd_world_sleep_state(self._h, None, None, C.byref(n)))
+        return {"sleeping": int(n.value), "wakeRequested": False}
+
+    def readSleepState(self):
+        """(sleeping flags, seconds each body's island has been quiet) per body."""
+        self._live()
+        a = np.zeros(self.bodyCount, dtype=np.int32)
+        t = np.zeros(self.bodyCount, dtype=np.float32)
+        L.check(L.lib().avbd_world_sleep_state(self._h, L.iptr(a), L.fptr(t), None))
+        return a.astype(bool), t
+
+    def importSleepState(self, asleep, time):
+        self._live()
+        a = np.ascontiguousarray(asleep, dtype=np.int32)
+        t = np.ascontiguousarray(time, dtype=np.float32)
+        L.check(L.lib().avbd_world_import_sleep_state(self._h, L.iptr(a), L.fptr(t)))
 
     def profile(self, enable: bool = True):
         """Start (and reset) or stop per-kernel-class timing and traffic accounting."""
@@ -439,6 +508,15 @@ class Batch:
         L.check(L.lib().avbd_batch_read_state(self._h, int(world), *(L.fptr(out[k]) for k in
                                                                      ("position", "rotation", "velocity", "angular", "prev_velocity"))))
         return out
+
+    def readSleepState(self, world: int):
+        if not 0 <= world < self.worldCount:
+            raise ValueError("world index out of range")
+        n = self.bodyCounts[world]
+        a = np.zeros(n, dtype=np.int32)
+        t = np.zeros(n, dtype=np.float32)
+        L.check(L.lib().avbd_batch_sleep_state(self._h, int(world), L.iptr(a), L.fptr(t), None))
+        return a.astype(bool), t
 
     def readCounters(self) -> dict:
         c = L.Counters()
@@ -581,6 +659,16 @@ class Server:
         L.check(L.lib().avbd_server_read_state(self._h, int(world), *(L.fptr(out[k]) for k in
                                                                        ("position", "rotation", "velocity", "angular", "prev_velocity"))))
         return out
+
+    def readSleepState(self, world: int):
+        self._live()
+        n = self._counts.get(int(world))
+        if n is None:
+            raise ValueError(f"no such world {world}")
+        a = np.zeros(n, dtype=np.int32)
+        t = np.zeros(n, dtype=np.float32)
+        L.check(L.lib().avbd_server_sleep_state(self._h, int(world), L.iptr(a), L.fptr(t), None))
+        return a.astype(bool), t
 
     def info(self, world: int) -> dict:
         self._live()

@@ -46,6 +46,11 @@ class SolverParams:
     color_rounds: int = 64
     broadphase: str = "auto"  # "grid", "hploc" (the tree of gpuHploc.js) or "auto"; same pairs
     bvh_rebuild: int = 16     # steps between tree rebuilds; refit in between
+    # island sleeping (src/native/cpu/sleeping.js:3-16): off unless enabled by the solver
+    # options ({sleeping: true | {speedThreshold, timeThreshold}}) or a body's allowSleep: true
+    sleeping: bool = False
+    sleep_speed: float = 0.08  # m/s, |(v, w)|
+    sleep_time: float = 0.6    # seconds of quiet before a body sleeps
 
 
 @dataclass
@@ -75,9 +80,15 @@ class SceneArrays:
     p2: np.ndarray
     params: SolverParams = field(default_factory=SolverParams)
     restitution: np.ndarray | None = None  # per body, 0..1 (None: all zero)
+    allow_sleep: np.ndarray | None = None  # per body, bool (None: all may sleep)
 
     def restitution_or_zero(self) -> np.ndarray:
         return self.restitution if self.restitution is not None else np.zeros(self.n_bodies, dtype=np.float64)
+
+    def allow_sleep_or_one(self) -> np.ndarray:
+        if self.allow_sleep is None:
+            return np.ones(self.n_bodies, dtype=np.int32)
+        return np.asarray(self.allow_sleep).astype(np.int32)
 
     @property
     def n_bodies(self) -> int:
@@ -90,7 +101,7 @@ class SceneArrays:
 
 class _Body:
     __slots__ = ("pos", "quat", "size", "vel", "angvel", "prev_vel", "mass", "moment",
-                 "friction", "radius", "shape", "group", "mask", "restitution")
+                 "friction", "radius", "shape", "group", "mask", "restitution", "allow_sleep")
 
     def __init__(self, size, density, friction, position, velocity=(0.0, 0.0, 0.0)):
         # body.ts:32-54
@@ -112,6 +123,7 @@ class _Body:
         self.group = MASK_ALL
         self.mask = MASK_ALL
         self.restitution = 0.0
+        self.allow_sleep = True
 
 
 class SceneBuilder:
@@ -183,6 +195,7 @@ class SceneBuilder:
             ra=np.array([c[3] for c in self.cons], dtype=np.float64).reshape(m, 3),
             rb=np.array([c[4] for c in self.cons], dtype=np.float64).reshape(m, 3),
             restitution=np.array([b.restitution for b in B], dtype=np.float64),
+            allow_sleep=np.array([b.allow_sleep for b in B], dtype=bool),
             p0=np.array([c[5] for c in self.cons], dtype=np.float64),
             p1=np.array([c[6] for c in self.cons], dtype=np.float64),
             p2=np.array([c[7] for c in self.cons], dtype=np.float64),
@@ -265,6 +278,8 @@ class AvbdScene3D:
         for k in options:
             if k not in allowed:
                 raise ValueError(f"unknown body option {k}")
+        if "allowSleep" in options and not isinstance(options["allowSleep"], bool):
+            raise ValueError("allowSleep must be a boolean")
         if "restitution" in options:
             e = options["restitution"]
             if not isinstance(e, (int, float)) or not math.isfinite(e) or e < 0 or e > 1:
@@ -298,6 +313,9 @@ class AvbdScene3D:
         b.group = _mask(options.get("group", MASK_ALL))
         b.mask = _mask(options.get("collidesWith", MASK_ALL))
         b.restitution = float(options.get("restitution", 0.0))
+        b.allow_sleep = bool(options.get("allowSleep", True))
+        if options.get("allowSleep") is True:  # scenes.js:240 sleepOptIn
+            self._b.params.sleeping = True
         if "mass" in options:
             mass = _positive(options["mass"], "mass", True)
             if b.mass == 0 and mass > 0:

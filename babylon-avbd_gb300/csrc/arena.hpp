@@ -135,6 +135,8 @@ struct Snapshot {
   std::vector<float4> vel, ang, vprev, size, mass;  // one per body
   std::vector<int4> meta;
   std::vector<float> restitution;
+  std::vector<int> sleep;
+  std::vector<float> sleepTime;
   std::vector<int2> jab;
   std::vector<float4> joint[10];  // rA rB stiff penLin penAng lamLin lamAng C0Lin C0Ang restQ
   std::vector<int> jbroken;
@@ -174,6 +176,8 @@ class Arena {
   BvhScratch bsc{};
   size_t bscKeys = 0, bscHist = 0, bscClusters = 0, bscBounds = 0;
   BounceBufs BB{};  // bounce pass (FLAG_RESTITUTION), see ensureBounce
+  SleepBufs SB{};   // island sleeping (FLAG_SLEEP), see ensureSleep
+  size_t sleepBodies = 0, sleepWorlds = 0;
   size_t bounceBodies = 0, bounceSlots = 0;
   std::vector<int> freeSlots;
   std::vector<WorldRec> W;
@@ -281,6 +285,8 @@ class Arena {
     for (float4** p : {&B.vel, &B.ang, &B.vprev, &B.size, &B.mass}) *p = dalloc<float4>(N);
     B.meta = dalloc<int4>(N);
     B.restitution = dalloc<float>(N);
+    B.sleep = dalloc<int>(N);
+    B.sleepTime = dalloc<float>(N);
     J.ab = dalloc<int2>(NJ);
     for (float4** p : {&J.rA, &J.rB, &J.stiff, &J.penLin, &J.penAng, &J.lamLin, &J.lamAng, &J.C0Lin, &J.C0Ang, &J.restQ})
       *p = dalloc<float4>(NJ);
@@ -334,7 +340,8 @@ class Arena {
   }
 
   void release() {
-    void* ptrs[] = {B.pose, B.pose0, B.poseY, B.vel, B.ang, B.vprev, B.size, B.mass, B.meta, B.restitution, BB.inVel,
+    void* ptrs[] = {B.pose, B.pose0, B.poseY, B.vel, B.ang, B.vprev, B.size, B.mass, B.meta, B.restitution, B.sleep,
+                    B.sleepTime, SB.parent, SB.flags, SB.wake, SB.err, BB.inVel,
                     BB.inAng, BB.ra, BB.rb, BB.nk, BB.delta, J.ab, J.rA,
                     J.rB, J.stiff, J.penLin, J.penAng, J.lamLin, J.lamAng, J.C0Lin, J.C0Ang, J.restQ, J.broken, worlds,
                     which, pairN, wover, wactive, active, activeBodies, activeJoints, pairPrefix, pairCount, G.cellCount,
@@ -427,6 +434,8 @@ class Arena {
     for (float4** p : {&B.vel, &B.ang, &B.vprev, &B.size, &B.mass}) regrow(*p, o, N);
     regrow(B.meta, o, N);
     regrow(B.restitution, o, N);
+    regrow(B.sleep, o, N);
+    regrow(B.sleepTime, o, N);
     int* c = dalloc<int>(2 * N);  // both colour buffers, stride = capacity
     CK(cudaMemcpyAsync(c, T.color, o * 4, cudaMemcpyDeviceToDevice, s));
     CK(cudaMemcpyAsync(c + N, T.color + o, o * 4, cudaMemcpyDeviceToDevice, s));
@@ -508,14 +517,14 @@ class Arena {
   size_t scratchBytes() const { return itemCap * sizeof(int4); }
   static size_t scratchReserve(long long nb) { return size_t(nb) * 512; }
   size_t footprint(long long nb, long long nj, long long slots, long long nw) const {
-    const size_t perBody = 12 * 16 + 2 * 4 + 1 + 12 * 4 + 32 + 4 * PAIR_TMP;
+    const size_t perBody = 12 * 16 + 2 * 4 + 1 + 14 * 4 + 32 + 4 * PAIR_TMP;
     const size_t perJoint = 8 + 10 * 16 + 4 + 4 + 8;
     const size_t perSlot = 2 * (8 + 4 + 3 * 16 + MAX_CONTACTS * 64) + 16 + 4 * 4 + 8;
     const size_t perWorld = sizeof(WorldDev) + 4 * 4 + 16 + 4 + MAX_LARGE * 4;
     return size_t(nb) * perBody + size_t(tableFor(size_t(nb))) * 8 + size_t(nj) * perJoint + size_t(slots) * perSlot +
            size_t(nw) * perWorld + size_t(ncCap) * 12 + scanBytes + size_t(bvhCap) * (32 + 12) +
            (2 * bscKeys * sizeof(uint2) + bscHist * 4 + bscClusters * 4 + bscBounds * 16) +
-           (bounceBodies * 32 + bounceSlots * 52);
+           (bounceBodies * 32 + bounceSlots * 52) + (sleepBodies * 8 + sleepWorlds * 4 + 4);
   }
   size_t deviceBytes() const { return footprint(bodyCap, jointCap, slotCap, maxWorlds) + scratchBytes(); }
 
@@ -628,6 +637,9 @@ class Arena {
           Wd.flags |= FLAG_RESTITUTION;
           break;
         }
+    if (p.sleeping) Wd.flags |= FLAG_SLEEP;
+    Wd.sleepSpeed = p.sleep_speed > 0.f ? p.sleep_speed : 0.08f;
+    Wd.sleepDelay = p.sleep_time > 0.f ? p.sleep_time : 0.6f;
     Wd.bodyCount = d.n_bodies;
     R.largeLocal.clear();
     float largeR = INFINITY;
@@ -847,6 +859,7 @@ class Arena {
       std::vector<float4> pos(n), rot(n), vel(n), ang(n), vprev(n), size(n), mass(n);
       std::vector<int4> meta(n);
       std::vector<float> rest(n);
+      std::vector<int> sleepBits(n);
       auto v3at = [&](const float* a, size_t k) { return a ? make_float4(a[3 * k], a[3 * k + 1], a[3 * k + 2], 0.f) : make_float4(0, 0, 0, 0); };
       for (size_t i = 0; i < n; i++) {
         pos[i] = v3at(d.position, i);
@@ -860,6 +873,7 @@ class Arena {
         size[i].w = d.friction[i];
         mass[i] = make_float4(d.mass[i], d.moment[3 * i], d.moment[3 * i + 1], d.moment[3 * i + 2]);
         rest[i] = d.restitution ? d.restitution[i] : 0.f;
+        sleepBits[i] = (d.allow_sleep && d.allow_sleep[i] == 0) ? 0 : SLEEP_ALLOW;
         const uint32_t grp = d.group ? d.group[i] : 0xffffffffu, msk = d.collides_with ? d.collides_with[i] : 0xffffffffu;
         meta[i] = make_int4(w, d.shape[i], int(grp), int(msk));
       }
@@ -874,6 +888,9 @@ class Arena {
       for (int k = 0; k < 5; k++) put(dst[k] + off, src[k], n * 16);
       put(B.meta + off, meta.data(), n * 16);
       put(B.restitution + off, rest.data(), n * 4);
+      put(B.sleep + off, sleepBits.data(), n * 4);
+      std::vector<float> zeros(n, 0.f);
+      put(B.sleepTime + off, zeros.data(), n * 4);
       std::vector<int> minus(n, -1);
       put(T.color + off, minus.data(), n * 4);
       put(T.color + bodyCap + off, minus.data(), n * 4);
@@ -974,6 +991,8 @@ class Arena {
     getRange(S->mass, B.mass, off, n);
     getRange(S->meta, B.meta, off, n);
     getRange(S->restitution, B.restitution, off, n);
+    getRange(S->sleep, B.sleep, off, n);
+    getRange(S->sleepTime, B.sleepTime, off, n);
     getRange(S->jab, J.ab, joff, nj);
     for (auto& ab : S->jab) {
       if (ab.x >= 0) ab.x -= int(off);
@@ -1025,6 +1044,8 @@ class Arena {
     putRange(B.mass, off, S.mass);
     putRange(B.meta, off, S.meta);
     putRange(B.restitution, off, S.restitution);
+    putRange(B.sleep, off, S.sleep);
+    putRange(B.sleepTime, off, S.sleepTime);
     for (auto& ab : S.jab) {
       if (ab.x >= 0) ab.x += int(off);
       ab.y += int(off);
@@ -1128,6 +1149,7 @@ class Arena {
         throw Error(AVBD_E_INVALID, "rotation must be nonzero");
     }
     W[w].edits.insert(W[w].edits.end(), rec, rec + 12 * size_t(n));
+    if (n > 0) wakeWorld(w);  // queued commands wake the world (src/native/cpu/world.js:132-133)
   }
 
   // Apply world w's queued records (the reference applies them at its next step, or at
@@ -1225,6 +1247,115 @@ class Arena {
   // ------------------------------------------------------------------ ticks
   // bounce-pass scratch (worlds with FLAG_RESTITUTION): incoming velocities per body, state per
   // active pair; allocated on first use at the arena's capacities
+  // island-sleeping scratch (worlds with FLAG_SLEEP), allocated on first use
+  void ensureSleep() {
+    if (sleepBodies < size_t(bodyCap)) {
+      CK(cudaStreamSynchronize(s));
+      rescratch(SB.parent, size_t(bodyCap));
+      rescratch(SB.flags, size_t(bodyCap));
+      sleepBodies = size_t(bodyCap);
+    }
+    if (sleepWorlds < size_t(maxWorlds)) {
+      CK(cudaStreamSynchronize(s));
+      rescratch(SB.wake, size_t(maxWorlds));
+      sleepWorlds = size_t(maxWorlds);
+    }
+    if (!SB.err) {
+      SB.err = dalloc<int>(1);
+      CK(cudaMemsetAsync(SB.err, 0, sizeof(int), s));
+    }
+  }
+
+  // Wake every body of world w (src/native/cpu/sleeping.js wake): queued commands, pose and
+  // velocity writes and sleep settings do this, as the reference's world does.
+  void wakeWorld(int w) {
+    WorldRec& R = W[w];
+    if (!(R.dev.flags & FLAG_SLEEP) || R.nBodies == 0) return;
+    if (R.resident) {
+      launch_sleep_wake(B, R.dev.bodyOff, R.nBodies, s);
+      CK(cudaGetLastError());
+    } else if (R.snap) {
+      for (int& b : R.snap->sleep) b &= ~SLEEP_ASLEEP;
+      std::fill(R.snap->sleepTime.begin(), R.snap->sleepTime.end(), 0.f);
+    }
+  }
+
+  // Sleeping on/off for world w (enableSleeping / disableSleeping of src/native/cpu/world.js:
+  // 869-878); turning it off or changing the thresholds wakes the world first.
+  void setSleeping(int w, bool on, float speed, float delay) {
+    if (w < 0 || w >= maxWorlds || !W[w].live) throw Error(AVBD_E_INVALID, "no such world");
+    if (on && (!(speed > 0.f) || !(delay > 0.f) || !std::isfinite(speed) || !std::isfinite(delay)))
+      throw Error(AVBD_E_INVALID, "Sleep thresholds must be positive and finite");
+    wakeWorld(w);
+    WorldDev& D = W[w].dev;
+    D.flags = on ? (D.flags | FLAG_SLEEP) : (D.flags & ~FLAG_SLEEP);
+    if (on) {
+      D.sleepSpeed = speed;
+      D.sleepDelay = delay;
+    }
+    if (W[w].resident) uploadWorldDev(w);
+  }
+
+  // allowSleep of one body (setSleepEnabled, src/native/cpu/world.js:859-867): enabling it turns
+  // sleeping on with the default thresholds if it was off; the world wakes.
+  void setSleepAllowed(int w, int body, bool allowed) {
+    if (w < 0 || w >= maxWorlds || !W[w].live) throw Error(AVBD_E_INVALID, "no such world");
+    WorldRec& R = W[w];
+    if (body < 0 || body >= R.nBodies) throw Error(AVBD_E_INVALID, "body index out of range");
+    if (allowed && !(R.dev.flags & FLAG_SLEEP)) setSleeping(w, true, 0.08f, 0.6f);
+    if (R.resident) {
+      int bits = 0;
+      get(&bits, B.sleep + R.dev.bodyOff + body, 4);
+      bits = allowed ? (bits | SLEEP_ALLOW) : (bits & ~SLEEP_ALLOW);
+      put(B.sleep + R.dev.bodyOff + body, &bits, 4);
+    } else if (R.snap) {
+      int& bits = R.snap->sleep[body];
+      bits = allowed ? (bits | SLEEP_ALLOW) : (bits & ~SLEEP_ALLOW);
+    }
+    wakeWorld(w);
+  }
+
+  // Per-body sleep flags (1: asleep) and quiet times of world w; returns the sleeping count.
+  int sleepState(int w, int32_t* asleep, float* time) {
+    if (w < 0 || w >= maxWorlds || !W[w].live) throw Error(AVBD_E_INVALID, "no such world");
+    WorldRec& R = W[w];
+    const size_t n = size_t(R.nBodies);
+    std::vector<int> bits(n);
+    std::vector<float> t(n);
+    if (R.resident) {
+      if (n) {
+        get(bits.data(), B.sleep + R.dev.bodyOff, n * 4);
+        get(t.data(), B.sleepTime + R.dev.bodyOff, n * 4);
+      }
+    } else if (R.snap) {
+      bits = R.snap->sleep;
+      t = R.snap->sleepTime;
+    }
+    int count = 0;
+    for (size_t i = 0; i < n; i++) {
+      const int a = (bits[i] & SLEEP_ASLEEP) ? 1 : 0;
+      count += a;
+      if (asleep) asleep[i] = a;
+      if (time) time[i] = t[i];
+    }
+    return count;
+  }
+
+  // Load per-body sleep flags and quiet times into world w (state import for tests and tools).
+  void setSleepState(int w, const int32_t* asleep, const float* time) {
+    const WorldRec& R = resident(w);
+    const size_t n = size_t(R.nBodies);
+    if (!n) return;
+    std::vector<int> bits(n);
+    get(bits.data(), B.sleep + R.dev.bodyOff, n * 4);
+    for (size_t i = 0; i < n; i++) {
+      if (asleep) bits[i] = asleep[i] ? (bits[i] | SLEEP_ASLEEP) : (bits[i] & ~SLEEP_ASLEEP);
+    }
+    put(B.sleep + R.dev.bodyOff, bits.data(), n * 4);
+    if (time) put(B.sleepTime + R.dev.bodyOff, time, n * 4);
+    flush();
+  }
+
   void ensureBounce() {
     if (bounceBodies < size_t(bodyCap)) {
       CK(cudaStreamSynchronize(s));
@@ -1366,6 +1497,12 @@ class Arena {
     if (bounce) launch_bounce_capture(B, t, BB, s);
     launch_velocities(B, worlds, t, s);
     if (bounce) launch_bounce(B, P, t, T, ctr, pairBudget, BB, worlds, s);
+    bool sleeping = false;
+    for (int w : act) sleeping |= (W[w].dev.flags & FLAG_SLEEP) != 0;
+    if (sleeping) {
+      ensureSleep();
+      launch_sleep(B, worlds, J, P, NC, t, ctr, pairBudget, SB, maxWorlds, s);
+    }
     if (prof) span(P_OTHER, v0, mark());
     if (prof) {
       CK(cudaMemsetAsync(traffic, 0, 3 * sizeof(unsigned long long), s));

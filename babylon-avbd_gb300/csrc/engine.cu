@@ -48,7 +48,7 @@ __global__ void k_read_selected(BodyPtrs bd, const WorldDev* __restrict__ worlds
     o[4] = q.x; o[5] = q.y; o[6] = q.z; o[7] = q.w;
     o[8] = p0.x; o[9] = p0.y; o[10] = p0.z; o[11] = 0.f;
     o[12] = q0.x; o[13] = q0.y; o[14] = q0.z; o[15] = q0.w;
-    o[16] = sz.x; o[17] = sz.y; o[18] = sz.z; o[19] = m.x;
+    o[16] = sz.x; o[17] = sz.y; o[18] = sz.z; o[19] = (bd.sleep[i] & SLEEP_ASLEEP) ? 0.f : m.x;  // effective mass
     o[20] = m.y; o[21] = m.z; o[22] = m.w; o[23] = p.w;
     o[24] = py.x; o[25] = py.y; o[26] = py.z; o[27] = 0.f;
     o[28] = qy.x; o[29] = qy.y; o[30] = qy.z; o[31] = qy.w;
@@ -340,6 +340,7 @@ int avbd_world_set_poses(avbd_world* w, const uint32_t* indices, int32_t n, cons
   if (dr) A.put(dr, rotation, size_t(n) * 16);
   k_set_poses<<<grid_blocks(n, 128), 128, 0, A.s>>>(A.B, di, n, R.dev.bodyOff, dp, dr); note_launches(1);
   CK(cudaGetLastError());
+  A.wakeWorld(w->w);  // setPoses wakes the world (src/native/cpu/world.js:165-170)
   API_END
 }
 
@@ -350,6 +351,7 @@ int avbd_world_set_velocities(avbd_world* w, const uint32_t* indices, int32_t n,
   bind(A.ctx);
   const WorldRec& R = A.resident(w->w);
   setVelocities(A, R.dev.bodyOff, R.nBodies, indices, n, velocity, angular);
+  if (n > 0) A.wakeWorld(w->w);
   API_END
 }
 
@@ -364,7 +366,49 @@ int avbd_world_counters(avbd_world* w, avbd_counters* out) {
 int avbd_world_edit(avbd_world* w, const uint32_t* records, int32_t n) {
   API_BEGIN
   REQUIRE(w && (n == 0 || records), "null argument");
+  bind(w->A->ctx);
   w->A->queueEdits(w->w, records, n);
+  API_END
+}
+
+int avbd_world_set_sleeping(avbd_world* w, int32_t enabled, float speed_threshold, float time_threshold) {
+  API_BEGIN
+  REQUIRE(w, "null world");
+  bind(w->A->ctx);
+  w->A->setSleeping(w->w, enabled != 0, speed_threshold, time_threshold);
+  API_END
+}
+
+int avbd_world_set_sleep_enabled(avbd_world* w, int32_t body, int32_t enabled) {
+  API_BEGIN
+  REQUIRE(w, "null world");
+  bind(w->A->ctx);
+  w->A->setSleepAllowed(w->w, body, enabled != 0);
+  API_END
+}
+
+int avbd_world_wake_all(avbd_world* w) {
+  API_BEGIN
+  REQUIRE(w, "null world");
+  bind(w->A->ctx);
+  w->A->wakeWorld(w->w);
+  API_END
+}
+
+int avbd_world_sleep_state(avbd_world* w, int32_t* asleep, float* quiet_time, int32_t* n_sleeping) {
+  API_BEGIN
+  REQUIRE(w, "null world");
+  bind(w->A->ctx);
+  const int c = w->A->sleepState(w->w, asleep, quiet_time);
+  if (n_sleeping) *n_sleeping = c;
+  API_END
+}
+
+int avbd_world_import_sleep_state(avbd_world* w, const int32_t* asleep, const float* quiet_time) {
+  API_BEGIN
+  REQUIRE(w, "null world");
+  bind(w->A->ctx);
+  w->A->setSleepState(w->w, asleep, quiet_time);
   API_END
 }
 
@@ -571,6 +615,17 @@ int avbd_batch_set_velocities(avbd_batch* b, const uint32_t* indices, int32_t n,
   REQUIRE(b, "null batch");
   bind(b->A->ctx);
   setVelocities(*b->A, 0, int(b->bodies), indices, n, velocity, angular);
+  // the worlds whose bodies got velocities wake
+  std::vector<std::pair<long long, int>> start;  // (first body, world slot) in body order
+  for (int w : b->worlds) start.emplace_back(b->A->W[w].dev.bodyOff, w);
+  std::sort(start.begin(), start.end());
+  std::vector<char> hit(start.size(), 0);
+  for (int k = 0; k < n; k++) {
+    const auto it = std::upper_bound(start.begin(), start.end(), std::make_pair((long long)indices[k], INT32_MAX));
+    hit[size_t(it - start.begin()) - 1] = 1;
+  }
+  for (size_t k = 0; k < hit.size(); k++)
+    if (hit[k]) b->A->wakeWorld(start[k].second);
   API_END
 }
 
@@ -578,7 +633,18 @@ int avbd_batch_edit(avbd_batch* b, int32_t world, const uint32_t* records, int32
   API_BEGIN
   REQUIRE(b && (n == 0 || records), "null argument");
   REQUIRE(world >= 0 && world < int32_t(b->worlds.size()), "world index out of range");
+  bind(b->A->ctx);
   b->A->queueEdits(b->worlds[world], records, n);
+  API_END
+}
+
+int avbd_batch_sleep_state(avbd_batch* b, int32_t world, int32_t* asleep, float* quiet_time, int32_t* n_sleeping) {
+  API_BEGIN
+  REQUIRE(b, "null batch");
+  REQUIRE(world >= 0 && world < int32_t(b->worlds.size()), "world index out of range");
+  bind(b->A->ctx);
+  const int c = b->A->sleepState(b->worlds[world], asleep, quiet_time);
+  if (n_sleeping) *n_sleeping = c;
   API_END
 }
 

@@ -45,6 +45,9 @@ constexpr int FLAG_MASS_PENALTY = 1;
 constexpr int FLAG_FACE_BIAS = 2;
 constexpr int FLAG_BVH = 4;  // broadphase by the world's bounding-volume hierarchy (bvh.cu)
 constexpr int FLAG_RESTITUTION = 8;  // some body has restitution > 0: run the bounce pass
+constexpr int FLAG_SLEEP = 16;       // island sleeping after each step (sleep.cu)
+constexpr int SLEEP_ASLEEP = 1;      // the body sleeps: the solve leaves it where it is
+constexpr int SLEEP_ALLOW = 2;       // allowSleep (a body without it keeps its island awake)
 
 // Per-world parameters and ranges (96 bytes).
 struct WorldDev {
@@ -55,6 +58,8 @@ struct WorldDev {
   int flags, bodyOff, bodyCount, largeOff;
   int largeCount, jointOff, jointCount, pairOff;
   int pairCap, bvhNodeOff, bvhRoot, pad0;  // bvhRoot: local node id (-1: empty tree)
+  float sleepSpeed, sleepDelay;            // FLAG_SLEEP: |(v, w)| threshold, seconds of quiet
+  int pad1, pad2;
 };
 
 // Poses are stored as interleaved pairs (pos, rot) of 32 bytes: a gather of a body's pose, or of
@@ -64,6 +69,8 @@ struct BodyPtrs {
   float4 *vel, *ang, *vprev, *size, *mass;
   int4* meta;
   float* restitution;  // per body (0 for most)
+  int* sleep;          // per body: SLEEP_ASLEEP | SLEEP_ALLOW
+  float* sleepTime;    // per body: seconds its island has been quiet (FLAG_SLEEP worlds)
   __host__ __device__ __forceinline__ float4& pos(int i) const { return pose[2 * size_t(i)]; }
   __host__ __device__ __forceinline__ float4& rot(int i) const { return pose[2 * size_t(i) + 1]; }
   __host__ __device__ __forceinline__ float4& pos0(int i) const { return pose0[2 * size_t(i)]; }
@@ -264,6 +271,18 @@ struct BounceBufs {
 void launch_bounce_capture(const BodyPtrs& b, Tick t, BounceBufs bb, cudaStream_t s);
 void launch_bounce(const BodyPtrs& b, PairPtrs P, Tick t, Topo topo, const Counters* ctr, int pairBudget, BounceBufs bb,
                    const WorldDev* worlds, cudaStream_t s);
+// Island sleeping (sleep.cu): union-find parents and island flags per body, a wake flag per
+// world, an error counter (union retries that ran out).
+struct SleepBufs {
+  int* parent;
+  int* flags;
+  int* wake;
+  int* err;
+};
+void launch_sleep(const BodyPtrs& b, const WorldDev* worlds, JointPtrs J, PairPtrs P, NoCollide nc, Tick t,
+                  const Counters* ctr, int pairBudget, SleepBufs sb, int maxWorlds, cudaStream_t s);
+// wake every body of bodies [off, off + n): asleep cleared, quiet time 0
+void launch_sleep_wake(const BodyPtrs& b, int off, int n, cudaStream_t s);
 // Body command records of one world (sorted by body, ranges per body; see k_apply_edits), and
 // the warm-start drop of teleported bodies (sorted local indices) in its last pair region.
 void launch_apply_edits(const BodyPtrs& b, const uint32_t* rec, const int2* ranges, int nranges, int bodyOff, cudaStream_t s);

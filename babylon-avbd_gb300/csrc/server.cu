@@ -389,8 +389,19 @@ int avbd_server_world_info(avbd_server* s, int64_t world_id, int32_t* n_bodies, 
 int avbd_server_edit(avbd_server* s, int64_t world_id, const uint32_t* records, int32_t n) {
   API_BEGIN
   REQUIRE(s && (n == 0 || records), "null argument");
+  bind(s->ctx);
   const Served& w = s->get(world_id);
   s->A->queueEdits(w.slot, records, n);
+  API_END
+}
+
+int avbd_server_sleep_state(avbd_server* s, int64_t world_id, int32_t* asleep, float* quiet_time, int32_t* n_sleeping) {
+  API_BEGIN
+  REQUIRE(s, "null server");
+  bind(s->ctx);
+  const Served& w = s->get(world_id);
+  const int c = s->A->sleepState(w.slot, asleep, quiet_time);
+  if (n_sleeping) *n_sleeping = c;
   API_END
 }
 

@@ -53,6 +53,10 @@ typedef struct avbd_params {
   int32_t color_rounds; /* Jones-Plassmann round budget per step */
   int32_t broadphase;   /* options.broadphase (src/native/scenes.d.ts:299-300): AVBD_BROADPHASE_* */
   int32_t bvh_rebuild;  /* options.bvh.rebuildInterval: steps between tree rebuilds; <= 0: 16 */
+  int32_t sleeping;     /* options.sleeping / a body's allowSleep: true (src/native/cpu/world.js:103-108):
+                           island sleeping after each step (src/native/cpu/sleeping.js) */
+  float sleep_speed;    /* speedThreshold, |(v, w)| in m/s [0.08] */
+  float sleep_time;     /* timeThreshold, seconds of quiet before sleeping [0.6] */
 } avbd_params;
 
 /* Candidate search. Both give the same pair set; the tree (hierarchical PLOC, src/gpu/gpuHploc.js)
@@ -91,6 +95,8 @@ typedef struct avbd_scene_desc {
   const float* cons_p2;          /* joint: fracture threshold on |lambda_ang| */
   const float* restitution;      /* n [0] restitution 0..1 (addBox/addSphere option; the velocity
                                     bounce pass of src/native/cpu/restitution.js runs when > 0) */
+  const int32_t* allow_sleep;    /* n [1] allowSleep option (scenes.js:235-240): 0 keeps the body's
+                                    island awake */
 } avbd_scene_desc;
 
 /* readCounters() of src/vendor/three-avbd-lib/solver3D.ts:1460-1463 plus engine state. */
@@ -205,6 +211,20 @@ int avbd_world_export_state(avbd_world* w, float* jpen_lin, float* jpen_ang, flo
                             int32_t* jbroken, uint32_t* mpairs, int32_t* mcount, uint32_t* cfeature, float* cra,
                             float* crb, float* cpen, float* clam, int32_t* cstick);
 
+/* Island sleeping (src/native/cpu/sleeping.js; world API of src/native/cpu/world.js:859-890).
+ * enableSleeping / disableSleeping: enabled != 0 turns it on with the given thresholds
+ * (speedThreshold |(v, w)| m/s, timeThreshold s; both > 0), 0 turns it off; either wakes the
+ * world. setSleepEnabled (allowSleep of one body; enabling turns sleeping on with the defaults
+ * 0.08 / 0.6 if it was off; wakes the world). wakeAll. Queued body commands, setPoses and
+ * setVelocities also wake the world. Sleep state per body: 1 = asleep, and the seconds its island
+ * has been quiet; n_sleeping = readSleepStats().sleeping. Any output pointer may be NULL. */
+int avbd_world_set_sleeping(avbd_world* w, int32_t enabled, float speed_threshold, float time_threshold);
+int avbd_world_set_sleep_enabled(avbd_world* w, int32_t body, int32_t enabled);
+int avbd_world_wake_all(avbd_world* w);
+int avbd_world_sleep_state(avbd_world* w, int32_t* asleep, float* quiet_time, int32_t* n_sleeping);
+/* Load per-body sleep flags and quiet times (state import for one-step comparisons; NULL skips). */
+int avbd_world_import_sleep_state(avbd_world* w, const int32_t* asleep, const float* quiet_time);
+
 /* ---------------------------------------------------------------- batched worlds */
 
 /* Many independent worlds stepped together: one launch sequence per step covers every world
@@ -227,6 +247,8 @@ int avbd_batch_read_poses(avbd_batch* b, float* out);
 int avbd_batch_set_velocities(avbd_batch* b, const uint32_t* indices, int32_t n, const float* velocity, const float* angular);
 /* Body commands (as avbd_world_edit) for world `world` of the batch (world-local body indices). */
 int avbd_batch_edit(avbd_batch* b, int32_t world, const uint32_t* records, int32_t n);
+/* Sleep state of world `world` of the batch (as avbd_world_sleep_state). */
+int avbd_batch_sleep_state(avbd_batch* b, int32_t world, int32_t* asleep, float* quiet_time, int32_t* n_sleeping);
 
 /* Profiling (see avbd_profile): enable resets the accumulators; read returns them. */
 int avbd_world_profile(avbd_world* w, int32_t enable);
@@ -282,6 +304,8 @@ int avbd_server_world_info(avbd_server* s, int64_t world_id, int32_t* n_bodies, 
                            int32_t* resident);
 /* Body commands (as avbd_world_edit), applied before the world's next step. */
 int avbd_server_edit(avbd_server* s, int64_t world_id, const uint32_t* records, int32_t n);
+/* Sleep state of a served world, resident or evicted (as avbd_world_sleep_state). */
+int avbd_server_sleep_state(avbd_server* s, int64_t world_id, int32_t* asleep, float* quiet_time, int32_t* n_sleeping);
 /* Evict a world now (its queued steps wait for a restore). */
 int avbd_server_evict(avbd_server* s, int64_t world_id);
 /* Drop a world; its outstanding tickets never complete. */

@@ -219,6 +219,7 @@ template <class R> struct Body {
   R size[3] = {1, 1, 1};
   R mass = 0, moment[3] = {0, 0, 0}, friction = 0, radius = 0, restitution = 0;
   int shape = SHAPE_BOX;
+  bool sleeping = false, allowSleep = true;  // sleeping: skipped by the solve, as a static body
   uint32_t group = 0xffffffffu, mask = 0xffffffffu;
   std::vector<int> forces;  // force ids, in link order (newest last)
 };
@@ -278,6 +279,10 @@ template <class R> class Solver {
   R up[3] = {0, 0, 1};      // app only
   bool colored = false;     // GPU order (see header)
   int colorRounds = 64;
+  // island sleeping (src/native/cpu/sleeping.js): off unless enabled
+  bool sleepOn = false;
+  R sleepSpeed = R(0.08), sleepDelay = R(0.6);
+  std::vector<R> sleepTime;
 
   std::vector<Body<R>> bodies;
   std::vector<std::unique_ptr<Force<R>>> store;
@@ -917,10 +922,11 @@ template <class R> class Solver {
     int a, b;
     R n[3], ra[3], rb[3], k, target, impulse, delta;
   };
-  R invMass(int i) const { return bodies[i].mass > 0 ? R(1) / bodies[i].mass : R(0); }
+  // a sleeping body takes no impulse (restitution.js inverseMass)
+  R invMass(int i) const { return bodies[i].mass > 0 && !bodies[i].sleeping ? R(1) / bodies[i].mass : R(0); }
   void invInertia(R* o, int i, const R* t) const {
     const Body<R>& bd = bodies[i];
-    if (!(bd.mass > 0)) {
+    if (!(bd.mass > 0) || bd.sleeping) {
       Mt::set3(o, 0, 0, 0);
       return;
     }
@@ -990,7 +996,7 @@ template <class R> class Solver {
       }
       std::vector<R> dvs(3 * bodies.size(), R(0)), dws(3 * bodies.size(), R(0));
       for (int i = 0; i < int(bodies.size()); i++) {
-        if (!(bodies[i].mass > 0)) continue;
+        if (!(bodies[i].mass > 0) || bodies[i].sleeping) continue;
         R dv[3] = {0, 0, 0}, dw[3] = {0, 0, 0};
         for (int id : lists[i]) {
           if (id >= int(slot.size()) || slot[id] < 0) continue;
@@ -1006,7 +1012,7 @@ template <class R> class Solver {
         for (int k = 0; k < 3; k++) { dvs[3 * i + k] = dv[k]; dws[3 * i + k] = dw[k]; }
       }
       for (int i = 0; i < int(bodies.size()); i++) {
-        if (!(bodies[i].mass > 0)) continue;
+        if (!(bodies[i].mass > 0) || bodies[i].sleeping) continue;
         for (int k = 0; k < 3; k++) { bodies[i].v[k] += dvs[3 * i + k]; bodies[i].w[k] += dws[3 * i + k]; }
       }
     }
@@ -1041,7 +1047,7 @@ template <class R> class Solver {
         if (!std::isfinite(accelWeight)) accelWeight = 0;
         std::memcpy(body.x0, body.pos, sizeof(body.x0));
         std::memcpy(body.q0, body.q, sizeof(body.q0));
-        if (body.mass > 0) {
+        if (body.mass > 0 && !body.sleeping) {
           Mt::addScaled3(body.pos, body.pos, body.v, dt);
           Mt::addScaled3(body.pos, body.pos, up, gravity * accelWeight * dt * dt);
           Mt::scale3(t, body.w, dt);
@@ -1059,7 +1065,7 @@ template <class R> class Solver {
         if (!std::isfinite(accelWeight)) accelWeight = 0;
         std::memcpy(body.x0, body.pos, sizeof(body.x0));
         std::memcpy(body.q0, body.q, sizeof(body.q0));
-        if (body.mass > 0) {
+        if (body.mass > 0 && !body.sleeping) {
           Mt::addScaled3(body.pos, body.pos, body.v, dt);
           body.pos[2] += gravity * (accelWeight * dt * dt);
           Mt::scale3(t, body.w, dt);
@@ -1079,10 +1085,11 @@ template <class R> class Solver {
     for (int it = 0; it < iterations; it++) {
       if (colored) {
         for (int c = 0; c < MAX_COLORS; c++)
-          for (int b : buckets[c]) solveBody(b, lists[b], false);
+          for (int b : buckets[c])
+            if (!bodies[b].sleeping) solveBody(b, lists[b], false);
       } else {
         for (int b = n - 1; b >= 0; b--) {
-          if (bodies[b].mass <= 0) continue;
+          if (bodies[b].mass <= 0 || bodies[b].sleeping) continue;
           solveBody(b, bodies[b].forces, true);
         }
       }
@@ -1094,7 +1101,7 @@ template <class R> class Solver {
     }
     for (Body<R>& body : bodies) {
       std::memcpy(body.vprev, body.v, sizeof(body.v));
-      if (body.mass > 0) {
+      if (body.mass > 0 && !body.sleeping) {
         R t[3];
         Mt::sub3(t, body.pos, body.x0);
         Mt::div3(body.v, t, dt);
@@ -1107,6 +1114,73 @@ template <class R> class Solver {
   void step() {
     stepCollide();
     stepSolve();
+    if (sleepOn) sleepAfter();
+  }
+
+  // Island sleeping after the step (src/native/cpu/sleeping.js:26-108). Islands: dynamic bodies
+  // joined by any live constraint (joint, spring, ignore pair, manifold with contacts); an
+  // island is supported when one of its bodies touches a static body or hangs from the world.
+  // A supported island whose bodies all allow sleep and move no faster than the threshold
+  // (|(v, w)|, the 6-vector) accumulates time; each body whose time reaches the delay sleeps
+  // with zero velocity. A live constraint between a sleeping and an awake dynamic body wakes
+  // the whole world before the next step. The speed is sqrt of the left-to-right sum of the six
+  // squares, in the solver's precision.
+  void wakeAll() {
+    for (Body<R>& b : bodies) b.sleeping = false;
+    std::fill(sleepTime.begin(), sleepTime.end(), R(0));
+  }
+  static R sleepSpeedOf(const Body<R>& b) {
+    const R s = ((((b.v[0] * b.v[0] + b.v[1] * b.v[1]) + b.v[2] * b.v[2]) + b.w[0] * b.w[0]) + b.w[1] * b.w[1]) +
+                b.w[2] * b.w[2];
+    return std::sqrt(s);
+  }
+  void sleepAfter() {
+    const int n = int(bodies.size());
+    if (int(sleepTime.size()) != n) sleepTime.assign(n, R(0));
+    std::vector<int> root(n);
+    for (int i = 0; i < n; i++) root[i] = i;
+    auto find = [&](int i) {
+      while (root[i] != i) {
+        root[i] = root[root[i]];
+        i = root[i];
+      }
+      return i;
+    };
+    std::vector<char> support(n, 0);
+    std::vector<std::pair<int, int>> edges;
+    auto dyn = [&](int i) { return bodies[i].mass > 0; };
+    for (int id : forces) {
+      const Force<R>& f = *store[id];
+      if (f.broken) continue;
+      if (f.type == F_MANIFOLD && f.contacts.empty()) continue;
+      const int a = f.a, b = f.b;
+      if (a < 0) support[b] = 1;
+      else if (!dyn(a)) support[b] = 1;
+      else if (!dyn(b)) support[a] = 1;
+      else root[find(a)] = find(b);
+      edges.emplace_back(a, b);
+    }
+    std::vector<char> supported(n, 0), stable(n, 1);
+    for (int i = 0; i < n; i++)
+      if (support[i]) supported[find(i)] = 1;
+    for (int i = 0; i < n; i++)
+      if (dyn(i) && !(bodies[i].allowSleep && sleepSpeedOf(bodies[i]) <= sleepSpeed)) stable[find(i)] = 0;
+    for (int i = 0; i < n; i++) {
+      if (!dyn(i)) continue;
+      const int r = find(i);
+      sleepTime[i] = supported[r] && stable[r] ? sleepTime[i] + dt : R(0);
+      if (sleepTime[i] >= sleepDelay) {
+        Body<R>& b = bodies[i];
+        b.sleeping = true;
+        Mt::set3(b.v, 0, 0, 0);
+        Mt::set3(b.w, 0, 0, 0);
+      }
+    }
+    for (const auto& e : edges)
+      if (e.first >= 0 && dyn(e.first) && dyn(e.second) && bodies[e.first].sleeping != bodies[e.second].sleeping) {
+        wakeAll();
+        break;
+      }
   }
   int forceCount() const { return int(forces.size()); }
 
@@ -1116,6 +1190,7 @@ template <class R> class Solver {
   // (value.w = dt), 4 teleport (position, rotation = point; step-start and inertial poses follow;
   // the body's manifolds are dropped), 5 angular impulse, 6 torque (value.w = dt).
   void applyEdits(const uint32_t* rec, int n) {
+    if (n > 0 && sleepOn) wakeAll();  // queued body commands wake the world (world.js:132-133)
     for (int k = 0; k < n; k++) {
       const uint32_t* u = rec + 12 * size_t(k);
       float f[12];

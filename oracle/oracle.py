@@ -25,7 +25,8 @@ class _Scene(C.Structure):
                 ("angvel", _dp), ("prev_vel", _dp), ("mass", _dp), ("moment", _dp),
                 ("friction", _dp), ("radius", _dp), ("shape", _ip), ("group", _up), ("mask", _up),
                 ("n_cons", C.c_int), ("kind", _ip), ("ca", _ip), ("cb", _ip), ("ra", _dp),
-                ("rb", _dp), ("p0", _dp), ("p1", _dp), ("p2", _dp), ("restitution", _dp)]
+                ("rb", _dp), ("p0", _dp), ("p1", _dp), ("p2", _dp), ("restitution", _dp),
+                ("allow_sleep", _ip)]
 
 
 class _Params(C.Structure):
@@ -33,7 +34,8 @@ class _Params(C.Structure):
                 ("iterations", C.c_int), ("alpha", C.c_double), ("beta_lin", C.c_double),
                 ("beta_ang", C.c_double), ("gamma", C.c_double), ("app", C.c_int),
                 ("mass_penalty", C.c_int), ("face_bias", C.c_int), ("colored", C.c_int),
-                ("color_rounds", C.c_int)]
+                ("color_rounds", C.c_int), ("sleeping", C.c_int), ("sleep_speed", C.c_double),
+                ("sleep_time", C.c_double)]
 
 
 class _State(C.Structure):
@@ -75,6 +77,11 @@ def lib():
         L.oracle_world_collide.argtypes = [C.c_void_p, C.c_int, C.c_int, _dp, _up, _dp, _dp]
         L.oracle_world_import.argtypes = [C.c_void_p, C.POINTER(_State)]
         L.oracle_world_edit.argtypes = [C.c_void_p, C.POINTER(C.c_uint32), C.c_int]
+        L.oracle_world_set_sleep.argtypes = [C.c_void_p, _ip, _dp]
+        L.oracle_world_sleep_state.argtypes = [C.c_void_p, _ip, _dp]
+        L.oracle_world_sleep_state.restype = C.c_int
+        L.oracle_world_wake_all.argtypes = [C.c_void_p]
+        L.oracle_world_sleep_after.argtypes = [C.c_void_p]
         L.oracle_worlds_step_parallel.argtypes = [C.POINTER(C.c_void_p), C.c_int, C.c_int, C.c_int]
         L.oracle_worlds_step_parallel.restype = C.c_int
         _lib = L
@@ -116,10 +123,11 @@ class OracleWorld:
                    d(scene.friction), d(scene.radius), i32(scene.shape), u32(scene.group),
                    u32(scene.mask), scene.n_cons, i32(scene.kind), i32(scene.ca), i32(scene.cb),
                    d(scene.ra), d(scene.rb), d(scene.p0), d(scene.p1), d(scene.p2),
-                   d(scene.restitution_or_zero()))
+                   d(scene.restitution_or_zero()), i32(scene.allow_sleep_or_one()))
         prm = _Params(p.dt, p.gravity, (C.c_double * 3)(*p.up), p.iterations, p.alpha, p.beta_lin,
                       p.beta_ang, p.gamma, int(app), int(p.mass_penalty), int(p.face_bias),
-                      int(colored), int(p.color_rounds))
+                      int(colored), int(p.color_rounds), int(bool(p.sleeping)), float(p.sleep_speed),
+                      float(p.sleep_time))
         self.h = L.oracle_world_create(int(fp64), C.byref(s), C.byref(prm))
         self.n = scene.n_bodies
         self.n_joints = int(np.sum((scene.kind == 0) | (scene.kind == 1)))
@@ -222,6 +230,26 @@ class OracleWorld:
                    i32(st["mcount"]), u32(st["cfeature"]), d(st["cra"]), d(st["crb"]),
                    d(st["cpen"]), d(st["clam"]), i32(st["cstick"]), i32(st.get("colors")))
         lib().oracle_world_import(self.h, C.byref(s))
+
+    def set_sleep(self, asleep, time):
+        """Load per-body sleep state (flags, accumulated quiet seconds)."""
+        a = np.ascontiguousarray(asleep, dtype=np.int32)
+        t = np.ascontiguousarray(time, dtype=np.float64)
+        lib().oracle_world_set_sleep(self.h, _ptr(a, C.c_int32), _ptr(t, C.c_double))
+
+    def sleep_state(self):
+        """(sleeping flags, quiet seconds) per body."""
+        a = np.zeros(self.n, dtype=np.int32)
+        t = np.zeros(self.n, dtype=np.float64)
+        lib().oracle_world_sleep_state(self.h, _ptr(a, C.c_int32), _ptr(t, C.c_double))
+        return a.astype(bool), t
+
+    def wake_all(self):
+        lib().oracle_world_wake_all(self.h)
+
+    def sleep_after(self):
+        """The sleeping pass alone (``step`` runs it after the solve when sleeping is on)."""
+        lib().oracle_world_sleep_after(self.h)
 
     def edit(self, records):
         """Apply body command records (n x 12 uint32 words, ``src/gpu/bodyCommands2D.js``

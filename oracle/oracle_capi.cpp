@@ -40,6 +40,7 @@ struct oracle_scene {
   const double* p1;  // joint: angular stiffness; spring: rest (-1: current distance)
   const double* p2;  // joint: fracture
   const double* restitution;  // n (null: 0)
+  const int32_t* allow_sleep;  // n (null: 1)
 };
 
 struct oracle_params {
@@ -48,6 +49,8 @@ struct oracle_params {
   int iterations;
   double alpha, beta_lin, beta_ang, gamma;
   int app, mass_penalty, face_bias, colored, color_rounds;
+  int sleeping;
+  double sleep_speed, sleep_time;
 };
 
 struct OracleWorld {
@@ -71,6 +74,9 @@ template <class R> static Solver<R>* build(const oracle_scene* s, const oracle_p
   for (int i = 0; i < 3; i++) w->up[i] = R(p->up[i]);
   w->colored = p->colored != 0;
   w->colorRounds = p->color_rounds > 0 ? p->color_rounds : 64;
+  w->sleepOn = p->sleeping != 0;
+  w->sleepSpeed = R(p->sleep_speed);
+  w->sleepDelay = R(p->sleep_time);
   for (int i = 0; i < s->n_bodies; i++) {
     Body<R> b;
     for (int k = 0; k < 3; k++) {
@@ -89,6 +95,7 @@ template <class R> static Solver<R>* build(const oracle_scene* s, const oracle_p
     b.group = s->group ? s->group[i] : 0xffffffffu;
     b.mask = s->mask ? s->mask[i] : 0xffffffffu;
     b.restitution = s->restitution ? R(s->restitution[i]) : R(0);
+    b.allowSleep = s->allow_sleep ? s->allow_sleep[i] != 0 : true;
     w->addBody(b);
   }
   for (int c = 0; c < s->n_cons; c++) {
@@ -130,6 +137,32 @@ extern "C" void oracle_world_step(void* h, int steps) {
 extern "C" void oracle_world_step_collide(void* h) { DISPATCH(h, S.stepCollide()); }
 extern "C" void oracle_world_step_solve(void* h) { DISPATCH(h, S.stepSolve()); }
 extern "C" void oracle_world_set_colored(void* h, int colored) { DISPATCH(h, S.colored = colored != 0); }
+
+// Sleep state per body: sleeping flag and accumulated quiet time (import for one-step parity).
+extern "C" void oracle_world_set_sleep(void* h, const int32_t* asleep, const double* time) {
+  DISPATCH(h, {
+    const int n = int(S.bodies.size());
+    S.sleepTime.assign(n, 0);
+    for (int i = 0; i < n; i++) {
+      S.bodies[i].sleeping = asleep[i] != 0;
+      S.sleepTime[i] = decltype(S.dt)(time[i]);
+    }
+  });
+}
+extern "C" int oracle_world_sleep_state(void* h, int32_t* asleep, double* time) {
+  int count = 0;
+  DISPATCH(h, {
+    const int n = int(S.bodies.size());
+    for (int i = 0; i < n; i++) {
+      asleep[i] = S.bodies[i].sleeping ? 1 : 0;
+      time[i] = i < int(S.sleepTime.size()) ? double(S.sleepTime[i]) : 0.0;
+      count += asleep[i];
+    }
+  });
+  return count;
+}
+extern "C" void oracle_world_wake_all(void* h) { DISPATCH(h, S.wakeAll()); }
+extern "C" void oracle_world_sleep_after(void* h) { DISPATCH(h, S.sleepAfter()); }
 
 extern "C" int oracle_world_body_count(void* h) {
   int n = 0;

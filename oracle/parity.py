@@ -40,6 +40,8 @@ def compare_step(world, scene, warm: int, edits=None):
     for name, fp64 in (("fp32", False), ("fp64", True)):
         o = O.OracleWorld(scene, fp64=fp64, app=True, colored=True)
         o.import_state(st)
+        if "asleep" in st:
+            o.set_sleep(st["asleep"], st["sleep_time"])
         if edits is not None and len(edits):
             o.edit(edits)
         oracles[name] = o
