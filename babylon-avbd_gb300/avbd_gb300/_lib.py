@@ -117,6 +117,13 @@ SIGNATURES = [
     ("avbd_world_sleep_state", C.c_int, [C.c_void_p, _ip, _fp, _ip]),
     ("avbd_world_import_sleep_state", C.c_int, [C.c_void_p, _ip, _fp]),
     ("avbd_batch_sleep_state", C.c_int, [C.c_void_p, C.c_int32, _ip, _fp, _ip]),
+    ("avbd_world_watch_contacts", C.c_int, [C.c_void_p, _up, C.c_int32, C.c_int32, C.c_int32]),
+    ("avbd_world_reset_contact_history", C.c_int, [C.c_void_p, _up, C.c_int32]),
+    ("avbd_world_contact_events", C.c_int, [C.c_void_p, _up, C.c_int64, _i64p, _i64p, _ip]),
+    ("avbd_batch_watch_contacts", C.c_int, [C.c_void_p, C.c_int32, _up, C.c_int32, C.c_int32, C.c_int32]),
+    ("avbd_batch_contact_events", C.c_int, [C.c_void_p, C.c_int32, _up, C.c_int64, _i64p, _i64p, _ip]),
+    ("avbd_server_watch_contacts", C.c_int, [C.c_void_p, C.c_int64, _up, C.c_int32, C.c_int32, C.c_int32]),
+    ("avbd_server_contact_events", C.c_int, [C.c_void_p, C.c_int64, _up, C.c_int64, _i64p, _i64p, _ip]),
     ("avbd_server_sleep_state", C.c_int, [C.c_void_p, C.c_int64, _ip, _fp, _ip]),
 ]
 

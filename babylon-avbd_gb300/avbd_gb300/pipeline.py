@@ -58,6 +58,48 @@ def _sleep_thresholds(opt, p):
     return float(speed), float(time)
 
 
+def _watch_args(options, body_count):
+    """(indices array or None, n, maxPairs, maxEvents) of watchContacts({indices, maxPairs,
+    maxEvents}) (src/native/solver3D.js:256-284)."""
+    options = options or {}
+    max_pairs = options.get("maxPairs", 8192)
+    max_events = options.get("maxEvents", 4096)
+    for v in (max_pairs, max_events):
+        if not isinstance(v, (int, np.integer)) or isinstance(v, bool) or v < 1:
+            raise ValueError("Contact capacities must be positive integers")
+    idx = options.get("indices")
+    if idx is None:
+        return None, 0, int(max_pairs), int(max_events)
+    if not isinstance(idx, (list, tuple, np.ndarray)):
+        raise ValueError("Watched indices must be an array")
+    arr = np.ascontiguousarray(np.asarray(idx, dtype=np.int64))
+    if arr.size and (arr.min() < 0 or arr.max() >= body_count):
+        raise ValueError("A live body index is required")
+    arr = np.ascontiguousarray(arr.astype(np.uint32))
+    return arr, int(arr.size), int(max_pairs), int(max_events)
+
+
+def _read_events(fn, *args) -> dict:
+    """readContactEvents(): {events, dropped, full} with events as the reference reports them
+    (type "begin"/"end", kind, a, b, step, point, normal, impulse, isTrigger)."""
+    raw = _read_events_raw(fn, *args)
+    ev = raw["records"]
+    f = ev.view(np.float32)
+    events = [{"type": "begin" if r[0] == 1 else "end", "kind": int(r[0]), "a": int(r[1]), "b": int(r[2]),
+               "step": int(r[3]), "point": [float(x) for x in f[k, 4:7]], "impulse": float(f[k, 7]),
+               "normal": [float(x) for x in f[k, 8:11]], "isTrigger": False}
+              for k, r in enumerate(ev)]
+    return {"events": events, "dropped": raw["dropped"], "full": raw["full"]}
+
+
+def _read_events_raw(fn, *args) -> dict:
+    n, dropped, full = C.c_int64(), C.c_int64(), C.c_int32()
+    L.check(fn(*args, None, 0, C.byref(n), C.byref(dropped), C.byref(full)))
+    out = np.zeros((n.value, 12), dtype=np.uint32)
+    L.check(fn(*args, L.uptr(out), n.value, C.byref(n), C.byref(dropped), C.byref(full)))
+    return {"records": out[: n.value], "dropped": int(dropped.value), "full": bool(full.value)}
+
+
 def _arrays(scene) -> SceneArrays:
     if isinstance(scene, AvbdScene3D):
         scene.created = True
@@ -449,6 +491,36 @@ class World:
         L.check(L.lib().avbd_world_sleep_state(self._h, L.iptr(a), L.fptr(t), None))
         return a.astype(bool), t
 
+    # contact events (src/native/solver3D.js:256-310) -------------------------
+    def watchContacts(self, options=None):
+        """Turn contact begin/end events on (every body watched) or choose the watched bodies
+        ({indices, maxPairs, maxEvents})."""
+        self._live()
+        idx, n, mp, me = _watch_args(options, self.bodyCount)
+        L.check(L.lib().avbd_world_watch_contacts(self._h, L.uptr(idx), n, mp, me))
+        return self
+
+    def readContactEvents(self) -> dict:
+        self._live()
+        self.watchContacts()
+        return _read_events(L.lib().avbd_world_contact_events, self._h)
+
+    def readContactEventsRaw(self) -> dict:
+        """The events as an (n, 12) uint32 array (floats as bits) plus dropped/full."""
+        self._live()
+        self.watchContacts()
+        return _read_events_raw(L.lib().avbd_world_contact_events, self._h)
+
+    def resetContactHistory(self, indices):
+        self._live()
+        if not isinstance(indices, np.ndarray) or indices.dtype != np.uint32:
+            raise ValueError("Contact resets require Uint32 3D body slots")
+        arr = np.ascontiguousarray(indices)
+        if arr.size and (np.any(np.diff(arr.astype(np.int64)) <= 0) or int(arr.max()) >= self.bodyCount):
+            raise ValueError("Contact reset slots must be unique and ascending")
+        L.check(L.lib().avbd_world_reset_contact_history(self._h, L.uptr(arr), int(arr.size)))
+        return self
+
     def importSleepState(self, asleep, time):
         self._live()
         a = np.ascontiguousarray(asleep, dtype=np.int32)
@@ -508,6 +580,21 @@ class Batch:
         L.check(L.lib().avbd_batch_read_state(self._h, int(world), *(L.fptr(out[k]) for k in
                                                                      ("position", "rotation", "velocity", "angular", "prev_velocity"))))
         return out
+
+    def watchContacts(self, world: int, options=None):
+        if not 0 <= world < self.worldCount:
+            raise ValueError("world index out of range")
+        idx, n, mp, me = _watch_args(options, self.bodyCounts[world])
+        L.check(L.lib().avbd_batch_watch_contacts(self._h, int(world), L.uptr(idx), n, mp, me))
+        return self
+
+    def readContactEventsRaw(self, world: int) -> dict:
+        self.watchContacts(world)
+        return _read_events_raw(L.lib().avbd_batch_contact_events, self._h, int(world))
+
+    def readContactEvents(self, world: int) -> dict:
+        self.watchContacts(world)
+        return _read_events(L.lib().avbd_batch_contact_events, self._h, int(world))
 
     def readSleepState(self, world: int):
         if not 0 <= world < self.worldCount:
@@ -659,6 +746,23 @@ class Server:
         L.check(L.lib().avbd_server_read_state(self._h, int(world), *(L.fptr(out[k]) for k in
                                                                        ("position", "rotation", "velocity", "angular", "prev_velocity"))))
         return out
+
+    def watchContacts(self, world: int, options=None):
+        self._live()
+        n = self._counts.get(int(world))
+        if n is None:
+            raise ValueError(f"no such world {world}")
+        idx, k, mp, me = _watch_args(options, n)
+        L.check(L.lib().avbd_server_watch_contacts(self._h, int(world), L.uptr(idx), k, mp, me))
+        return self
+
+    def readContactEventsRaw(self, world: int) -> dict:
+        self.watchContacts(world)
+        return _read_events_raw(L.lib().avbd_server_contact_events, self._h, int(world))
+
+    def readContactEvents(self, world: int) -> dict:
+        self.watchContacts(world)
+        return _read_events(L.lib().avbd_server_contact_events, self._h, int(world))
 
     def readSleepState(self, world: int):
         self._live()

@@ -1,7 +1,7 @@
 """Build the engine's shared library ``avbd_gb300/libavbd_gb300.so`` for sm_103a.
 
 Each CUDA translation unit is compiled in parallel with nvcc (one ``-gencode``), then linked
-with ``-shared``. The collision, solve, engine and sleep units are compiled with ``-fmad=false`` so their
+with ``-shared``. The collision, solve, engine, sleep and event units are compiled with ``-fmad=false`` so their
 float arithmetic is rounded operation by operation, as the reference's is.
 
 Usage: python babylon-avbd_gb300/build.py [--force]   (AVBD_DEFINES="NAME=VALUE ..." adds -D flags)
@@ -31,6 +31,7 @@ UNITS = {
     "server.cu": [],
     "bvh.cu": [],
     "sleep.cu": ["-fmad=false"],
+    "events.cu": ["-fmad=false"],
 }
 
 

@@ -137,6 +137,7 @@ struct Snapshot {
   std::vector<float> restitution;
   std::vector<int> sleep;
   std::vector<float> sleepTime;
+  std::vector<uint32_t> watch, watchPrev;
   std::vector<int2> jab;
   std::vector<float4> joint[10];  // rA rB stiff penLin penAng lamLin lamAng C0Lin C0Ang restQ
   std::vector<int> jbroken;
@@ -162,6 +163,13 @@ struct WorldRec {
   int bvhOff = 0, bvhRebuild = 16, sinceBuild = 0;
   bool built = false;
   std::vector<uint32_t> edits;  // body command records waiting for the next step (12 words each)
+  long long steps = 0;          // steps taken
+  // contact events (FLAG_EVENTS): device region of evCap events while resident, events already
+  // drained to the host (12 words each), events dropped past the capacity
+  int evCap = 0;
+  float4* evDev = nullptr;
+  std::vector<uint32_t> evHost;
+  long long evDropped = 0;
 };
 
 class Arena {
@@ -177,6 +185,8 @@ class Arena {
   size_t bscKeys = 0, bscHist = 0, bscClusters = 0, bscBounds = 0;
   BounceBufs BB{};  // bounce pass (FLAG_RESTITUTION), see ensureBounce
   SleepBufs SB{};   // island sleeping (FLAG_SLEEP), see ensureSleep
+  EventBufs EV{};   // contact events (FLAG_EVENTS), per world; see watchContacts
+  size_t evWorlds = 0;
   size_t sleepBodies = 0, sleepWorlds = 0;
   size_t bounceBodies = 0, bounceSlots = 0;
   std::vector<int> freeSlots;
@@ -287,6 +297,8 @@ class Arena {
     B.restitution = dalloc<float>(N);
     B.sleep = dalloc<int>(N);
     B.sleepTime = dalloc<float>(N);
+    B.watch = dalloc<uint32_t>(N);
+    B.watchPrev = dalloc<uint32_t>(N);
     J.ab = dalloc<int2>(NJ);
     for (float4** p : {&J.rA, &J.rB, &J.stiff, &J.penLin, &J.penAng, &J.lamLin, &J.lamAng, &J.C0Lin, &J.C0Ang, &J.restQ})
       *p = dalloc<float4>(NJ);
@@ -341,7 +353,8 @@ class Arena {
 
   void release() {
     void* ptrs[] = {B.pose, B.pose0, B.poseY, B.vel, B.ang, B.vprev, B.size, B.mass, B.meta, B.restitution, B.sleep,
-                    B.sleepTime, SB.parent, SB.flags, SB.wake, SB.err, BB.inVel,
+                    B.sleepTime, B.watch, B.watchPrev, EV.region, EV.count, EV.cap, EV.step, SB.parent, SB.flags,
+                    SB.wake, SB.err, BB.inVel,
                     BB.inAng, BB.ra, BB.rb, BB.nk, BB.delta, J.ab, J.rA,
                     J.rB, J.stiff, J.penLin, J.penAng, J.lamLin, J.lamAng, J.C0Lin, J.C0Ang, J.restQ, J.broken, worlds,
                     which, pairN, wover, wactive, active, activeBodies, activeJoints, pairPrefix, pairCount, G.cellCount,
@@ -351,6 +364,7 @@ class Arena {
                     T.adjList, G.bvh.node, G.bvh.parent, G.bvh.escape, G.bvh.minIdx, bsc.keys[0], bsc.keys[1], bsc.hist,
                     bsc.clusters, bsc.bounds, editRec, editRanges, editTele, io};
     for (void* p : ptrs) dfree(p);
+    for (WorldRec& R : W) dfree(R.evDev);
     if (ctrHost) cudaFreeHost(ctrHost);
     if (activeHost) cudaFreeHost(activeHost);
     if (wactiveHost) cudaFreeHost(wactiveHost);
@@ -436,6 +450,8 @@ class Arena {
     regrow(B.restitution, o, N);
     regrow(B.sleep, o, N);
     regrow(B.sleepTime, o, N);
+    regrow(B.watch, o, N);
+    regrow(B.watchPrev, o, N);
     int* c = dalloc<int>(2 * N);  // both colour buffers, stride = capacity
     CK(cudaMemcpyAsync(c, T.color, o * 4, cudaMemcpyDeviceToDevice, s));
     CK(cudaMemcpyAsync(c + N, T.color + o, o * 4, cudaMemcpyDeviceToDevice, s));
@@ -517,14 +533,15 @@ class Arena {
   size_t scratchBytes() const { return itemCap * sizeof(int4); }
   static size_t scratchReserve(long long nb) { return size_t(nb) * 512; }
   size_t footprint(long long nb, long long nj, long long slots, long long nw) const {
-    const size_t perBody = 12 * 16 + 2 * 4 + 1 + 14 * 4 + 32 + 4 * PAIR_TMP;
+    const size_t perBody = 12 * 16 + 2 * 4 + 1 + 16 * 4 + 32 + 4 * PAIR_TMP;
     const size_t perJoint = 8 + 10 * 16 + 4 + 4 + 8;
     const size_t perSlot = 2 * (8 + 4 + 3 * 16 + MAX_CONTACTS * 64) + 16 + 4 * 4 + 8;
     const size_t perWorld = sizeof(WorldDev) + 4 * 4 + 16 + 4 + MAX_LARGE * 4;
     return size_t(nb) * perBody + size_t(tableFor(size_t(nb))) * 8 + size_t(nj) * perJoint + size_t(slots) * perSlot +
            size_t(nw) * perWorld + size_t(ncCap) * 12 + scanBytes + size_t(bvhCap) * (32 + 12) +
            (2 * bscKeys * sizeof(uint2) + bscHist * 4 + bscClusters * 4 + bscBounds * 16) +
-           (bounceBodies * 32 + bounceSlots * 52) + (sleepBodies * 8 + sleepWorlds * 4 + 4);
+           (bounceBodies * 32 + bounceSlots * 52) + (sleepBodies * 8 + sleepWorlds * 4 + 4) + evWorlds * 20 +
+           eventBytes();
   }
   size_t deviceBytes() const { return footprint(bodyCap, jointCap, slotCap, maxWorlds) + scratchBytes(); }
 
@@ -891,6 +908,8 @@ class Arena {
       put(B.sleep + off, sleepBits.data(), n * 4);
       std::vector<float> zeros(n, 0.f);
       put(B.sleepTime + off, zeros.data(), n * 4);
+      put(B.watch + off, zeros.data(), n * 4);
+      put(B.watchPrev + off, zeros.data(), n * 4);
       std::vector<int> minus(n, -1);
       put(T.color + off, minus.data(), n * 4);
       put(T.color + bodyCap + off, minus.data(), n * 4);
@@ -954,6 +973,7 @@ class Arena {
     CK(cudaStreamSynchronize(s));
     WorldRec& R = W[w];
     if (R.resident) freeResident(R);
+    dfree(R.evDev);
     R = WorldRec();
     freeSlots.push_back(w);
     rebuildNoCollide();
@@ -993,6 +1013,11 @@ class Arena {
     getRange(S->restitution, B.restitution, off, n);
     getRange(S->sleep, B.sleep, off, n);
     getRange(S->sleepTime, B.sleepTime, off, n);
+    getRange(S->watch, B.watch, off, n);
+    getRange(S->watchPrev, B.watchPrev, off, n);
+    drainEvents(w);
+    dfree(R.evDev);
+    R.evDev = nullptr;
     getRange(S->jab, J.ab, joff, nj);
     for (auto& ab : S->jab) {
       if (ab.x >= 0) ab.x -= int(off);
@@ -1046,6 +1071,9 @@ class Arena {
     putRange(B.restitution, off, S.restitution);
     putRange(B.sleep, off, S.sleep);
     putRange(B.sleepTime, off, S.sleepTime);
+    putRange(B.watch, off, S.watch);
+    putRange(B.watchPrev, off, S.watchPrev);
+    if (R.dev.flags & FLAG_EVENTS) placeEvents(w);
     for (auto& ab : S.jab) {
       if (ab.x >= 0) ab.x += int(off);
       ab.y += int(off);
@@ -1356,6 +1384,146 @@ class Arena {
     flush();
   }
 
+  // ---------------------------------------------------------------- contact events
+  size_t eventBytes() const {
+    size_t b = 0;
+    for (const WorldRec& R : W)
+      if (R.evDev) b += size_t(R.evCap) * EVENT_FLOAT4 * 16;
+    return b;
+  }
+  // per-world event arrays at the arena's world capacity
+  void ensureEventArrays() {
+    if (evWorlds >= size_t(maxWorlds)) return;
+    const size_t o = evWorlds, nw = size_t(maxWorlds);
+    if (o == 0) {
+      EV.region = dalloc<float4*>(nw);
+      EV.count = dalloc<int>(nw);
+      EV.cap = dalloc<int>(nw);
+      EV.step = dalloc<int>(nw);
+    } else {
+      regrow(EV.region, o, nw);
+      regrow(EV.count, o, nw);
+      regrow(EV.cap, o, nw);
+      regrow(EV.step, o, nw);
+    }
+    evWorlds = nw;
+  }
+  // device region of a resident world with events on; its counters restart
+  void placeEvents(int w) {
+    WorldRec& R = W[w];
+    ensureEventArrays();
+    if (!R.evDev) R.evDev = dalloc<float4>(size_t(R.evCap) * EVENT_FLOAT4);
+    const int zero = 0, step = int(R.steps);
+    put(EV.region + w, &R.evDev, sizeof(float4*));
+    put(EV.count + w, &zero, 4);
+    put(EV.cap + w, &R.evCap, 4);
+    put(EV.step + w, &step, 4);
+  }
+  // watchContacts (src/native/solver3D.js:256-284): the first call turns events on with room for
+  // maxEvents per read and watches every body unless `select`; with `select`, exactly the given
+  // bodies are watched. A newly watched body begins its current contacts at the next step.
+  void watchContacts(int w, const uint32_t* idx, int n, int maxEvents, bool select) {
+    if (w < 0 || w >= maxWorlds || !W[w].live) throw Error(AVBD_E_INVALID, "no such world");
+    if (maxEvents < 1) throw Error(AVBD_E_INVALID, "Contact capacities must be positive integers");
+    WorldRec& R = W[w];
+    for (int k = 0; select && k < n; k++)
+      if (idx[k] >= uint32_t(R.nBodies)) throw Error(AVBD_E_INVALID, "body index out of range");
+    const bool first = !(R.dev.flags & FLAG_EVENTS);
+    if (!first && !select) return;
+    const size_t nb = size_t(R.nBodies);
+    std::vector<uint32_t> words(nb), prev(nb);
+    if (R.resident) {
+      if (nb) get(words.data(), B.watch + R.dev.bodyOff, nb * 4);
+    } else {
+      words = R.snap->watch;
+    }
+    std::vector<char> on(nb, select ? 0 : 1);
+    for (int k = 0; select && k < n; k++) on[idx[k]] = 1;
+    for (size_t i = 0; i < nb; i++) words[i] = (words[i] & ~WATCH_ON) | (on[i] ? WATCH_ON : 0u);
+    if (first) {
+      R.evCap = maxEvents;
+      R.dev.flags |= FLAG_EVENTS;
+      if (R.resident) {
+        placeEvents(w);
+        uploadWorldDev(w);
+      }
+    }
+    if (R.resident) {
+      if (nb) put(B.watch + R.dev.bodyOff, words.data(), nb * 4);
+      if (first && nb) put(B.watchPrev + R.dev.bodyOff, prev.data(), nb * 4);
+      flush();
+    } else {
+      R.snap->watch = words;
+      if (first) R.snap->watchPrev = prev;
+    }
+  }
+  // resetContactHistory (src/vendor/three-avbd-lib/contacts.ts resetBodies): new lifetimes for
+  // the given bodies (ascending, unique): their contacts begin afresh, none of the old ones end.
+  void resetContactHistory(int w, const uint32_t* idx, int n) {
+    if (w < 0 || w >= maxWorlds || !W[w].live) throw Error(AVBD_E_INVALID, "no such world");
+    WorldRec& R = W[w];
+    long long prev = -1;
+    for (int k = 0; k < n; k++) {
+      if ((long long)idx[k] <= prev || idx[k] >= uint32_t(R.nBodies))
+        throw Error(AVBD_E_INVALID, "Contact reset slots must be unique, ascending and in range");
+      prev = idx[k];
+    }
+    if (n == 0) return;
+    const size_t nb = size_t(R.nBodies);
+    std::vector<uint32_t> words(nb);
+    if (R.resident) get(words.data(), B.watch + R.dev.bodyOff, nb * 4);
+    else words = R.snap->watch;
+    for (int k = 0; k < n; k++) words[idx[k]] += 2u;
+    if (R.resident) {
+      put(B.watch + R.dev.bodyOff, words.data(), nb * 4);
+      flush();
+    } else {
+      R.snap->watch = words;
+    }
+  }
+  void drainEvents(int w) {
+    WorldRec& R = W[w];
+    if (!(R.dev.flags & FLAG_EVENTS) || !R.resident || !R.evDev) return;
+    int cnt = 0;
+    get(&cnt, EV.count + w, 4);
+    const int n = std::min(cnt, R.evCap);
+    if (n > 0) {
+      const size_t at = R.evHost.size();
+      R.evHost.resize(at + 12 * size_t(n));
+      get(R.evHost.data() + at, R.evDev, size_t(n) * EVENT_FLOAT4 * 16);
+    }
+    R.evDropped += cnt - n;
+    const int zero = 0;
+    put(EV.count + w, &zero, 4);
+    flush();
+  }
+  // readContactEvents: the events since the last read in step order (within a step: begins then
+  // ends, each by (a, b)), 12 words each: kind, a, b, step, point xyz, impulse, normal xyz, 0.
+  // With out == nullptr or cap too small only the count is returned and nothing is consumed.
+  long long readEvents(int w, uint32_t* out, long long cap, long long* dropped) {
+    if (w < 0 || w >= maxWorlds || !W[w].live) throw Error(AVBD_E_INVALID, "no such world");
+    drainEvents(w);
+    WorldRec& R = W[w];
+    const long long n = (long long)(R.evHost.size() / 12);
+    if (dropped) *dropped = R.evDropped;
+    if (!out || cap < n) return n;
+    std::vector<long long> order(static_cast<size_t>(n));
+    for (long long k = 0; k < n; k++) order[size_t(k)] = k;
+    const uint32_t* e = R.evHost.data();
+    std::stable_sort(order.begin(), order.end(), [&](long long x, long long y) {
+      const uint32_t* a = e + 12 * x;
+      const uint32_t* b = e + 12 * y;
+      if (a[3] != b[3]) return a[3] < b[3];
+      if (a[0] != b[0]) return a[0] < b[0];
+      if (a[1] != b[1]) return a[1] < b[1];
+      return a[2] < b[2];
+    });
+    for (long long k = 0; k < n; k++) std::memcpy(out + 12 * k, e + 12 * order[size_t(k)], 48);
+    R.evHost.clear();
+    R.evDropped = 0;
+    return n;
+  }
+
   void ensureBounce() {
     if (bounceBodies < size_t(bodyCap)) {
       CK(cudaStreamSynchronize(s));
@@ -1503,6 +1671,9 @@ class Arena {
       ensureSleep();
       launch_sleep(B, worlds, J, P, NC, t, ctr, pairBudget, SB, maxWorlds, s);
     }
+    bool events = false;
+    for (int w : act) events |= (W[w].dev.flags & FLAG_EVENTS) != 0;
+    if (events) launch_events(B, worlds, P, t, ctr, pairBudget, EV, s);
     if (prof) span(P_OTHER, v0, mark());
     if (prof) {
       CK(cudaMemsetAsync(traffic, 0, 3 * sizeof(unsigned long long), s));
@@ -1516,7 +1687,10 @@ class Arena {
       profSteps++;
     }
     launch_tick_end(t, s);
-    for (int w : act) W[w].which ^= 1;
+    for (int w : act) {
+      W[w].which ^= 1;
+      W[w].steps++;
+    }
     lastPairs = ctrHost->activePairs;
     lastJoints = nj;
     steps++;

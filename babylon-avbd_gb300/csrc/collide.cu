@@ -833,23 +833,6 @@ __device__ int collide(float4 pA, float4 qA, float4 sA, int shA, float4 pB, floa
 
 // ------------------------------------------------------------------ narrowphase kernel
 
-__device__ __forceinline__ int find_pair(const uint2* __restrict__ pairs, int base, int n, uint2 key) {
-  const unsigned long long k = (unsigned long long)key.x << 32 | key.y;
-  pairs += base;
-  int a = 0, b = n;
-  while (a < b) {
-    int m = (a + b) >> 1;
-    uint2 p = pairs[m];
-    unsigned long long pk = (unsigned long long)p.x << 32 | p.y;
-    if (pk < k) a = m + 1;
-    else b = m;
-  }
-  if (a < n) {
-    uint2 p = pairs[a];
-    if (p.x == key.x && p.y == key.y) return base + a;
-  }
-  return -1;
-}
 
 // Warm start and store the contacts of pair p (cpuPhysics3D.js:108-145): match the previous
 // step's contacts of the same pair by feature, keep sticking anchors (not for rolling pairs),

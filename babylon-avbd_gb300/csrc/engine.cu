@@ -404,6 +404,36 @@ int avbd_world_sleep_state(avbd_world* w, int32_t* asleep, float* quiet_time, in
   API_END
 }
 
+int avbd_world_watch_contacts(avbd_world* w, const uint32_t* indices, int32_t n, int32_t max_pairs, int32_t max_events) {
+  API_BEGIN
+  REQUIRE(w, "null world");
+  REQUIRE(max_pairs >= 1 && max_events >= 1, "Contact capacities must be positive integers");
+  REQUIRE(!indices || n >= 0, "negative count");
+  bind(w->A->ctx);
+  w->A->watchContacts(w->w, indices, n, max_events, indices != nullptr);
+  API_END
+}
+
+int avbd_world_reset_contact_history(avbd_world* w, const uint32_t* indices, int32_t n) {
+  API_BEGIN
+  REQUIRE(w && (n == 0 || indices), "null argument");
+  REQUIRE(n >= 0, "negative count");
+  bind(w->A->ctx);
+  w->A->resetContactHistory(w->w, indices, n);
+  API_END
+}
+
+int avbd_world_contact_events(avbd_world* w, uint32_t* out, int64_t cap, int64_t* n, int64_t* dropped, int32_t* full) {
+  API_BEGIN
+  REQUIRE(w && n, "null argument");
+  bind(w->A->ctx);
+  long long d = 0;
+  *n = w->A->readEvents(w->w, out, cap, &d);
+  if (dropped) *dropped = d;
+  if (full) *full = d > 0;
+  API_END
+}
+
 int avbd_world_import_sleep_state(avbd_world* w, const int32_t* asleep, const float* quiet_time) {
   API_BEGIN
   REQUIRE(w, "null world");
@@ -635,6 +665,31 @@ int avbd_batch_edit(avbd_batch* b, int32_t world, const uint32_t* records, int32
   REQUIRE(world >= 0 && world < int32_t(b->worlds.size()), "world index out of range");
   bind(b->A->ctx);
   b->A->queueEdits(b->worlds[world], records, n);
+  API_END
+}
+
+int avbd_batch_watch_contacts(avbd_batch* b, int32_t world, const uint32_t* indices, int32_t n, int32_t max_pairs,
+                              int32_t max_events) {
+  API_BEGIN
+  REQUIRE(b, "null batch");
+  REQUIRE(world >= 0 && world < int32_t(b->worlds.size()), "world index out of range");
+  REQUIRE(max_pairs >= 1 && max_events >= 1, "Contact capacities must be positive integers");
+  REQUIRE(!indices || n >= 0, "negative count");
+  bind(b->A->ctx);
+  b->A->watchContacts(b->worlds[world], indices, n, max_events, indices != nullptr);
+  API_END
+}
+
+int avbd_batch_contact_events(avbd_batch* b, int32_t world, uint32_t* out, int64_t cap, int64_t* n, int64_t* dropped,
+                              int32_t* full) {
+  API_BEGIN
+  REQUIRE(b && n, "null argument");
+  REQUIRE(world >= 0 && world < int32_t(b->worlds.size()), "world index out of range");
+  bind(b->A->ctx);
+  long long d = 0;
+  *n = b->A->readEvents(b->worlds[world], out, cap, &d);
+  if (dropped) *dropped = d;
+  if (full) *full = d > 0;
   API_END
 }
 

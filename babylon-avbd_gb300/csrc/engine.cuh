@@ -48,6 +48,12 @@ constexpr int FLAG_RESTITUTION = 8;  // some body has restitution > 0: run the b
 constexpr int FLAG_SLEEP = 16;       // island sleeping after each step (sleep.cu)
 constexpr int SLEEP_ASLEEP = 1;      // the body sleeps: the solve leaves it where it is
 constexpr int SLEEP_ALLOW = 2;       // allowSleep (a body without it keeps its island awake)
+constexpr int FLAG_EVENTS = 32;      // contact begin/end events after each step (events.cu)
+// A watch word: bit 0 = the body reports its contacts; the bits above count its lifetimes
+// (resetContactHistory adds 2), so a changed word restarts the body's contact history.
+constexpr uint32_t WATCH_ON = 1u;
+constexpr uint32_t EVENT_BEGIN = 1u, EVENT_END = 2u;
+constexpr int EVENT_FLOAT4 = 3;  // per event: (kind, a, b, step) bits; (point, impulse); (normal, 0)
 
 // Per-world parameters and ranges (96 bytes).
 struct WorldDev {
@@ -71,6 +77,7 @@ struct BodyPtrs {
   float* restitution;  // per body (0 for most)
   int* sleep;          // per body: SLEEP_ASLEEP | SLEEP_ALLOW
   float* sleepTime;    // per body: seconds its island has been quiet (FLAG_SLEEP worlds)
+  uint32_t *watch, *watchPrev;  // per body: contact-event watch word now and at the last event pass
   __host__ __device__ __forceinline__ float4& pos(int i) const { return pose[2 * size_t(i)]; }
   __host__ __device__ __forceinline__ float4& rot(int i) const { return pose[2 * size_t(i) + 1]; }
   __host__ __device__ __forceinline__ float4& pos0(int i) const { return pose0[2 * size_t(i)]; }
@@ -260,6 +267,36 @@ void launch_primal(const BodyPtrs& b, const WorldDev* worlds, JointPtrs j, PairP
 // Joint duals of one iteration (contact duals run inside launch_primal, see k_primal).
 void launch_dual_joints(const BodyPtrs& b, const WorldDev* worlds, JointPtrs j, Tick t, int iteration, cudaStream_t s);
 void launch_velocities(const BodyPtrs& b, const WorldDev* worlds, Tick t, cudaStream_t s);
+// Contact events (FLAG_EVENTS worlds), per world: its event region, events written since the
+// last read (may pass the capacity), the capacity, and the steps it has taken.
+struct EventBufs {
+  float4** region;
+  int* count;
+  int* cap;
+  int* step;
+};
+void launch_events(const BodyPtrs& b, const WorldDev* worlds, PairPtrs P, Tick t, const Counters* ctr, int pairBudget,
+                   EventBufs ev, cudaStream_t s);
+
+// Slot of pair `key` in the sorted region [base, base + n) of a pair buffer, or -1.
+__device__ __forceinline__ int find_pair(const uint2* __restrict__ pairs, int base, int n, uint2 key) {
+  const unsigned long long k = (unsigned long long)key.x << 32 | key.y;
+  pairs += base;
+  int a = 0, b = n;
+  while (a < b) {
+    int m = (a + b) >> 1;
+    uint2 p = pairs[m];
+    unsigned long long pk = (unsigned long long)p.x << 32 | p.y;
+    if (pk < k) a = m + 1;
+    else b = m;
+  }
+  if (a < n) {
+    uint2 p = pairs[a];
+    if (p.x == key.x && p.y == key.y) return base + a;
+  }
+  return -1;
+}
+
 // Restitution (src/native/cpu/restitution.js): per active pair q the bounce state: ra (xyz,
 // target speed), rb (xyz, accumulated impulse), nk (normal, effective mass k; k == 0: inactive),
 // delta (this round's impulse change); incoming velocities per body.

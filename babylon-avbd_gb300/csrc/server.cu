@@ -395,6 +395,31 @@ int avbd_server_edit(avbd_server* s, int64_t world_id, const uint32_t* records, 
   API_END
 }
 
+int avbd_server_watch_contacts(avbd_server* s, int64_t world_id, const uint32_t* indices, int32_t n, int32_t max_pairs,
+                               int32_t max_events) {
+  API_BEGIN
+  REQUIRE(s, "null server");
+  REQUIRE(max_pairs >= 1 && max_events >= 1, "Contact capacities must be positive integers");
+  REQUIRE(!indices || n >= 0, "negative count");
+  bind(s->ctx);
+  const Served& w = s->get(world_id);
+  s->A->watchContacts(w.slot, indices, n, max_events, indices != nullptr);
+  API_END
+}
+
+int avbd_server_contact_events(avbd_server* s, int64_t world_id, uint32_t* out, int64_t cap, int64_t* n, int64_t* dropped,
+                               int32_t* full) {
+  API_BEGIN
+  REQUIRE(s && n, "null argument");
+  bind(s->ctx);
+  const Served& w = s->get(world_id);
+  long long d = 0;
+  *n = s->A->readEvents(w.slot, out, cap, &d);
+  if (dropped) *dropped = d;
+  if (full) *full = d > 0;
+  API_END
+}
+
 int avbd_server_sleep_state(avbd_server* s, int64_t world_id, int32_t* asleep, float* quiet_time, int32_t* n_sleeping) {
   API_BEGIN
   REQUIRE(s, "null server");

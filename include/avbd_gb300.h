@@ -222,6 +222,22 @@ int avbd_world_set_sleeping(avbd_world* w, int32_t enabled, float speed_threshol
 int avbd_world_set_sleep_enabled(avbd_world* w, int32_t body, int32_t enabled);
 int avbd_world_wake_all(avbd_world* w);
 int avbd_world_sleep_state(avbd_world* w, int32_t* asleep, float* quiet_time, int32_t* n_sleeping);
+/* Contact events (src/native/solver3D.js:256-310 watchContacts / readContactEvents /
+ * resetContactHistory; src/vendor/three-avbd-lib/contacts.ts). watch_contacts: the first call turns
+ * events on, with room for max_events events between reads, watching every body when indices is
+ * NULL; with indices, exactly those n bodies are watched. max_pairs is validated (>= 1) but not a
+ * limit here: touching pairs are found in the world's own sorted pair lists, not a bounded set.
+ * contact_events: the events since the last read, 12 words each: kind (1 begin, 2 end), body a,
+ * body b (world-local, a > b), step (1-based count of the world's steps), point xyz, impulse
+ * (|sum of normal lambda| x dt), normal xyz (from b to a), 0 -- floats as bits; in step order,
+ * within a step begins then ends, each by (a, b). With out NULL or cap < *n only *n is set and
+ * nothing is consumed. dropped = events past the capacity since the last read; full = dropped > 0.
+ * reset_contact_history: new lifetimes for the bodies (ascending, unique): their contacts begin
+ * afresh at the next step and none of the old ones end. */
+int avbd_world_watch_contacts(avbd_world* w, const uint32_t* indices, int32_t n, int32_t max_pairs, int32_t max_events);
+int avbd_world_reset_contact_history(avbd_world* w, const uint32_t* indices, int32_t n);
+int avbd_world_contact_events(avbd_world* w, uint32_t* out, int64_t cap, int64_t* n, int64_t* dropped, int32_t* full);
+
 /* Load per-body sleep flags and quiet times (state import for one-step comparisons; NULL skips). */
 int avbd_world_import_sleep_state(avbd_world* w, const int32_t* asleep, const float* quiet_time);
 
@@ -247,6 +263,11 @@ int avbd_batch_read_poses(avbd_batch* b, float* out);
 int avbd_batch_set_velocities(avbd_batch* b, const uint32_t* indices, int32_t n, const float* velocity, const float* angular);
 /* Body commands (as avbd_world_edit) for world `world` of the batch (world-local body indices). */
 int avbd_batch_edit(avbd_batch* b, int32_t world, const uint32_t* records, int32_t n);
+/* Contact events of world `world` of the batch (as avbd_world_watch_contacts / _contact_events). */
+int avbd_batch_watch_contacts(avbd_batch* b, int32_t world, const uint32_t* indices, int32_t n, int32_t max_pairs,
+                              int32_t max_events);
+int avbd_batch_contact_events(avbd_batch* b, int32_t world, uint32_t* out, int64_t cap, int64_t* n, int64_t* dropped,
+                              int32_t* full);
 /* Sleep state of world `world` of the batch (as avbd_world_sleep_state). */
 int avbd_batch_sleep_state(avbd_batch* b, int32_t world, int32_t* asleep, float* quiet_time, int32_t* n_sleeping);
 
@@ -304,6 +325,12 @@ int avbd_server_world_info(avbd_server* s, int64_t world_id, int32_t* n_bodies, 
                            int32_t* resident);
 /* Body commands (as avbd_world_edit), applied before the world's next step. */
 int avbd_server_edit(avbd_server* s, int64_t world_id, const uint32_t* records, int32_t n);
+/* Contact events of a served world (as avbd_world_watch_contacts / _contact_events); events of an
+ * evicted world wait on the host. */
+int avbd_server_watch_contacts(avbd_server* s, int64_t world_id, const uint32_t* indices, int32_t n, int32_t max_pairs,
+                               int32_t max_events);
+int avbd_server_contact_events(avbd_server* s, int64_t world_id, uint32_t* out, int64_t cap, int64_t* n, int64_t* dropped,
+                               int32_t* full);
 /* Sleep state of a served world, resident or evicted (as avbd_world_sleep_state). */
 int avbd_server_sleep_state(avbd_server* s, int64_t world_id, int32_t* asleep, float* quiet_time, int32_t* n_sleeping);
 /* Evict a world now (its queued steps wait for a restore). */
