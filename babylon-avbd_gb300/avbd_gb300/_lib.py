@@ -37,6 +37,11 @@ class SceneDesc(C.Structure):
                 ("allow_sleep", _ip)]
 
 
+class CastFilter(C.Structure):
+    _fields_ = [("collides_with", C.c_uint32), ("membership", C.c_uint32), ("has_membership", C.c_int32),
+                ("include_triggers", C.c_int32), ("n_ignore", C.c_int32), ("ignore", C.c_uint32 * 16)]
+
+
 class Counters(C.Structure):
     _fields_ = [("pairs", C.c_int64), ("manifolds", C.c_int64), ("contacts", C.c_int64),
                 ("joints", C.c_int64), ("colors", C.c_int32), ("conflicts", C.c_int32),
@@ -118,6 +123,9 @@ SIGNATURES = [
     ("avbd_world_import_sleep_state", C.c_int, [C.c_void_p, _ip, _fp]),
     ("avbd_batch_sleep_state", C.c_int, [C.c_void_p, C.c_int32, _ip, _fp, _ip]),
     ("avbd_world_watch_contacts", C.c_int, [C.c_void_p, _up, C.c_int32, C.c_int32, C.c_int32]),
+    ("avbd_world_cast", C.c_int, [C.c_void_p, _fp, C.c_int32, C.c_void_p, _fp]),
+    ("avbd_batch_cast", C.c_int, [C.c_void_p, C.c_int32, _fp, C.c_int32, C.c_void_p, _fp]),
+    ("avbd_server_cast", C.c_int, [C.c_void_p, C.c_int64, _fp, C.c_int32, C.c_void_p, _fp]),
     ("avbd_world_reset_contact_history", C.c_int, [C.c_void_p, _up, C.c_int32]),
     ("avbd_world_contact_events", C.c_int, [C.c_void_p, _up, C.c_int64, _i64p, _i64p, _ip]),
     ("avbd_batch_watch_contacts", C.c_int, [C.c_void_p, C.c_int32, _up, C.c_int32, C.c_int32, C.c_int32]),

@@ -100,6 +100,70 @@ def _read_events_raw(fn, *args) -> dict:
     return {"records": out[: n.value], "dropped": int(dropped.value), "full": bool(full.value)}
 
 
+def _cast_filter(options, body_count) -> "L.CastFilter":
+    """The body filter of a cast ({ignore, collidesWith, membership, includeTriggers},
+    src/gpu/shapeQueries.js:97-135)."""
+    options = options or {}
+    cw = options.get("collidesWith", 0xFFFFFFFF)
+    if not isinstance(cw, (int, np.integer)) or isinstance(cw, bool) or not 0 <= cw <= 0xFFFFFFFF:
+        raise ValueError("Query mask must be an unsigned 32-bit integer")
+    it = options.get("includeTriggers", True)
+    if not isinstance(it, bool):
+        raise ValueError("includeTriggers must be boolean")
+    mem = options.get("membership")
+    if mem is not None and (not isinstance(mem, (int, np.integer)) or isinstance(mem, bool) or not 0 <= mem <= 0xFFFFFFFF):
+        raise ValueError("Query membership must be an unsigned 32-bit integer")
+    ign = list(options.get("ignore", []))
+    if len(ign) > 16 or any(not isinstance(i, (int, np.integer)) or not 0 <= i < body_count for i in ign):
+        raise ValueError("Queries can ignore up to 16 live body indices")
+    f = L.CastFilter()
+    f.collides_with = int(cw)
+    f.membership = 0 if mem is None else int(mem)
+    f.has_membership = 0 if mem is None else 1
+    f.include_triggers = int(it)
+    f.n_ignore = len(ign)
+    for k, i in enumerate(ign):
+        f.ignore[k] = int(i)
+    return f
+
+
+def _cast(fn, args, casts, options, body_count):
+    """sphereCastAll: [{origin, direction, radius?, maxDistance?}] -> [hit or None]; a hit is
+    {index, distance, normal, center, point}."""
+    options = options or {}
+    q = np.zeros((len(casts), 8), dtype=np.float32)
+    dirs = []
+    for k, c in enumerate(casts):
+        o = np.asarray(c["origin"], dtype=np.float64)
+        d = np.asarray(c["direction"], dtype=np.float64)
+        r = c.get("radius", 0.0) or 0.0
+        md = c.get("maxDistance", options.get("maxDistance", 3e38))
+        if o.shape != (3,) or d.shape != (3,) or not np.all(np.isfinite(o)) or not np.all(np.isfinite(d)) \
+                or not np.linalg.norm(d):
+            raise ValueError("A query requires 3 finite components and a nonzero direction")
+        if not np.isfinite(r) or r < 0 or not np.isfinite(md) or md < 0:
+            raise ValueError("Query radius and maximum distance must be finite and nonnegative")
+        q[k] = [*o, md, *d, r]
+        dirs.append((o, d / np.linalg.norm(d), float(r)))
+    if not len(casts):
+        return []
+    f = _cast_filter(options, body_count)
+    hits = np.zeros((len(casts), 8), dtype=np.float32)
+    L.check(fn(*args, L.fptr(q), len(casts), C.byref(f), L.fptr(hits)))
+    idx = hits.view(np.uint32)[:, 4]
+    out = []
+    for k, (o, d, r) in enumerate(dirs):
+        t = float(hits[k, 3])
+        if t < 0:
+            out.append(None)
+            continue
+        n = hits[k, :3].astype(np.float64)
+        center = o + t * d
+        out.append({"index": int(idx[k]), "distance": t, "normal": n.tolist(), "center": center.tolist(),
+                    "point": (center - r * n).tolist()})
+    return out
+
+
 def _arrays(scene) -> SceneArrays:
     if isinstance(scene, AvbdScene3D):
         scene.created = True
@@ -491,6 +555,20 @@ class World:
         L.check(L.lib().avbd_world_sleep_state(self._h, L.iptr(a), L.fptr(t), None))
         return a.astype(bool), t
 
+    # shape casts (src/native/solver3D.js:244-251) ----------------------------
+    def raycast(self, origin, direction, options=None):
+        return self.sphereCast(origin, 0.0, direction, options)
+
+    def sphereCast(self, origin, radius, direction, options=None):
+        return self.sphereCastAll([{"origin": origin, "radius": radius, "direction": direction}], options)[0]
+
+    def raycastAll(self, rays, options=None):
+        return self.sphereCastAll([{**r, "radius": 0.0} for r in rays], options)
+
+    def sphereCastAll(self, casts, options=None):
+        self._live()
+        return _cast(L.lib().avbd_world_cast, (self._h,), casts, options, self.bodyCount)
+
     # contact events (src/native/solver3D.js:256-310) -------------------------
     def watchContacts(self, options=None):
         """Turn contact begin/end events on (every body watched) or choose the watched bodies
@@ -580,6 +658,11 @@ class Batch:
         L.check(L.lib().avbd_batch_read_state(self._h, int(world), *(L.fptr(out[k]) for k in
                                                                      ("position", "rotation", "velocity", "angular", "prev_velocity"))))
         return out
+
+    def sphereCastAll(self, world: int, casts, options=None):
+        if not 0 <= world < self.worldCount:
+            raise ValueError("world index out of range")
+        return _cast(L.lib().avbd_batch_cast, (self._h, int(world)), casts, options, self.bodyCounts[world])
 
     def watchContacts(self, world: int, options=None):
         if not 0 <= world < self.worldCount:
@@ -746,6 +829,13 @@ class Server:
         L.check(L.lib().avbd_server_read_state(self._h, int(world), *(L.fptr(out[k]) for k in
                                                                        ("position", "rotation", "velocity", "angular", "prev_velocity"))))
         return out
+
+    def sphereCastAll(self, world: int, casts, options=None):
+        self._live()
+        n = self._counts.get(int(world))
+        if n is None:
+            raise ValueError(f"no such world {world}")
+        return _cast(L.lib().avbd_server_cast, (self._h, int(world)), casts, options, n)
 
     def watchContacts(self, world: int, options=None):
         self._live()

@@ -32,6 +32,7 @@ UNITS = {
     "bvh.cu": [],
     "sleep.cu": ["-fmad=false"],
     "events.cu": ["-fmad=false"],
+    "queries.cu": [],
 }
 
 

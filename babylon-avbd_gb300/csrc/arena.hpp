@@ -1524,6 +1524,48 @@ class Arena {
     return n;
   }
 
+  // ---------------------------------------------------------------- shape casts
+  // raycastAll / sphereCastAll against world w's current poses; queued commands apply first
+  // (src/native/solver3D.js:244-251). queries: 8 floats each (origin, max distance, direction,
+  // radius); hits: 8 floats each (normal, distance or -1, body index as bits, 0, 0, 0).
+  void cast(int w, const float* queries, int n, const avbd_cast_filter& filt, float* hits) {
+    if (w < 0 || w >= maxWorlds || !W[w].live) throw Error(AVBD_E_INVALID, "no such world");
+    if (n < 0) throw Error(AVBD_E_INVALID, "negative count");
+    if (filt.n_ignore < 0 || filt.n_ignore > 16) throw Error(AVBD_E_INVALID, "Queries can ignore up to 16 live body indices");
+    const WorldRec& R0 = W[w];
+    for (int k = 0; k < filt.n_ignore; k++)
+      if (filt.ignore[k] >= uint32_t(R0.nBodies)) throw Error(AVBD_E_INVALID, "Queries can ignore up to 16 live body indices");
+    std::vector<CastQuery> qs(static_cast<size_t>(n));
+    for (int k = 0; k < n; k++) {
+      const float* q = queries + 8 * size_t(k);
+      for (int j = 0; j < 8; j++)
+        if (!std::isfinite(q[j])) throw Error(AVBD_E_INVALID, "A query requires finite components and a nonzero direction");
+      const double len = std::sqrt(double(q[4]) * q[4] + double(q[5]) * q[5] + double(q[6]) * q[6]);
+      if (!(len > 0)) throw Error(AVBD_E_INVALID, "A query requires finite components and a nonzero direction");
+      if (q[7] < 0.f || q[3] < 0.f) throw Error(AVBD_E_INVALID, "Query radius and maximum distance must be finite and nonnegative");
+      qs[k].o = make_float4(q[0], q[1], q[2], q[3]);
+      qs[k].d = make_float4(float(q[4] / len), float(q[5] / len), float(q[6] / len), q[7]);
+    }
+    if (n == 0) return;
+    flushEdits(w);
+    const WorldRec& R = resident(w);
+    CastFilter f{};
+    f.collidesWith = filt.collides_with;
+    f.membership = filt.membership;
+    f.hasMembership = filt.has_membership != 0;
+    f.nIgnore = filt.n_ignore;
+    for (int k = 0; k < filt.n_ignore; k++) f.ignore[k] = filt.ignore[k];
+    const size_t qb = align256(size_t(n) * sizeof(CastQuery)), bb = align256(size_t(n) * 8);
+    char* io = ioBuffer(qb + bb + size_t(n) * 32);
+    CastQuery* dq = reinterpret_cast<CastQuery*>(io);
+    unsigned long long* best = reinterpret_cast<unsigned long long*>(io + qb);
+    float4* out = reinterpret_cast<float4*>(io + qb + bb);
+    put(dq, qs.data(), size_t(n) * sizeof(CastQuery));
+    launch_cast(B, R.dev.bodyOff, R.nBodies, dq, n, f, best, out, s);
+    CK(cudaGetLastError());
+    get(hits, out, size_t(n) * 32);
+  }
+
   void ensureBounce() {
     if (bounceBodies < size_t(bodyCap)) {
       CK(cudaStreamSynchronize(s));

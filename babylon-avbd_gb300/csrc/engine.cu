@@ -434,6 +434,15 @@ int avbd_world_contact_events(avbd_world* w, uint32_t* out, int64_t cap, int64_t
   API_END
 }
 
+int avbd_world_cast(avbd_world* w, const float* queries, int32_t n, const avbd_cast_filter* filter, float* hits) {
+  API_BEGIN
+  REQUIRE(w && (n == 0 || (queries && hits)), "null argument");
+  bind(w->A->ctx);
+  avbd_cast_filter all{0xffffffffu, 0u, 0, 1, 0, {0}};
+  w->A->cast(w->w, queries, n, filter ? *filter : all, hits);
+  API_END
+}
+
 int avbd_world_import_sleep_state(avbd_world* w, const int32_t* asleep, const float* quiet_time) {
   API_BEGIN
   REQUIRE(w, "null world");
@@ -690,6 +699,17 @@ int avbd_batch_contact_events(avbd_batch* b, int32_t world, uint32_t* out, int64
   *n = b->A->readEvents(b->worlds[world], out, cap, &d);
   if (dropped) *dropped = d;
   if (full) *full = d > 0;
+  API_END
+}
+
+int avbd_batch_cast(avbd_batch* b, int32_t world, const float* queries, int32_t n, const avbd_cast_filter* filter,
+                    float* hits) {
+  API_BEGIN
+  REQUIRE(b && (n == 0 || (queries && hits)), "null argument");
+  REQUIRE(world >= 0 && world < int32_t(b->worlds.size()), "world index out of range");
+  bind(b->A->ctx);
+  avbd_cast_filter all{0xffffffffu, 0u, 0, 1, 0, {0}};
+  b->A->cast(b->worlds[world], queries, n, filter ? *filter : all, hits);
   API_END
 }
 

@@ -278,6 +278,21 @@ struct EventBufs {
 void launch_events(const BodyPtrs& b, const WorldDev* worlds, PairPtrs P, Tick t, const Counters* ctr, int pairBudget,
                    EventBufs ev, cudaStream_t s);
 
+// Shape casts (queries.cu): per query origin.xyz + maximum distance, unit direction.xyz +
+// radius (0: a ray); the body filter of the query.
+struct CastQuery {
+  float4 o, d;
+};
+struct CastFilter {
+  uint32_t collidesWith, membership;
+  int hasMembership, nIgnore;
+  uint32_t ignore[16];
+};
+// nearest hit of each query among bodies [off, off + nb): out[2q] = (normal, distance or -1),
+// out[2q + 1].x = body (local index, as bits); best: n 64-bit scratch words
+void launch_cast(const BodyPtrs& b, int off, int nb, const CastQuery* qs, int n, const CastFilter& f,
+                 unsigned long long* best, float4* out, cudaStream_t s);
+
 // Slot of pair `key` in the sorted region [base, base + n) of a pair buffer, or -1.
 __device__ __forceinline__ int find_pair(const uint2* __restrict__ pairs, int base, int n, uint2 key) {
   const unsigned long long k = (unsigned long long)key.x << 32 | key.y;

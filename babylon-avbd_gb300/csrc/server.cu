@@ -420,6 +420,18 @@ int avbd_server_contact_events(avbd_server* s, int64_t world_id, uint32_t* out, 
   API_END
 }
 
+int avbd_server_cast(avbd_server* s, int64_t world_id, const float* queries, int32_t n, const avbd_cast_filter* filter,
+                     float* hits) {
+  API_BEGIN
+  REQUIRE(s && (n == 0 || (queries && hits)), "null argument");
+  bind(s->ctx);
+  const Served& w = s->get(world_id);
+  REQUIRE(s->A->W[w.slot].resident, "world is evicted: advance it before casting");
+  avbd_cast_filter all{0xffffffffu, 0u, 0, 1, 0, {0}};
+  s->A->cast(w.slot, queries, n, filter ? *filter : all, hits);
+  API_END
+}
+
 int avbd_server_sleep_state(avbd_server* s, int64_t world_id, int32_t* asleep, float* quiet_time, int32_t* n_sleeping) {
   API_BEGIN
   REQUIRE(s, "null server");

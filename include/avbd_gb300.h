@@ -238,6 +238,23 @@ int avbd_world_watch_contacts(avbd_world* w, const uint32_t* indices, int32_t n,
 int avbd_world_reset_contact_history(avbd_world* w, const uint32_t* indices, int32_t n);
 int avbd_world_contact_events(avbd_world* w, uint32_t* out, int64_t cap, int64_t* n, int64_t* dropped, int32_t* full);
 
+/* Shape casts: raycastAll / sphereCastAll (src/native/solver3D.js:244-251, the GPU backend's
+ * src/gpu/shapeQueries.js cast): the nearest body each ray (radius 0) or swept sphere hits, against
+ * the current poses after queued commands apply. queries: n x 8 floats (origin xyz, max distance,
+ * direction xyz (any nonzero length), radius); hits: n x 8 floats (normal xyz, distance (-1: no
+ * hit), body index (uint32 bits), 0, 0, 0). Ties in distance go to the lowest body index. The
+ * center of the hit sphere is origin + distance x unit direction, the touching point center -
+ * radius x normal. filter NULL: every body. */
+typedef struct avbd_cast_filter {
+  uint32_t collides_with;   /* bodies whose group & collides_with != 0 [0xffffffff] */
+  uint32_t membership;      /* with has_membership: bodies whose collidesWith & membership != 0 */
+  int32_t has_membership;
+  int32_t include_triggers; /* accepted for the interface; this engine has no trigger bodies */
+  int32_t n_ignore;         /* <= 16 body indices skipped */
+  uint32_t ignore[16];
+} avbd_cast_filter;
+int avbd_world_cast(avbd_world* w, const float* queries, int32_t n, const avbd_cast_filter* filter, float* hits);
+
 /* Load per-body sleep flags and quiet times (state import for one-step comparisons; NULL skips). */
 int avbd_world_import_sleep_state(avbd_world* w, const int32_t* asleep, const float* quiet_time);
 
@@ -263,6 +280,9 @@ int avbd_batch_read_poses(avbd_batch* b, float* out);
 int avbd_batch_set_velocities(avbd_batch* b, const uint32_t* indices, int32_t n, const float* velocity, const float* angular);
 /* Body commands (as avbd_world_edit) for world `world` of the batch (world-local body indices). */
 int avbd_batch_edit(avbd_batch* b, int32_t world, const uint32_t* records, int32_t n);
+/* Shape casts against world `world` of the batch (as avbd_world_cast). */
+int avbd_batch_cast(avbd_batch* b, int32_t world, const float* queries, int32_t n, const avbd_cast_filter* filter,
+                    float* hits);
 /* Contact events of world `world` of the batch (as avbd_world_watch_contacts / _contact_events). */
 int avbd_batch_watch_contacts(avbd_batch* b, int32_t world, const uint32_t* indices, int32_t n, int32_t max_pairs,
                               int32_t max_events);
@@ -325,6 +345,9 @@ int avbd_server_world_info(avbd_server* s, int64_t world_id, int32_t* n_bodies, 
                            int32_t* resident);
 /* Body commands (as avbd_world_edit), applied before the world's next step. */
 int avbd_server_edit(avbd_server* s, int64_t world_id, const uint32_t* records, int32_t n);
+/* Shape casts against a resident served world (as avbd_world_cast). */
+int avbd_server_cast(avbd_server* s, int64_t world_id, const float* queries, int32_t n, const avbd_cast_filter* filter,
+                     float* hits);
 /* Contact events of a served world (as avbd_world_watch_contacts / _contact_events); events of an
  * evicted world wait on the host. */
 int avbd_server_watch_contacts(avbd_server* s, int64_t world_id, const uint32_t* indices, int32_t n, int32_t max_pairs,
