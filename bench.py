@@ -397,10 +397,10 @@ def run_ours(args, dist):
     value = total_bodies * args.steps / (elapsed_ms / 1000.0)
     # ---------------- roofline of the dominant kernel class
     peak, peak_kind = load_peaks()
-    # the solve class: k_world_solve (one block per world) beside the per-colour k_primal launches,
-    # both with the contact duals fused, plus the joint duals of the per-colour worlds
+    # the solve class: the per-colour k_primal launches with the contact duals fused, plus the
+    # joint duals (k_dual_joints) of every iteration
     classes = {"solve": (prof["ms_primal"] + prof["ms_dual"], prof["bytes_primal"] + prof["bytes_dual"],
-                         "k_world_solve + k_primal (primal and dual of every iteration)"),
+                         "k_primal + k_dual_joints (primal and dual of every iteration)"),
                "collide": (prof["ms_collide"], prof["bytes_collide"], "collision kernels")}
     dom = max(classes, key=lambda k: classes[k][0])
     ms, byts, kname = classes[dom]
