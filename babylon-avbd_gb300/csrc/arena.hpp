@@ -1683,12 +1683,14 @@ class Arena {
     launch_body_warmstart(B, worlds, t, s);
     if (prof) span(P_OTHER, o0, mark());
     const int ncolors = ctrHost->ncolors;
+    bool sleepy = false;
+    for (int w : act) sleepy |= (W[w].dev.flags & FLAG_SLEEP) != 0;
     for (int it = 0; it < maxIter; it++) {
       for (int c = 0; c < ncolors; c++) {
         const int cnt = ctrHost->colorCount[c];
         if (!cnt) continue;
         cudaEvent_t a = prof ? mark() : nullptr;
-        launch_primal(B, worlds, J, P, t, T, ctr, c, it, cnt, ctrHost->colorItems[c], s);
+        launch_primal(B, worlds, J, P, t, T, ctr, c, it, cnt, ctrHost->colorItems[c], sleepy, s);
         if (prof) {
           span(P_PRIMAL, a, mark());
           profPrimalLaunches += 1;

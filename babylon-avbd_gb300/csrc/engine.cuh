@@ -262,8 +262,9 @@ __host__ __device__ __forceinline__ int item_contact(int code) { return code & 7
 __host__ __device__ __forceinline__ int item_side(int code) { return (code >> 3) & 1; }
 __host__ __device__ __forceinline__ bool item_dual_owner(int code) { return (code & 16) != 0; }
 __host__ __device__ __forceinline__ int item_iterations(int code) { return code >> 5; }
+// sleepy: some stepped world has sleeping on (rows of sleeping bodies are skipped: nobody reads them)
 void launch_primal(const BodyPtrs& b, const WorldDev* worlds, JointPtrs j, PairPtrs P, Tick t, Topo topo, const Counters* ctr,
-                   int color, int iteration, int nBodiesColor, int nItemsColor, cudaStream_t s);
+                   int color, int iteration, int nBodiesColor, int nItemsColor, bool sleepy, cudaStream_t s);
 // Joint duals of one iteration (contact duals run inside launch_primal, see k_primal).
 void launch_dual_joints(const BodyPtrs& b, const WorldDev* worlds, JointPtrs j, Tick t, int iteration, cudaStream_t s);
 void launch_velocities(const BodyPtrs& b, const WorldDev* worlds, Tick t, cudaStream_t s);

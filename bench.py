@@ -62,6 +62,8 @@ def args_parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-plain", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--sleeping", action="store_true",
+                   help="world_mix with island sleeping on (a different workload: settled piles sleep)")
     return p.parse_args()
 
 
@@ -179,6 +181,11 @@ def build_worlds(args, rank):
            "count_median": 256, "count_clip": [16, 8192], "lognormal_sigma": round(float(sigma), 4),
            "seed": seed, "iterations": 10, "dt": "1/60", "shapes": "70% boxes, 30% spheres",
            "l2": "inputs larger than L2 (no flush needed)"}
+    if getattr(args, "sleeping", False):
+        for w in worlds:
+            w.params.sleeping = True
+        cfg["workload"] += "_sleeping"
+        cfg["sleeping"] = {"speedThreshold": 0.08, "timeThreshold": 0.6}
     return worlds, cfg
 
 
