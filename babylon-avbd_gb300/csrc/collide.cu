@@ -940,7 +940,10 @@ __global__ void __launch_bounds__(256) k_np_classify(BodyPtrs bd, const WorldDev
 }
 
 // Pass 2a: contacts of box-box pairs that SAT found overlapping.
-__global__ void __launch_bounds__(128) k_np_box(BodyPtrs bd, const WorldDev* __restrict__ worlds, PairPtrs cur, Tick t,
+#ifndef AVBD_NP_BOX_MINB
+#define AVBD_NP_BOX_MINB 5
+#endif
+__global__ void __launch_bounds__(128, AVBD_NP_BOX_MINB) k_np_box(BodyPtrs bd, const WorldDev* __restrict__ worlds, PairPtrs cur, Tick t,
                                                 NarrowScratch ns) {
   const int n = ns.ctr[0];
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
@@ -974,8 +977,11 @@ __global__ void __launch_bounds__(128) k_np_box(BodyPtrs bd, const WorldDev* __r
 
 // Pass 2b: pairs with a sphere (generic support-function SAT, one contact): sphere-box pairs,
 // then sphere-sphere pairs in a lighter instance of the same code.
+#ifndef AVBD_NP_SPHERE_MINB
+#define AVBD_NP_SPHERE_MINB 5  // blocks per SM the register allocation must allow
+#endif
 template <bool BOTH_ROUND>
-__global__ void __launch_bounds__(128) k_np_sphere(BodyPtrs bd, const WorldDev* __restrict__ worlds, PairPtrs cur, Tick t,
+__global__ void __launch_bounds__(128, AVBD_NP_SPHERE_MINB) k_np_sphere(BodyPtrs bd, const WorldDev* __restrict__ worlds, PairPtrs cur, Tick t,
                                                    NarrowScratch ns) {
   const int n = ns.ctr[BOTH_ROUND ? 2 : 1];
   const int* list = BOTH_ROUND ? ns.sphere2List : ns.sphereList;
