@@ -431,6 +431,13 @@ def run_ours(args, dist):
     e2e = None
     log(f"timed region done: {elapsed_ms:.1f} ms")
     if not args.no_e2e:
+        # the same steps of the run as the device-timed region: a fresh batch of the same worlds,
+        # the same warm-up (later steps of a pile carry more contacts and take longer)
+        batch.destroy()
+        batch = pipe.createBatch(worlds)
+        for _ in range(args.warmup):
+            batch.step(1)
+        pipe.synchronize()
         offs = np.cumsum([0] + batch.bodyCounts[:-1])
         # one command per world: kick its last body (world offset + count - 1) upwards
         idx_host = torch.from_numpy((offs + np.array(batch.bodyCounts) - 1).astype(np.int64)).pin_memory()
