@@ -124,6 +124,9 @@ SIGNATURES = [
     ("avbd_batch_sleep_state", C.c_int, [C.c_void_p, C.c_int32, _ip, _fp, _ip]),
     ("avbd_world_watch_contacts", C.c_int, [C.c_void_p, _up, C.c_int32, C.c_int32, C.c_int32]),
     ("avbd_world_cast", C.c_int, [C.c_void_p, _fp, C.c_int32, C.c_void_p, _fp]),
+    ("avbd_world_read_joints", C.c_int, [C.c_void_p, _fp]),
+    ("avbd_world_set_filters", C.c_int, [C.c_void_p, _up, C.c_int32, _up, _up]),
+    ("avbd_batch_read_joints", C.c_int, [C.c_void_p, C.c_int32, _fp]),
     ("avbd_batch_cast", C.c_int, [C.c_void_p, C.c_int32, _fp, C.c_int32, C.c_void_p, _fp]),
     ("avbd_server_cast", C.c_int, [C.c_void_p, C.c_int64, _fp, C.c_int32, C.c_void_p, _fp]),
     ("avbd_world_reset_contact_history", C.c_int, [C.c_void_p, _up, C.c_int32]),

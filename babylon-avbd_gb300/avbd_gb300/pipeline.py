@@ -555,6 +555,40 @@ class World:
         L.check(L.lib().avbd_world_sleep_state(self._h, L.iptr(a), L.fptr(t), None))
         return a.astype(bool), t
 
+    # joints, filters, handles (src/native/scenes.d.ts:350-440) ----------------
+    def readJoints(self) -> np.ndarray:
+        """32 floats per joint or spring in creation order (the reference's joint record)."""
+        self._live()
+        out = np.zeros(self.jointCount * 32, dtype=np.float32)
+        if self.jointCount:
+            L.check(L.lib().avbd_world_read_joints(self._h, L.fptr(out)))
+        return out
+
+    def setFilters(self, indices, groups, collidesWith):
+        self._live()
+        idx = np.asarray(indices, dtype=np.int64).reshape(-1)
+        g = np.asarray(groups, dtype=np.int64).reshape(-1)
+        m = np.asarray(collidesWith, dtype=np.int64).reshape(-1)
+        if not (idx.size == g.size == m.size):
+            raise ValueError("Filter arrays must have matching lengths")
+        if idx.size and (idx.min() < 0 or idx.max() >= self.bodyCount):
+            raise ValueError("A live body index is required")
+        for a in (g, m):
+            if a.size and (a.min() < 0 or a.max() > 0xFFFFFFFF):
+                raise ValueError("Collision masks must be unsigned 32-bit integers")
+        ia, ga, ma = (np.ascontiguousarray(a.astype(np.uint32)) for a in (idx, g, m))
+        L.check(L.lib().avbd_world_set_filters(self._h, L.uptr(ia), int(ia.size), L.uptr(ga), L.uptr(ma)))
+        return self
+
+    def gpuIndex(self, referenceIndex: int) -> int:
+        """Bodies keep their creation index here (no reordering of slots)."""
+        if not 0 <= int(referenceIndex) < self.bodyCount:
+            raise ValueError("A live body index is required")
+        return int(referenceIndex)
+
+    def bodyIndex(self, body) -> int:
+        return self.gpuIndex(body)
+
     # shape casts (src/native/solver3D.js:244-251) ----------------------------
     def raycast(self, origin, direction, options=None):
         return self.sphereCast(origin, 0.0, direction, options)
@@ -641,6 +675,7 @@ class Batch:
         self.worldCount = len(arrays_list)
         self.bodyCounts = [a.n_bodies for a in arrays_list]
         self._dts = [float(a.params.dt) for a in arrays_list]
+        self._jointCounts = [p.n_joints for p in self._packed]
         self.bodyCount = int(sum(self.bodyCounts))
 
     def step(self, steps: int = 1):
@@ -657,6 +692,15 @@ class Batch:
                for k in ("position", "rotation", "velocity", "angular", "prev_velocity")}
         L.check(L.lib().avbd_batch_read_state(self._h, int(world), *(L.fptr(out[k]) for k in
                                                                      ("position", "rotation", "velocity", "angular", "prev_velocity"))))
+        return out
+
+    def readJoints(self, world: int) -> np.ndarray:
+        if not 0 <= world < self.worldCount:
+            raise ValueError("world index out of range")
+        n = self._jointCounts[world]
+        out = np.zeros(n * 32, dtype=np.float32)
+        if n:
+            L.check(L.lib().avbd_batch_read_joints(self._h, int(world), L.fptr(out)))
         return out
 
     def sphereCastAll(self, world: int, casts, options=None):

@@ -354,6 +354,31 @@ class AvbdScene3D:
         return self._b.joint(a, b, _vector(anchorA, 3, "anchorA"), _vector(anchorB, 3, "anchorB"),
                              linearStiffness, angularStiffness, frac)
 
+    def addHinge(self, a, b, anchorA=(0, 0, 0), anchorB=(0, 0, 0), axisA=(0, 1, 0), axisB=(0, 1, 0), span=1.0,
+                 **options):
+        """A hinge as two ball joints span apart along the axis (scenes.js:587-601); returns their
+        constraint indices. Angle limits and motors (angular constraints) are not supported here."""
+        self._editable()
+        self._check(a, b)
+        if any(k in options for k in ("minAngle", "maxAngle", "motor")):
+            raise ValueError("hinge angle limits and motors are not supported by the gb300 backend")
+        if options:
+            raise ValueError(f"unknown hinge option {next(iter(options))}")
+        span = _positive(span, "span")
+
+        def unit(v):
+            v = _vector(v, 3, "axis")
+            ln = math.sqrt(sum(x * x for x in v))
+            if ln < 1e-8:
+                raise ValueError("Angular axis requires three finite, nonzero components")
+            return [x / ln for x in v]
+
+        ua, ub = unit(axisA), unit(axisB)
+        aa, bb = _vector(anchorA, 3, "anchorA"), _vector(anchorB, 3, "anchorB")
+        return tuple(self.addJoint(a, b, [aa[i] + sign * span * 0.5 * ua[i] for i in range(3)],
+                                   [bb[i] + sign * span * 0.5 * ub[i] for i in range(3)])
+                     for sign in (-1, 1))
+
     def addSpring(self, a, b, anchorA=(0, 0, 0), anchorB=(0, 0, 0), stiffness=1000.0, rest=-1.0) -> int:
         self._editable()
         self._check(a, b)

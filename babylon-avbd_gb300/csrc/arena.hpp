@@ -1524,6 +1524,64 @@ class Arena {
     return n;
   }
 
+  // ---------------------------------------------------------------- joints and filters
+  // readJoints (src/vendor/three-avbd-lib/solver3D.ts:1456-1458, record layout
+  // avbd3d/gpu/layout.ts:27-36, infinities as +-3e38 as src/native/cpu/world.js:603-660): 32 floats
+  // per joint or spring in creation order: penalty lin (w: linear stiffness, 0 once broken),
+  // penalty ang (w: angular stiffness, 0 once broken), lambda lin (w: fracture), lambda ang
+  // (w: torque arm), C0 lin, C0 ang, rA (w: spring rest length), rB.
+  void readJoints(int w, float* out) {
+    if (w < 0 || w >= maxWorlds || !W[w].live) throw Error(AVBD_E_INVALID, "no such world");
+    flushEdits(w);
+    const WorldRec& R = resident(w);
+    const size_t nj = size_t(R.nJoints), off = size_t(R.dev.jointOff);
+    if (!nj) return;
+    std::vector<float4> f[10];
+    const float4* src[10] = {J.rA, J.rB, J.stiff, J.penLin, J.penAng, J.lamLin, J.lamAng, J.C0Lin, J.C0Ang, J.restQ};
+    for (int k = 0; k < 9; k++) getRange(f[k], src[k], off, nj);
+    std::vector<int> broken;
+    getRange(broken, J.broken, off, nj);
+    auto fin = [](float x) { return x == INFINITY ? 3e38f : (x == -INFINITY ? -3e38f : x); };
+    for (size_t j = 0; j < nj; j++) {
+      float* o = out + 32 * j;
+      const float4 ra = f[0][j], rb = f[1][j], st = f[2][j];
+      const float4 blocks[6] = {f[3][j], f[4][j], f[5][j], f[6][j], f[7][j], f[8][j]};
+      for (int b = 0; b < 6; b++) {
+        o[4 * b] = blocks[b].x;
+        o[4 * b + 1] = blocks[b].y;
+        o[4 * b + 2] = blocks[b].z;
+        o[4 * b + 3] = 0.f;
+      }
+      o[3] = broken[j] ? 0.f : fin(st.x);
+      o[7] = broken[j] ? 0.f : fin(st.y);
+      o[11] = fin(st.z);
+      o[15] = st.w;
+      o[24] = ra.x; o[25] = ra.y; o[26] = ra.z; o[27] = rb.w;
+      o[28] = rb.x; o[29] = rb.y; o[30] = rb.z; o[31] = 0.f;
+    }
+  }
+
+  // setFilters (src/native/cpu/world.js:327-341): collision group and collidesWith of the given
+  // bodies; the world wakes.
+  void setFilters(int w, const uint32_t* idx, int n, const uint32_t* groups, const uint32_t* masks) {
+    if (w < 0 || w >= maxWorlds || !W[w].live) throw Error(AVBD_E_INVALID, "no such world");
+    if (n < 0) throw Error(AVBD_E_INVALID, "negative count");
+    const WorldRec& R = resident(w);
+    for (int k = 0; k < n; k++)
+      if (idx[k] >= uint32_t(R.nBodies)) throw Error(AVBD_E_INVALID, "body index out of range");
+    if (n == 0) return;
+    const size_t nb = size_t(R.nBodies), off = size_t(R.dev.bodyOff);
+    std::vector<int4> meta;
+    getRange(meta, B.meta, off, nb);
+    for (int k = 0; k < n; k++) {
+      meta[idx[k]].z = int(groups[k]);
+      meta[idx[k]].w = int(masks[k]);
+    }
+    putRange(B.meta, off, meta);
+    flush();
+    wakeWorld(w);
+  }
+
   // ---------------------------------------------------------------- shape casts
   // raycastAll / sphereCastAll against world w's current poses; queued commands apply first
   // (src/native/solver3D.js:244-251). queries: 8 floats each (origin, max distance, direction,

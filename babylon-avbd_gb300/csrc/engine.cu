@@ -434,6 +434,23 @@ int avbd_world_contact_events(avbd_world* w, uint32_t* out, int64_t cap, int64_t
   API_END
 }
 
+int avbd_world_read_joints(avbd_world* w, float* out) {
+  API_BEGIN
+  REQUIRE(w && out, "null argument");
+  bind(w->A->ctx);
+  w->A->readJoints(w->w, out);
+  API_END
+}
+
+int avbd_world_set_filters(avbd_world* w, const uint32_t* indices, int32_t n, const uint32_t* groups,
+                           const uint32_t* collides_with) {
+  API_BEGIN
+  REQUIRE(w && (n == 0 || (indices && groups && collides_with)), "null argument");
+  bind(w->A->ctx);
+  w->A->setFilters(w->w, indices, n, groups, collides_with);
+  API_END
+}
+
 int avbd_world_cast(avbd_world* w, const float* queries, int32_t n, const avbd_cast_filter* filter, float* hits) {
   API_BEGIN
   REQUIRE(w && (n == 0 || (queries && hits)), "null argument");
@@ -699,6 +716,15 @@ int avbd_batch_contact_events(avbd_batch* b, int32_t world, uint32_t* out, int64
   *n = b->A->readEvents(b->worlds[world], out, cap, &d);
   if (dropped) *dropped = d;
   if (full) *full = d > 0;
+  API_END
+}
+
+int avbd_batch_read_joints(avbd_batch* b, int32_t world, float* out) {
+  API_BEGIN
+  REQUIRE(b && out, "null argument");
+  REQUIRE(world >= 0 && world < int32_t(b->worlds.size()), "world index out of range");
+  bind(b->A->ctx);
+  b->A->readJoints(b->worlds[world], out);
   API_END
 }
 

@@ -255,6 +255,17 @@ typedef struct avbd_cast_filter {
 } avbd_cast_filter;
 int avbd_world_cast(avbd_world* w, const float* queries, int32_t n, const avbd_cast_filter* filter, float* hits);
 
+/* readJoints() (src/vendor/three-avbd-lib/solver3D.ts:1456-1458): 32 floats per joint or spring in
+ * creation order, the reference's record (avbd3d/gpu/layout.ts:27-36): penalty lin (w: linear
+ * stiffness, 0 once broken), penalty ang (w: angular stiffness, 0 once broken), lambda lin
+ * (w: fracture threshold), lambda ang (w: torque arm), C0 lin, C0 ang, rA (w: spring rest
+ * length), rB; infinities as +-3e38. Queued commands apply first. */
+int avbd_world_read_joints(avbd_world* w, float* out);
+/* setFilters(indices, groups, collidesWith) (src/native/scenes.d.ts:414-418): new collision
+ * filters for the given bodies; the world wakes. */
+int avbd_world_set_filters(avbd_world* w, const uint32_t* indices, int32_t n, const uint32_t* groups,
+                           const uint32_t* collides_with);
+
 /* Load per-body sleep flags and quiet times (state import for one-step comparisons; NULL skips). */
 int avbd_world_import_sleep_state(avbd_world* w, const int32_t* asleep, const float* quiet_time);
 
@@ -280,6 +291,8 @@ int avbd_batch_read_poses(avbd_batch* b, float* out);
 int avbd_batch_set_velocities(avbd_batch* b, const uint32_t* indices, int32_t n, const float* velocity, const float* angular);
 /* Body commands (as avbd_world_edit) for world `world` of the batch (world-local body indices). */
 int avbd_batch_edit(avbd_batch* b, int32_t world, const uint32_t* records, int32_t n);
+/* Joint records of world `world` of the batch (as avbd_world_read_joints). */
+int avbd_batch_read_joints(avbd_batch* b, int32_t world, float* out);
 /* Shape casts against world `world` of the batch (as avbd_world_cast). */
 int avbd_batch_cast(avbd_batch* b, int32_t world, const float* queries, int32_t n, const avbd_cast_filter* filter,
                     float* hits);

@@ -173,3 +173,20 @@ def test_stage_edits_layout_and_validation():
                 {"body": 0, "restitution": 0.5}):
         with _pt.raises(ValueError):
             stage_edits([bad], 5, 0.5)
+
+
+def test_hinge_is_two_ball_joints_along_the_axis():
+    # scenes.js:587-601: joints at anchor -+ span/2 along each body's axis
+    from avbd_gb300 import AvbdScene3D
+    sc = AvbdScene3D()
+    a = sc.addBox([1, 1, 1], density=0, position=[0, 2, 0])
+    b = sc.addBox([1, 1, 1], position=[0, 3.2, 0])
+    ids = sc.addHinge(a, b, anchorA=[0, 0.6, 0], anchorB=[0, -0.6, 0], axisA=[2, 0, 0], axisB=[1, 0, 0], span=0.8)
+    arr = sc.arrays()
+    assert ids == (0, 1) and list(arr.kind) == [0, 0]
+    assert np.allclose(arr.ra, [[-0.4, 0.6, 0], [0.4, 0.6, 0]]) and np.allclose(arr.rb, [[-0.4, -0.6, 0], [0.4, -0.6, 0]])
+    assert np.isinf(arr.p0).all() and np.all(arr.p1 == 0)
+    with pytest.raises(ValueError):
+        sc.addHinge(a, b, minAngle=-1.0)
+    with pytest.raises(ValueError):
+        sc.addHinge(a, b, axisA=[0, 0, 0])

@@ -1,0 +1,75 @@
+"""The rest of the native world surface (src/native/scenes.d.ts:317-454) through the C ABI:
+readJoints (the reference's 32-float joint record), setFilters (new collision filters take effect
+at the next step, bit-exact against the oracle built with the same filters), and a hinge (two ball
+joints, src/native/scenes.js:587-601) that lets its body turn about the hinge axis only.
+"""
+import numpy as np
+import pytest
+
+import parity
+import ref_scenes
+from avbd_gb300 import AvbdScene3D, createSolverPipeline, workloads
+from avbd_gb300.scene import SolverParams
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def pipe():
+    p = createSolverPipeline("gb300", device=0)
+    yield p
+    p.destroy()
+
+
+def test_read_joints_matches_the_exported_joint_state(pipe):
+    sc = ref_scenes.build(13)  # breakable joints
+    sc.params = SolverParams(dt=1 / 60, gravity=-10.0, up=(0.0, 0.0, 1.0), iterations=10)
+    w = pipe.createSolver(sc)
+    w.step(150)
+    rec = w.readJoints().reshape(-1, 32)
+    st = w.exportState()
+    joints = sc.kind != 2
+    assert rec.shape[0] == int(joints.sum())
+    assert np.array_equal(rec[:, 0:3], st["jpen_lin"]) and np.array_equal(rec[:, 4:7], st["jpen_ang"])
+    assert np.array_equal(rec[:, 8:11], st["jlam_lin"]) and np.array_equal(rec[:, 12:15], st["jlam_ang"])
+    broken = st["jbroken"] != 0
+    assert broken.any() and not broken.all()
+    p0 = np.where(np.isinf(sc.p0[joints]), 3e38, sc.p0[joints]).astype(np.float32)
+    assert np.all(rec[broken, 3] == 0) and np.array_equal(rec[~broken, 3], p0[~broken])
+    assert np.allclose(rec[:, 24:27], sc.ra[joints]) and np.allclose(rec[:, 28:31], sc.rb[joints])
+    w.destroy()
+
+
+def test_set_filters_takes_effect_and_matches_the_oracle(pipe):
+    sc = workloads.mixed_pile(300, seed=41, extent=4.0)
+    w = pipe.createSolver(sc)
+    w.step(40)
+    pairs = w.readPairs()
+    a, b = (int(x) for x in pairs[len(pairs) // 2])  # a touching pair: make them pass through
+    groups = np.array([2, 4], dtype=np.uint32)
+    w.setFilters([a, b], groups, np.array([0xFFFFFFFF & ~4, 0xFFFFFFFF & ~2], dtype=np.uint32))
+    sc2 = workloads.mixed_pile(300, seed=41, extent=4.0)
+    sc2.group[[a, b]] = groups
+    sc2.mask[[a, b]] = [0xFFFFFFFF & ~4, 0xFFFFFFFF & ~2]
+    rep = parity.compare_step(w, sc2, 0)
+    assert rep["pairs_equal"] and rep["contact_counts_equal"] and rep["colors_equal"], rep
+    assert rep["max_err_fp32"] <= parity.TOL, rep
+    assert not any((int(p[0]), int(p[1])) == (a, b) for p in w.readPairs())
+    w.destroy()
+
+
+def test_hinge_turns_about_its_axis_only(pipe):
+    sc = AvbdScene3D(timeStep=1 / 60, iterations=10, gravity=-10)
+    post = sc.addBox([0.2, 0.2, 2.0], density=0, position=[0, 5, 0])
+    door = sc.addBox([0.2, 2.0, 1.0], position=[0, 4, 0])
+    # hinge along z through the post's centre and the door's top edge (jointed bodies do not
+    # collide): the door swings in the x-y plane like a pendulum
+    sc.addHinge(post, door, anchorA=[0, 0, 0], anchorB=[0, 1.0, 0], axisA=[0, 0, 1], axisB=[0, 0, 1], span=0.8)
+    w = pipe.createSolver(sc)
+    w.setVelocities([door], [[2.0, 0.0, 0.0]])
+    for _ in range(60):
+        w.step(1)
+        q = w.readBodyState()["rotation"][door]
+        assert abs(q[0]) < 2e-2 and abs(q[1]) < 2e-2  # rotation about z only
+    assert abs(w.readBodyState()["rotation"][door][2]) > 0.05  # and it did swing
+    w.destroy()
