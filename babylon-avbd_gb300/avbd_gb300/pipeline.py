@@ -40,6 +40,71 @@ def _with_options(arrays: SceneArrays, options) -> SceneArrays:
         p.sleep_speed, p.sleep_time = _sleep_thresholds(options["sleeping"], p)
     out = copy.copy(arrays)
     out.params = p
+    if "spatialSort" in options:
+        if not isinstance(options["spatialSort"], bool):
+            raise ValueError("spatialSort must be a boolean")
+        if options["spatialSort"]:
+            out = spatial_sort(out)
+    return out
+
+
+def morton_order(pos: np.ndarray) -> np.ndarray:
+    """Body indices along a Z-order curve of their positions, 10 bits per axis, ties by index
+    (mortonOrder, src/vendor/three-avbd-lib/solver3D.ts:344-367)."""
+    n = len(pos)
+    if n == 0:
+        return np.zeros(0, dtype=np.int64)
+    lo, hi = pos.min(axis=0), pos.max(axis=0)
+    q = np.minimum(1023, np.floor((pos - lo) / np.maximum(hi - lo, 1e-9) * 1024)).astype(np.int64)
+
+    def spread(v):
+        x = v & 0x3FF
+        x = (x | (x << 16)) & 0x30000FF
+        x = (x | (x << 8)) & 0x300F00F
+        x = (x | (x << 4)) & 0x30C30C3
+        x = (x | (x << 2)) & 0x9249249
+        return x
+
+    code = spread(q[:, 0]) | (spread(q[:, 1]) << 1) | (spread(q[:, 2]) << 2)
+    return np.lexsort((np.arange(n), code))
+
+
+def spatial_sort(arrays: SceneArrays) -> SceneArrays:
+    """The scene with its bodies in Morton order (the reference GPU solver's default body slots,
+    solver3D.ts:564); constraints follow their bodies. ``order[slot]`` is the creation index.
+
+    Static and large bodies (radius above twice the median, at most 64 of them: the engine's
+    large-body rule) keep the first slots in creation order and only the rest are sorted: pairs are
+    enumerated by their higher-index body, so a static ground or a large body in a late slot would
+    enumerate most of its world on one thread."""
+    import copy
+    pos = np.asarray(arrays.pos, dtype=np.float64)
+    n = len(pos)
+    first = np.asarray(arrays.mass) <= 0
+    if n:
+        r = np.sort(np.asarray(arrays.radius, dtype=np.float64))
+        thr = 2.0 * r[n // 2]
+        if np.sum(r > thr) > 64:
+            thr = r[n - 65]
+        first |= np.asarray(arrays.radius) > thr
+    head = np.nonzero(first)[0]
+    rest = np.nonzero(~first)[0]
+    order = np.concatenate([head, rest[morton_order(pos[rest])]]).astype(np.int64)
+    slot = np.empty_like(order)
+    slot[order] = np.arange(len(order))
+    out = copy.copy(arrays)
+    for k in ("pos", "quat", "size", "vel", "angvel", "prev_vel", "mass", "moment", "friction", "radius",
+              "shape", "group", "mask"):
+        setattr(out, k, np.asarray(getattr(arrays, k))[order])
+    for k in ("restitution", "allow_sleep"):
+        v = getattr(arrays, k)
+        setattr(out, k, None if v is None else np.asarray(v)[order])
+    if arrays.n_cons:
+        ca = np.asarray(arrays.ca)
+        out.ca = np.where(ca >= 0, slot[np.maximum(ca, 0)], -1).astype(ca.dtype)
+        out.cb = slot[np.asarray(arrays.cb)].astype(np.asarray(arrays.cb).dtype)
+    base = arrays.order if getattr(arrays, "order", None) is not None else np.arange(len(order))
+    out.order = np.asarray(base)[order]
     return out
 
 
@@ -207,7 +272,7 @@ class SolverPipeline:
         self._live()
         arrays = _arrays(scene)
         if options:
-            unknown = set(options) - {"spatialSort", "broadphase", "bvh", "colorRounds"}
+            unknown = set(options) - {"spatialSort", "broadphase", "bvh", "colorRounds", "sleeping"}
             if unknown:
                 raise ValueError(f"unsupported solver options {sorted(unknown)}")
             arrays = _with_options(arrays, options)
@@ -335,6 +400,12 @@ class World:
         self.bodyCount = arrays.n_bodies
         self.jointCount = self._packed.n_joints
         self.dt = float(arrays.params.dt)
+        # body slots: creation order, or Morton order with spatialSort (order[slot] = creation index)
+        order = getattr(arrays, "order", None)
+        self._slot = None
+        if order is not None:
+            self._slot = np.empty(len(order), dtype=np.int64)
+            self._slot[np.asarray(order)] = np.arange(len(order))
         self.timeAccumulator = 0.0
 
     def _live(self):
@@ -581,10 +652,11 @@ class World:
         return self
 
     def gpuIndex(self, referenceIndex: int) -> int:
-        """Bodies keep their creation index here (no reordering of slots)."""
+        """The slot of the body created as `referenceIndex` (itself unless spatialSort moved it);
+        every other call takes and returns slots, as the reference's GPU world does."""
         if not 0 <= int(referenceIndex) < self.bodyCount:
             raise ValueError("A live body index is required")
-        return int(referenceIndex)
+        return int(referenceIndex) if self._slot is None else int(self._slot[int(referenceIndex)])
 
     def bodyIndex(self, body) -> int:
         return self.gpuIndex(body)

@@ -81,6 +81,7 @@ class SceneArrays:
     params: SolverParams = field(default_factory=SolverParams)
     restitution: np.ndarray | None = None  # per body, 0..1 (None: all zero)
     allow_sleep: np.ndarray | None = None  # per body, bool (None: all may sleep)
+    order: np.ndarray | None = None  # after a spatial sort: creation index of each body slot
 
     def restitution_or_zero(self) -> np.ndarray:
         return self.restitution if self.restitution is not None else np.zeros(self.n_bodies, dtype=np.float64)

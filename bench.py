@@ -62,6 +62,10 @@ def args_parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-plain", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--spatial-sort", choices=["on", "off", "auto"], default="auto",
+                   help="bodies of every world in Morton order (spatialSort, the reference GPU solver's "
+                        "default); auto: on for mixed_1m (uniformly seeded bodies), off for the others "
+                        "(their bodies are created in lattice or grid order already)")
     p.add_argument("--sleeping", action="store_true",
                    help="world_mix with island sleeping on (a different workload: settled piles sleep)")
     return p.parse_args()
@@ -156,6 +160,16 @@ class Clocks:
 
 # ------------------------------------------------------------------ workloads
 def build_worlds(args, rank):
+    worlds, cfg = _build_worlds(args, rank)
+    mode = getattr(args, "spatial_sort", "off")
+    if mode == "on" or (mode == "auto" and args.workload == "mixed_1m"):
+        from avbd_gb300.pipeline import spatial_sort
+        worlds = [spatial_sort(w) for w in worlds]
+        cfg["spatial_sort"] = "Morton order of each world's bodies (spatialSort)"
+    return worlds, cfg
+
+
+def _build_worlds(args, rank):
     from avbd_gb300 import workloads
     if args.workload == "box_pile":
         return [workloads.box_pile_c0()], {"workload": "box_pile_c0", "bodies": 1001, "iterations": 10,

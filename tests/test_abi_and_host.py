@@ -190,3 +190,22 @@ def test_hinge_is_two_ball_joints_along_the_axis():
         sc.addHinge(a, b, minAngle=-1.0)
     with pytest.raises(ValueError):
         sc.addHinge(a, b, axisA=[0, 0, 0])
+
+
+def test_spatial_sort_keeps_statics_first_and_remaps_constraints():
+    import ref_scenes
+    from avbd_gb300.pipeline import morton_order, spatial_sort
+    sc = ref_scenes.build(13)  # boxes, a static ground, breakable joints
+    ss = spatial_sort(sc)
+    n = sc.n_bodies
+    assert sorted(ss.order.tolist()) == list(range(n))
+    assert np.array_equal(ss.pos, sc.pos[ss.order]) and np.array_equal(ss.mass, sc.mass[ss.order])
+    nstatic = int(np.sum(sc.mass <= 0))
+    assert np.all(ss.mass[:nstatic] <= 0) and np.all(ss.mass[nstatic:] > 0)
+    slot = np.empty(n, dtype=np.int64)
+    slot[ss.order] = np.arange(n)
+    ca = np.where(sc.ca >= 0, slot[np.maximum(sc.ca, 0)], -1)
+    assert np.array_equal(ss.ca, ca) and np.array_equal(ss.cb, slot[sc.cb])
+    # the Morton key: 10 bits per axis over the bounds, ties by index
+    pts = np.array([[0.0, 0, 0], [1, 1, 1], [1, 0, 0], [0, 1, 0], [0, 0, 1], [1, 0, 0]])
+    assert morton_order(pts).tolist() == [0, 2, 5, 3, 4, 1]

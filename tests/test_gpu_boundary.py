@@ -73,3 +73,19 @@ def test_hinge_turns_about_its_axis_only(pipe):
         assert abs(q[0]) < 2e-2 and abs(q[1]) < 2e-2  # rotation about z only
     assert abs(w.readBodyState()["rotation"][door][2]) > 0.05  # and it did swing
     w.destroy()
+
+
+def test_spatial_sort_slots_and_parity(pipe):
+    # createSolver(scene, {spatialSort: true}): bodies in Morton-ordered slots (statics first);
+    # every call takes slots and gpuIndex maps creation indices to them
+    sc = workloads.mixed_pile(400, seed=17, extent=5.0)
+    w = pipe.createSolver(sc, {"spatialSort": True})
+    st = w.readBodyState()
+    for ref in (0, 5, 123, 399):
+        assert np.array_equal(st["position"][w.gpuIndex(ref)], sc.pos[ref].astype(np.float32))
+    from avbd_gb300.pipeline import spatial_sort
+    sorted_scene = spatial_sort(sc)
+    rep = parity.compare_step(w, sorted_scene, 30)
+    assert rep["pairs_equal"] and rep["contact_counts_equal"] and rep["colors_equal"], rep
+    assert rep["max_err_fp32"] <= parity.TOL, rep
+    w.destroy()
