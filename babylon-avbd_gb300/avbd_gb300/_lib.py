@@ -126,6 +126,7 @@ SIGNATURES = [
     ("avbd_world_cast", C.c_int, [C.c_void_p, _fp, C.c_int32, C.c_void_p, _fp]),
     ("avbd_world_read_joints", C.c_int, [C.c_void_p, _fp]),
     ("avbd_world_set_filters", C.c_int, [C.c_void_p, _up, C.c_int32, _up, _up]),
+    ("avbd_world_set_restitution", C.c_int, [C.c_void_p, _up, C.c_int32, _fp]),
     ("avbd_batch_read_joints", C.c_int, [C.c_void_p, C.c_int32, _fp]),
     ("avbd_batch_cast", C.c_int, [C.c_void_p, C.c_int32, _fp, C.c_int32, C.c_void_p, _fp]),
     ("avbd_server_cast", C.c_int, [C.c_void_p, C.c_int64, _fp, C.c_int32, C.c_void_p, _fp]),

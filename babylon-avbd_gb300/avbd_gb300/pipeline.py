@@ -15,7 +15,7 @@ import math
 import numpy as np
 
 from . import _lib as L
-from .scene import AvbdScene3D, SceneArrays
+from .scene import AvbdScene3D, SceneArrays, _mask
 
 
 def _with_options(arrays: SceneArrays, options) -> SceneArrays:
@@ -334,12 +334,42 @@ def _components(value, count, name):
     return a
 
 
-def stage_edits(edits, body_count: int, dt: float) -> np.ndarray:
+def stage_properties(edits, body_count: int) -> list:
+    """The property part of ``editBodies`` (``src/native/runtime.js:72-103``): per edit with any
+    of restitution / group / collidesWith / allowSleep, validated, in edit order."""
+    out = []
+    for edit in edits:
+        keys = {"isTrigger", "restitution", "group", "collidesWith", "allowSleep"} & set(edit)
+        if not keys:
+            continue
+        index = edit.get("body")
+        if not isinstance(index, (int, np.integer)) or not 0 <= int(index) < body_count:
+            raise ValueError("A live body index is required")
+        if "isTrigger" in edit:
+            raise ValueError("triggers are not supported by the gb300 backend")
+        if "allowSleep" in edit and not isinstance(edit["allowSleep"], bool):
+            raise ValueError("allowSleep must be a boolean")
+        e = edit.get("restitution")
+        if e is not None and (not isinstance(e, (int, float)) or not np.isfinite(e) or not 0 <= e <= 1):
+            raise ValueError("restitution must be between 0 and 1")
+        if "collidesWith" in edit and "group" not in edit:
+            raise ValueError("A collision-mask edit requires group as well")
+        for k in ("group", "collidesWith"):
+            if k in edit:
+                _mask(edit[k])
+        out.append({"index": int(index), "restitution": e, "group": edit.get("group"),
+                    "collidesWith": edit.get("collidesWith", 0xFFFFFFFF), "allowSleep": edit.get("allowSleep")})
+    return out
+
+
+def stage_edits(edits, body_count: int, dt: float, allow_properties: bool = False) -> np.ndarray:
     """``editBodies(edits)`` records (``src/native/runtime.js:62-167``): the whole batch is
     validated before anything is queued; per edit the teleport comes first, then velocity
-    replacements, impulses and forces in kind order. Returns (n, 12) uint32 words."""
+    replacements, impulses and forces in kind order. Returns (n, 12) uint32 words. Property keys
+    (restitution, group, collidesWith, allowSleep) are left to ``stage_properties`` when
+    ``allow_properties``, else refused."""
     words = []
-    unsupported = {"isTrigger", "restitution", "allowSleep", "group", "collidesWith"}
+    unsupported = {"isTrigger"} if allow_properties else {"isTrigger", "restitution", "allowSleep", "group", "collidesWith"}
 
     def record(index, kind, value, point):
         w = np.zeros(12, dtype=np.uint32)
@@ -462,11 +492,35 @@ class World:
 
     # ---- body commands (src/native/runtime.js:46-167, src/native/cpu/world.js:145-166)
     def editBodies(self, edits):
-        """Queue a validated batch of body edits for the next step."""
+        """Queue a validated batch of body edits for the next step; property edits (restitution,
+        group/collidesWith, allowSleep) apply after the commands, as runtime.js:157-165 does."""
         self._live()
-        rec = stage_edits(edits, self.bodyCount, self.dt)
+        edits = list(edits)
+        props = stage_properties(edits, self.bodyCount)
+        rec = stage_edits(edits, self.bodyCount, self.dt, allow_properties=True)
         if len(rec):
             L.check(L.lib().avbd_world_edit(self._h, L.uptr(rec), int(rec.shape[0])))
+        for p in props:
+            if p["restitution"] is not None:
+                self.setRestitution([p["index"]], [p["restitution"]])
+            if p["group"] is not None:
+                self.setFilters([p["index"]], [p["group"]], [p["collidesWith"]])
+            if p["allowSleep"] is not None:
+                self.setSleepEnabled(p["index"], p["allowSleep"])
+        return self
+
+    def setRestitution(self, indices, values):
+        self._live()
+        idx = np.ascontiguousarray(np.asarray(indices, dtype=np.int64).reshape(-1))
+        val = np.ascontiguousarray(np.asarray(values, dtype=np.float32).reshape(-1))
+        if idx.size != val.size:
+            raise ValueError("Restitution arrays must have matching lengths")
+        if idx.size and (idx.min() < 0 or idx.max() >= self.bodyCount):
+            raise ValueError("A live body index is required")
+        if not np.all((val >= 0) & (val <= 1)):
+            raise ValueError("restitution must be between 0 and 1")
+        ia = np.ascontiguousarray(idx.astype(np.uint32))
+        L.check(L.lib().avbd_world_set_restitution(self._h, L.uptr(ia), int(ia.size), L.fptr(val)))
         return self
 
     def editRecords(self, records):

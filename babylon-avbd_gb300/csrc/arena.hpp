@@ -1582,6 +1582,31 @@ class Arena {
     wakeWorld(w);
   }
 
+  // setRestitution (src/native/cpu/world.js:343-351): restitution 0..1 of the given bodies; the
+  // bounce pass runs while any body of the world has restitution > 0; the world wakes.
+  void setRestitution(int w, const uint32_t* idx, int n, const float* values) {
+    if (w < 0 || w >= maxWorlds || !W[w].live) throw Error(AVBD_E_INVALID, "no such world");
+    if (n < 0) throw Error(AVBD_E_INVALID, "negative count");
+    const WorldRec& R = resident(w);
+    for (int k = 0; k < n; k++) {
+      if (idx[k] >= uint32_t(R.nBodies)) throw Error(AVBD_E_INVALID, "body index out of range");
+      if (!(values[k] >= 0.f && values[k] <= 1.f)) throw Error(AVBD_E_INVALID, "restitution must be between 0 and 1");
+    }
+    if (n == 0) return;
+    const size_t nb = size_t(R.nBodies), off = size_t(R.dev.bodyOff);
+    std::vector<float> e;
+    getRange(e, B.restitution, off, nb);
+    for (int k = 0; k < n; k++) e[idx[k]] = values[k];
+    putRange(B.restitution, off, e);
+    bool any = false;
+    for (float x : e) any |= x > 0.f;
+    WorldDev& D = W[w].dev;
+    D.flags = any ? (D.flags | FLAG_RESTITUTION) : (D.flags & ~FLAG_RESTITUTION);
+    uploadWorldDev(w);
+    flush();
+    wakeWorld(w);
+  }
+
   // ---------------------------------------------------------------- shape casts
   // raycastAll / sphereCastAll against world w's current poses; queued commands apply first
   // (src/native/solver3D.js:244-251). queries: 8 floats each (origin, max distance, direction,

@@ -451,6 +451,14 @@ int avbd_world_set_filters(avbd_world* w, const uint32_t* indices, int32_t n, co
   API_END
 }
 
+int avbd_world_set_restitution(avbd_world* w, const uint32_t* indices, int32_t n, const float* values) {
+  API_BEGIN
+  REQUIRE(w && (n == 0 || (indices && values)), "null argument");
+  bind(w->A->ctx);
+  w->A->setRestitution(w->w, indices, n, values);
+  API_END
+}
+
 int avbd_world_cast(avbd_world* w, const float* queries, int32_t n, const avbd_cast_filter* filter, float* hits) {
   API_BEGIN
   REQUIRE(w && (n == 0 || (queries && hits)), "null argument");

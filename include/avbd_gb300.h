@@ -265,6 +265,9 @@ int avbd_world_read_joints(avbd_world* w, float* out);
  * filters for the given bodies; the world wakes. */
 int avbd_world_set_filters(avbd_world* w, const uint32_t* indices, int32_t n, const uint32_t* groups,
                            const uint32_t* collides_with);
+/* setRestitution per body (src/native/cpu/world.js:343-351; editBodies' restitution property):
+ * values in [0, 1]; the world wakes. */
+int avbd_world_set_restitution(avbd_world* w, const uint32_t* indices, int32_t n, const float* values);
 
 /* Load per-body sleep flags and quiet times (state import for one-step comparisons; NULL skips). */
 int avbd_world_import_sleep_state(avbd_world* w, const int32_t* asleep, const float* quiet_time);

@@ -209,3 +209,17 @@ def test_spatial_sort_keeps_statics_first_and_remaps_constraints():
     # the Morton key: 10 bits per axis over the bounds, ties by index
     pts = np.array([[0.0, 0, 0], [1, 1, 1], [1, 0, 0], [0, 1, 0], [0, 0, 1], [1, 0, 0]])
     assert morton_order(pts).tolist() == [0, 2, 5, 3, 4, 1]
+
+
+def test_stage_properties_validation():
+    from avbd_gb300.pipeline import stage_edits, stage_properties
+    edits = [{"body": 1, "restitution": 0.5, "linearVelocity": [0, 1, 0]},
+             {"body": 2, "group": 4, "collidesWith": 3}, {"body": 3, "allowSleep": False}]
+    props = stage_properties(edits, 5)
+    assert [p["index"] for p in props] == [1, 2, 3]
+    assert props[0]["restitution"] == 0.5 and props[1]["group"] == 4 and props[2]["allowSleep"] is False
+    assert stage_edits(edits, 5, 0.5, allow_properties=True).shape == (1, 12)
+    for bad in ({"body": 0, "restitution": 1.5}, {"body": 0, "collidesWith": 3}, {"body": 0, "allowSleep": 1},
+                {"body": 0, "isTrigger": True}, {"body": 7, "group": 1}):
+        with pytest.raises(ValueError):
+            stage_properties([bad], 5)

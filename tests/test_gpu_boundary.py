@@ -89,3 +89,26 @@ def test_spatial_sort_slots_and_parity(pipe):
     assert rep["pairs_equal"] and rep["contact_counts_equal"] and rep["colors_equal"], rep
     assert rep["max_err_fp32"] <= parity.TOL, rep
     w.destroy()
+
+
+def test_property_edits_apply_after_commands(pipe):
+    # editBodies' property part (src/native/runtime.js:72-103,157-165): restitution turns the
+    # bounce pass on for a world created without it; a group edit stops a pair colliding
+    sc = AvbdScene3D(timeStep=1 / 60, iterations=10, gravity=-10)
+    sc.addBox([20, 1, 20], position=[0, -0.5, 0], density=0)
+    ball = sc.addSphere(0.5, position=[0, 0.6, 0])
+    other = sc.addSphere(0.5, position=[3, 0.6, 0])
+    w = pipe.createSolver(sc)
+    w.editBodies([{"body": ball, "restitution": 0.8, "linearVelocity": [0, -6, 0]},
+                  {"body": other, "group": 2, "collidesWith": 0}])
+    vmax = 0.0
+    for _ in range(6):
+        w.step(1)
+        vmax = max(vmax, float(w.readBodyState()["velocity"][ball][1]))
+    assert vmax > 3.0  # bounced: about 0.8 x 6 m/s
+    assert all(int(p[0]) != other and int(p[1]) != other for p in w.readPairs())  # falls through
+    w.step(24)
+    assert w.readBodyState()["position"][other][1] < 0.0
+    with pytest.raises(ValueError):
+        w.editBodies([{"body": ball, "restitution": 2.0}])
+    w.destroy()

@@ -1,0 +1,88 @@
+"""Edge cases of the world, batch and server paths (the reference's tests include the empty and
+ground-only scenes, tests/avbd3d-ref.test.ts): worlds with no bodies, only static bodies, one free
+body; batches mixing them with ordinary worlds; a server admitting and stepping them; empty calls
+(no indices, no records, no queries) that must succeed and change nothing.
+"""
+import numpy as np
+import pytest
+
+import parity
+import ref_scenes
+from avbd_gb300 import createSolverPipeline, workloads
+from avbd_gb300.scene import SolverParams
+
+pytestmark = pytest.mark.gpu
+
+KEYS = ("position", "rotation", "velocity", "angular", "prev_velocity")
+
+
+@pytest.fixture(scope="module")
+def pipe():
+    p = createSolverPipeline("gb300", device=0)
+    yield p
+    p.destroy()
+
+
+def _scene(index):
+    sc = ref_scenes.build(index)
+    sc.params = SolverParams(dt=1 / 60, gravity=-10.0, up=(0.0, 0.0, 1.0), iterations=10)
+    return sc
+
+
+def test_empty_and_ground_only_worlds(pipe):
+    empty, ground = _scene(0), _scene(1)
+    assert empty.n_bodies == 0
+    w = pipe.createSolver(empty)
+    w.step(5)
+    assert w.readBodyState()["position"].shape == (0, 3)
+    assert w.readCounters()["pairs"] == 0
+    assert w.readSelectedBodies([]).size == 0
+    assert w.sphereCastAll([]) == [] and w.raycast([0, 0, 5], [0, 0, -1]) is None
+    w.editBodies([])
+    w.setVelocities([], [])
+    assert w.readContactEvents()["events"] == []
+    w.destroy()
+    g = pipe.createSolver(ground)
+    rep = parity.compare_step(g, ground, 10)
+    assert rep["max_err_fp32"] <= parity.TOL and rep["pairs_equal"], rep
+    g.destroy()
+
+
+def test_batch_and_server_with_empty_worlds(pipe):
+    scenes = [_scene(0), workloads.mixed_pile(50, seed=3, extent=4.0), _scene(1), _scene(0)]
+    alone = pipe.createSolver(scenes[1])
+    alone.step(12)
+    ref = alone.readBodyState()
+    alone.destroy()
+    batch = pipe.createBatch(scenes)
+    batch.step(12)
+    got = batch.readBodyState(1)
+    for k in KEYS:
+        assert np.array_equal(got[k], ref[k]), k
+    assert batch.readBodyState(0)["position"].shape == (0, 3)
+    poses = batch.readPoses()
+    assert poses.shape == (batch.bodyCount, 8)
+    batch.destroy()
+    server = pipe.createServer(budgetBytes=1 << 30)
+    ids = [server.admit(sc) for sc in scenes]
+    for i in ids:
+        server.advance(i, 12)
+    for _ in range(12):
+        server.tick()
+    for k in KEYS:
+        assert np.array_equal(server.readBodyState(ids[1])[k], ref[k]), k
+    assert server.readPoses([ids[0], ids[3]]).shape == (0, 8)
+    t = server.advance(ids[0], 0)
+    assert t in server.completed()
+    server.destroy()
+
+
+def test_one_free_body_falls_like_the_oracle(pipe):
+    from avbd_gb300 import AvbdScene3D
+    sc = AvbdScene3D(timeStep=1 / 60, iterations=10, gravity=-10)
+    sc.addSphere(0.5, position=[0, 10, 0], velocity=[1, 0, 0], angularVelocity=[0, 2, 0])
+    arr = sc.arrays()
+    w = pipe.createSolver(sc)
+    rep = parity.compare_step(w, arr, 20)
+    assert rep["max_err_fp32"] <= parity.TOL and rep["pairs_gpu"] == 0, rep
+    w.destroy()
