@@ -1,7 +1,7 @@
 """CUDA engine parity and behaviour (needs a GPU).
 
-Parity is checked one step at a time from the engine's own state (SURVEY-style seedFrom in
-reverse): after some warm-up steps the engine's state is loaded into the oracle and both take
+Parity is checked one step at a time from the engine's own state (the reference GPU solver's
+seedFrom, src/vendor/three-avbd-lib/solver3D.ts:942-979, in reverse): after some warm-up steps the engine's state is loaded into the oracle and both take
 one step in the same colour order (parity.compare_step). Bit-exact: candidate pair sets,
 contacts per pair, colours. Float: poses and velocities within 1e-5 relative
 (|gpu - cpu| <= 1e-5 (|cpu| + 1)) of the float32 oracle.
