@@ -292,6 +292,30 @@ __global__ void k_pair_worlds(const WorldDev* __restrict__ worlds, Tick t, const
   if (blockIdx.x == 0 && threadIdx.x == 0) t.pairPrefix[t.nActive] = 0;
 }
 
+// In-place heapsort of a (hi, lo) range by lo (the partners of one body are distinct).
+__device__ void heapsort_by_partner(uint2* a, int n) {
+  auto sift = [&](int root, int size) {
+    const uint2 v = a[root];
+    int at = root;
+    while (true) {
+      int child = 2 * at + 1;
+      if (child >= size) break;
+      if (child + 1 < size && a[child + 1].y > a[child].y) child++;
+      if (a[child].y <= v.y) break;
+      a[at] = a[child];
+      at = child;
+    }
+    a[at] = v;
+  };
+  for (int r = n / 2 - 1; r >= 0; r--) sift(r, n);
+  for (int size = n - 1; size > 0; size--) {
+    const uint2 top = a[0];
+    a[0] = a[size];
+    a[size] = top;
+    sift(0, size);
+  }
+}
+
 __global__ void k_pair_write(PairCtx c, const WorldDev* __restrict__ worlds, Grid g, Tick t, const int* __restrict__ pairStart,
                              uint2* __restrict__ pairs) {
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < t.nBodies; k += gridDim.x * blockDim.x) {
@@ -314,16 +338,21 @@ __global__ void k_pair_write(PairCtx c, const WorldDev* __restrict__ worlds, Gri
         if (slot < cap) out[slot] = make_uint2(uint32_t(i), uint32_t(j));
       });
     }
-    // insertion sort of this body's range by partner (a body has a few dozen partners at most)
+    // this body's range by partner: insertion sort for the usual few dozen partners, heapsort
+    // beyond (a static or large body in a late slot can own a large share of its world's pairs)
     const int end = min(local + n, cap);
-    for (int a = local + 1; a < end; a++) {
-      const uint2 v = out[a];
-      int b = a;
-      while (b > local && out[b - 1].y > v.y) {
-        out[b] = out[b - 1];
-        b--;
+    if (end - local <= 64) {
+      for (int a = local + 1; a < end; a++) {
+        const uint2 v = out[a];
+        int b = a;
+        while (b > local && out[b - 1].y > v.y) {
+          out[b] = out[b - 1];
+          b--;
+        }
+        out[b] = v;
       }
-      out[b] = v;
+    } else {
+      heapsort_by_partner(out + local, end - local);
     }
   }
 }

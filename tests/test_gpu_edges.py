@@ -86,3 +86,22 @@ def test_one_free_body_falls_like_the_oracle(pipe):
     rep = parity.compare_step(w, arr, 20)
     assert rep["max_err_fp32"] <= parity.TOL and rep["pairs_gpu"] == 0, rep
     w.destroy()
+
+
+@pytest.mark.parametrize("broadphase", ["grid", "hploc"])
+def test_ground_created_last_owns_its_pairs(pipe, broadphase):
+    # pairs belong to their higher-index body: a ground created after 2,000 bodies owns every
+    # contact with it (its range is ordered by heapsort beyond 64 partners); same pairs, same step
+    sc = workloads.mixed_pile(2000, seed=23, extent=8.0)
+    perm = np.r_[np.arange(1, sc.n_bodies), 0]  # the ground (body 0) moves to the last slot
+    for k in ("pos", "quat", "size", "vel", "angvel", "prev_vel", "mass", "moment", "friction", "radius",
+              "shape", "group", "mask"):
+        setattr(sc, k, np.asarray(getattr(sc, k))[perm])
+    sc.params.broadphase = broadphase
+    w = pipe.createSolver(sc)
+    rep = parity.compare_step(w, sc, 60)
+    assert rep["pairs_equal"] and rep["contact_counts_equal"] and rep["colors_equal"], rep
+    assert rep["max_err_fp32"] <= parity.TOL, rep
+    ground = sc.n_bodies - 1
+    assert int(np.sum(w.readPairs()[:, 0] == ground)) > 64
+    w.destroy()
