@@ -450,8 +450,9 @@ class World:
         L.check(L.lib().avbd_world_step(self._h, int(steps)))
         return self
 
-    def advance(self, elapsed: float, maxSubSteps: int = 8, maxFrameTime: float = 0.25) -> int:
-        """Fixed-step accumulator (``src/native/runtime.js:255-272``); returns steps taken."""
+    def advance(self, elapsed: float, maxSubSteps: int = 6, maxFrameTime: float = 0.05) -> int:
+        """Fixed-step accumulator (``src/native/runtime.js:238-272``, defaults maxSubSteps 6 and
+        maxFrameTime 0.05 s); returns steps taken."""
         self._live()
         if not math.isfinite(elapsed) or elapsed < 0:
             raise ValueError("elapsed must be finite nonnegative seconds")

@@ -223,3 +223,23 @@ def test_stage_properties_validation():
                 {"body": 0, "isTrigger": True}, {"body": 7, "group": 1}):
         with pytest.raises(ValueError):
             stage_properties([bad], 5)
+
+
+def test_advance_accumulator_matches_runtime_js():
+    # runtime.js:238-272: at most maxSubSteps (6) steps, elapsed clamped to maxFrameTime (0.05 s)
+    from avbd_gb300.pipeline import World
+    taken = []
+
+    class Fake:
+        dt = 1 / 60
+        timeAccumulator = 0.0
+        _live = lambda self: None  # noqa: E731
+        step = lambda self, n: taken.append(n)  # noqa: E731
+
+    f = Fake()
+    assert World.advance(f, 1.0) == 3 and taken == [3]  # 0.05 s -> 3 steps of 1/60
+    assert World.advance(f, 0.01) == 0 and abs(f.timeAccumulator - 0.01) < 1e-12
+    assert World.advance(f, 0.01) == 1
+    import pytest as _pt
+    with _pt.raises(ValueError):
+        World.advance(f, -1.0)
