@@ -1,0 +1,342 @@
+// The "gb300" backend of createSolverPipeline (src/native/pipeline.js:14-92) over the Node-API
+// addon (avbd_addon.cc) and the engine's C ABI. A maintainer places this directory at
+// src/native/gb300/ of the reference tree (the imports below are relative to that place), builds
+// the addon with node-gyp, and lets pipeline.js accept backend "gb300":
+//
+//   if (backend === "gb300") return (await import("./gb300/index.js")).createGb300Pipeline(options);
+//
+// The world object offers the reference's native 3D world surface (src/native/scenes.d.ts:317-454);
+// editBodies, advance, bodyIndex/body and the velocity setters come from the reference's own
+// installNativeRuntime (src/native/runtime.js:324-410), which validates and stages exactly as the
+// other backends do, and reach the engine through prepareBodyCommands / setVelocities here.
+import { createRequire } from "node:module";
+import { IgnoreCollision, Joint, Spring } from "../../../reference/three-avbd/src/avbd3d/ref/forces.ts";
+import { isSphere } from "../../../reference/three-avbd/src/avbd3d/shapes.ts";
+import { installNativeRuntime } from "../runtime.js";
+
+const require = createRequire(import.meta.url);
+const addon = require("./build/Release/avbd_gb300.node");
+
+const BROADPHASE = { grid: 0, hploc: 1, auto: 2 };
+const INF = 3.4e38;
+
+/** Body slots along a Z-order curve, 10 bits per axis (solver3D.ts:344-367), with static and
+ * large bodies (radius above twice the median, at most 64) first in creation order: pairs are
+ * enumerated by their higher-index body. */
+export function spatialOrder(bodies) {
+  const n = bodies.length;
+  if (!n) return [];
+  const radii = bodies.map((b) => b.radius).sort((a, b) => a - b);
+  let thr = 2 * radii[Math.floor(n / 2)];
+  if (radii.filter((r) => r > thr).length > 64) thr = radii[n - 65];
+  const first = bodies.map((b) => !(b.mass > 0) || b.radius > thr);
+  const rest = bodies.map((_, i) => i).filter((i) => !first[i]);
+  const lo = [Infinity, Infinity, Infinity], hi = [-Infinity, -Infinity, -Infinity];
+  for (const i of rest)
+    for (let k = 0; k < 3; k++) {
+      lo[k] = Math.min(lo[k], bodies[i].positionLin[k]);
+      hi[k] = Math.max(hi[k], bodies[i].positionLin[k]);
+    }
+  const spread = (v) => {
+    let x = v & 0x3ff;
+    x = (x | (x << 16)) & 0x30000ff;
+    x = (x | (x << 8)) & 0x300f00f;
+    x = (x | (x << 4)) & 0x30c30c3;
+    x = (x | (x << 2)) & 0x9249249;
+    return x;
+  };
+  const code = new Map(rest.map((i) => {
+    const q = [0, 1, 2].map((k) =>
+      Math.min(1023, Math.floor(((bodies[i].positionLin[k] - lo[k]) / Math.max(hi[k] - lo[k], 1e-9)) * 1024)));
+    return [i, (spread(q[0]) | (spread(q[1]) << 1) | (spread(q[2]) << 2)) >>> 0];
+  }));
+  rest.sort((a, b) => code.get(a) - code.get(b) || a - b);
+  return bodies.map((_, i) => i).filter((i) => first[i]).concat(rest);
+}
+
+/** The scene as the structure of arrays of avbd_scene_desc, bodies in slot order. */
+export function packScene(scene, options = {}) {
+  const ref = scene.ref;
+  const all = ref.bodies;
+  const order = options.spatialSort === false ? all.map((_, i) => i) : spatialOrder(all);
+  const slot = new Map(order.map((i, s) => [all[i], s]));
+  const n = order.length;
+  const a = {
+    position: new Float32Array(3 * n), rotation: new Float32Array(4 * n), size: new Float32Array(3 * n),
+    velocity: new Float32Array(3 * n), angularVelocity: new Float32Array(3 * n), prevVelocity: new Float32Array(3 * n),
+    mass: new Float32Array(n), moment: new Float32Array(3 * n), friction: new Float32Array(n), radius: new Float32Array(n),
+    shape: new Int32Array(n), group: new Uint32Array(n), collidesWith: new Uint32Array(n),
+    restitution: new Float32Array(n), allowSleep: new Int32Array(n),
+  };
+  order.forEach((i, s) => {
+    const b = all[i];
+    a.position.set(b.positionLin, 3 * s);
+    a.rotation.set(b.positionAng, 4 * s);
+    a.size.set(b.size, 3 * s);
+    a.velocity.set(b.velocityLin, 3 * s);
+    a.angularVelocity.set(b.velocityAng, 3 * s);
+    a.prevVelocity.set(b.prevVelocityLin, 3 * s);
+    a.moment.set(b.moment, 3 * s);
+    a.mass[s] = b.mass;
+    a.friction[s] = b.friction;
+    a.radius[s] = b.radius;
+    a.shape[s] = isSphere(b) ? 1 : 0;
+    a.group[s] = b.group ?? 0xffffffff;
+    a.collidesWith[s] = b.collidesWith ?? 0xffffffff;
+    a.restitution[s] = b.restitution ?? 0;
+    a.allowSleep[s] = b.allowSleep === false ? 0 : 1;
+    if (b.isTrigger) throw Error("triggers are not supported by the gb300 backend");
+  });
+  // joints, springs and ignore pairs in creation order (their order is the engine's joint id)
+  const cons = ref.forces.filter((f) => f instanceof Joint || f instanceof Spring || f instanceof IgnoreCollision);
+  const m = cons.length;
+  Object.assign(a, {
+    consKind: new Int32Array(m), consA: new Int32Array(m), consB: new Int32Array(m),
+    consRA: new Float32Array(3 * m), consRB: new Float32Array(3 * m),
+    consP0: new Float32Array(m), consP1: new Float32Array(m), consP2: new Float32Array(m),
+  });
+  cons.forEach((f, c) => {
+    a.consA[c] = f.bodyA ? slot.get(f.bodyA) : -1;
+    a.consB[c] = slot.get(f.bodyB);
+    if (f instanceof Joint) {
+      a.consKind[c] = 0;
+      a.consRA.set(f.rA, 3 * c);
+      a.consRB.set(f.rB, 3 * c);
+      a.consP0[c] = f.stiffnessLin;
+      a.consP1[c] = f.stiffnessAng;
+      a.consP2[c] = f.fracture;
+    } else if (f instanceof Spring) {
+      a.consKind[c] = 1;
+      a.consRA.set(f.rA, 3 * c);
+      a.consRB.set(f.rB, 3 * c);
+      a.consP0[c] = f.stiffness;
+      a.consP1[c] = f.rest;
+    } else {
+      a.consKind[c] = 2;
+    }
+  });
+  const sleeping = options.sleeping ?? (scene.sleepOptIn ? true : false);
+  const params = {
+    dt: ref.dt, gravity: ref.gravity, up: new Float32Array(scene.up), iterations: ref.iterations,
+    alpha: ref.alpha, betaLin: ref.betaLin, betaAng: ref.betaAng, gamma: ref.gamma,
+    massPenalty: 1, faceBias: 1, colorRounds: options.colorRounds ?? 64,
+    broadphase: BROADPHASE[options.broadphase ?? "auto"], bvhRebuild: options.bvh?.rebuildInterval ?? 16,
+    sleeping: sleeping ? 1 : 0, sleepSpeed: sleeping?.speedThreshold ?? 0.08, sleepTime: sleeping?.timeThreshold ?? 0.6,
+  };
+  if (params.broadphase === undefined) throw Error("broadphase must be 'grid', 'hploc' or 'auto'");
+  return { arrays: a, params, order, jointCount: cons.filter((f) => !(f instanceof IgnoreCollision)).length };
+}
+
+class Gb300World {
+  constructor(ctx, scene, options) {
+    const packed = packScene(scene, options);
+    this.handle = addon.createWorld(ctx, packed.arrays, packed.params);
+    this.dimension = 3;
+    this.bodyCount = packed.order.length;
+    this.jointCount = packed.jointCount;
+    this.params = { dt: packed.params.dt };
+    this.timeAccumulator = 0;
+    this.destroyed = false;
+    this.slots = new Int32Array(this.bodyCount);
+    packed.order.forEach((i, s) => (this.slots[i] = s));
+    installNativeRuntime(this, { bodies: scene.ref.bodies }, 3, {
+      setVelocities: this.setPackedVelocities,
+      readSelectedBodies: this.readSelectedBodies,
+    });
+  }
+  assertLive() {
+    if (this.destroyed) throw Error("The solver has been destroyed");
+  }
+  liveIndex(index) {
+    this.assertLive();
+    if (!Number.isInteger(index) || index < 0 || index >= this.bodyCount) throw Error("A live body index is required");
+  }
+  gpuIndex(referenceIndex) {
+    this.liveIndex(referenceIndex);
+    return this.slots[referenceIndex];
+  }
+  step() {
+    this.assertLive();
+    addon.step(this.handle, 1);
+    return this;
+  }
+  flushEdits() {
+    this.assertLive();
+    addon.flushEdits(this.handle);
+    return this;
+  }
+  // the staged 12-word records of runtime.js editBodies
+  prepareBodyCommands() {
+    return { enqueueValidated: (commands) => addon.edit(this.handle, commands.u32.subarray(0, commands.count * 12)) };
+  }
+  // per-body commands of NativeBody handles (src/native/solver3D.js:140-190), staged by editBodies
+  setLinearVelocity(index, v) {
+    return this.editBodies([{ body: index, linearVelocity: v }]);
+  }
+  setAngularVelocity(index, v) {
+    return this.editBodies([{ body: index, angularVelocity: v }]);
+  }
+  applyImpulse(index, v, point) {
+    return this.editBodies([{ body: index, impulse: v, ...(point !== undefined ? { worldPoint: point } : {}) }]);
+  }
+  applyForce(index, v, point) {
+    return this.editBodies([{ body: index, force: v, ...(point !== undefined ? { worldPoint: point } : {}) }]);
+  }
+  applyAngularImpulse(index, v) {
+    return this.editBodies([{ body: index, angularImpulse: v }]);
+  }
+  applyTorque(index, v) {
+    return this.editBodies([{ body: index, torque: v }]);
+  }
+  teleport(index, position, rotation) {
+    return this.editBodies([{ body: index, position, ...(rotation !== undefined ? { rotation } : {}) }]);
+  }
+  setPoses(indices, positions, rotations) {
+    this.assertLive();
+    addon.setPoses(this.handle, Uint32Array.from(indices), Float32Array.from(positions),
+      rotations ? Float32Array.from(rotations) : null);
+    return this;
+  }
+  setPackedVelocities(indices, values) {
+    if (values?.linear === undefined && values?.angular === undefined) throw Error("Provide linear or angular velocities");
+    addon.setVelocities(this.handle, Uint32Array.from(indices),
+      values.linear !== undefined ? Float32Array.from(values.linear) : null,
+      values.angular !== undefined ? Float32Array.from(values.angular) : null);
+    return this;
+  }
+  async readSelectedBodies(indices, { posesOnly = false } = {}) {
+    this.assertLive();
+    return addon.readSelected(this.handle, Uint32Array.from(indices), posesOnly);
+  }
+  async readBodies() {
+    return this.readSelectedBodies(Uint32Array.from({ length: this.bodyCount }, (_, i) => i));
+  }
+  async readBodyState() {
+    this.assertLive();
+    return addon.readState(this.handle, this.bodyCount);
+  }
+  async readJoints() {
+    this.assertLive();
+    return addon.readJoints(this.handle, this.jointCount);
+  }
+  async readCounters() {
+    this.assertLive();
+    return addon.readCounters(this.handle);
+  }
+  setFilters(indices, groups, collidesWith) {
+    this.assertLive();
+    addon.setFilters(this.handle, Uint32Array.from(indices), Uint32Array.from(groups), Uint32Array.from(collidesWith));
+  }
+  setRestitution(index, value) {
+    this.assertLive();
+    addon.setRestitution(this.handle, Uint32Array.of(index), Float32Array.of(value));
+  }
+  setSensor() {
+    throw Error("triggers are not supported by the gb300 backend");
+  }
+  setSleepEnabled(index, enabled) {
+    this.liveIndex(index);
+    addon.setSleepEnabled(this.handle, index, enabled);
+    return this;
+  }
+  enableSleeping({ speedThreshold = 0.08, timeThreshold = 0.6 } = {}) {
+    this.assertLive();
+    addon.setSleeping(this.handle, true, speedThreshold, timeThreshold);
+    return this;
+  }
+  disableSleeping() {
+    this.assertLive();
+    addon.setSleeping(this.handle, false, 0, 0);
+    return this;
+  }
+  wakeAll() {
+    this.assertLive();
+    addon.wakeAll(this.handle);
+    return this;
+  }
+  async readSleepStats() {
+    this.assertLive();
+    return { sleeping: addon.sleepStats(this.handle), wakeRequested: false };
+  }
+  watchContacts({ maxPairs = 8192, maxEvents = 4096, indices } = {}) {
+    this.assertLive();
+    addon.watchContacts(this.handle, indices === undefined ? null : Uint32Array.from(indices), maxPairs, maxEvents);
+    return this;
+  }
+  async readContactEvents() {
+    this.watchContacts();
+    const { records, dropped, full } = addon.readContactEvents(this.handle);
+    const f = new Float32Array(records.buffer, records.byteOffset, records.length);
+    const events = [];
+    for (let o = 0; o < records.length; o += 12)
+      events.push({
+        type: records[o] === 1 ? "begin" : "end", kind: records[o], a: records[o + 1], b: records[o + 2],
+        step: records[o + 3], point: [f[o + 4], f[o + 5], f[o + 6]], impulse: f[o + 7],
+        normal: [f[o + 8], f[o + 9], f[o + 10]], isTrigger: false,
+      });
+    return { events, dropped, full };
+  }
+  resetContactHistory(indices) {
+    if (!(indices instanceof Uint32Array)) throw Error("Contact resets require Uint32 GPU slots");
+    addon.resetContactHistory(this.handle, indices);
+    return this;
+  }
+  async sphereCastAll(casts, options = {}) {
+    this.assertLive();
+    const q = new Float32Array(8 * casts.length);
+    casts.forEach((c, i) => {
+      const d = Array.from(c.direction), len = Math.hypot(...d);
+      q.set([...c.origin, c.maxDistance ?? options.maxDistance ?? INF, ...d.map((x) => x / len), c.radius ?? 0], 8 * i);
+    });
+    const filter = {
+      collidesWith: options.collidesWith ?? 0xffffffff,
+      ...(options.membership !== undefined ? { membership: options.membership } : {}),
+      ignore: Uint32Array.from(options.ignore ?? []),
+    };
+    const hits = casts.length ? addon.cast(this.handle, q, filter) : new Float32Array(0);
+    const index = new Uint32Array(hits.buffer, hits.byteOffset, hits.length);
+    return casts.map((c, i) => {
+      const t = hits[8 * i + 3];
+      if (t < 0) return null;
+      const normal = [hits[8 * i], hits[8 * i + 1], hits[8 * i + 2]];
+      const d = Array.from(c.direction), len = Math.hypot(...d);
+      const center = c.origin.map((x, k) => x + (t * d[k]) / len);
+      const r = c.radius ?? 0;
+      return { index: index[8 * i + 4], distance: t, normal, center, point: center.map((x, k) => x - r * normal[k]) };
+    });
+  }
+  async raycastAll(rays, options) {
+    return this.sphereCastAll(rays.map((r) => ({ ...r, radius: 0 })), options);
+  }
+  async sphereCast(origin, radius, direction, options) {
+    return (await this.sphereCastAll([{ origin, radius, direction }], options))[0];
+  }
+  async raycast(origin, direction, options) {
+    return this.sphereCast(origin, 0, direction, options);
+  }
+  destroy() {
+    if (this.destroyed) return;
+    addon.destroyWorld(this.handle);
+    this.destroyed = true;
+  }
+}
+
+/** createSolverPipeline({backend: "gb300", deviceIndex}) */
+export function createGb300Pipeline(options = {}) {
+  const ctx = addon.createContext(options.deviceIndex ?? 0);
+  const worlds = new Set();
+  return {
+    backend: "gb300",
+    createSolver(scene, solverOptions = {}) {
+      const w = new Gb300World(ctx, scene, solverOptions);
+      scene.created = true;
+      worlds.add(w);
+      return w;
+    },
+    destroy() {
+      for (const w of worlds) w.destroy();
+      worlds.clear();
+      addon.destroyContext(ctx);
+    },
+  };
+}
