@@ -243,3 +243,19 @@ def test_advance_accumulator_matches_runtime_js():
     import pytest as _pt
     with _pt.raises(ValueError):
         World.advance(f, -1.0)
+
+
+def test_node_addon_compiles_against_the_node_api_declarations():
+    # the addon (babylon-avbd_gb300/node/avbd_addon.cc) cannot be built without Node; its C++ is
+    # checked here against declarations of the Node-API functions it calls and the real C ABI
+    import shutil
+    import subprocess
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("no g++")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([gxx, "-std=c++17", "-fsyntax-only", "-Wall", "-Wextra", "-Werror",
+                        "-I", os.path.join(root, "tests", "napi_decl"), "-I", os.path.join(root, "include"),
+                        "-DNODE_GYP_MODULE_NAME=avbd_gb300", os.path.join(root, "babylon-avbd_gb300", "node", "avbd_addon.cc")],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
