@@ -1006,6 +1006,21 @@ __global__ void __launch_bounds__(128, AVBD_NP_BOX_MINB) k_np_box(BodyPtrs bd, c
 
 // Pass 2b: pairs with a sphere (generic support-function SAT, one contact): sphere-box pairs,
 // then sphere-sphere pairs in a lighter instance of the same code.
+// A sphere and a box clearly apart: the distance from the sphere's centre to the box exceeds its
+// radius by far more than any rounding of the separating-axis search (1e-3 plus 1e-5 of the
+// coordinates' size), so that search would end with a positive gap and no contact: skip it.
+__device__ __forceinline__ bool sphere_box_apart(float4 pA, float4 qA, float4 sA, int shA, float4 pB, float4 qB, float4 sB) {
+  const bool sphereA = shA == SHAPE_SPHERE;
+  const float4 pc = sphereA ? pA : pB, pbx = sphereA ? pB : pA, qbx = sphereA ? qB : qA, sbx = sphereA ? sB : sA;
+  const float r = (sphereA ? sA : sB).x * 0.5f;
+  const V3 l = rotateInv(qbx, v3(pc) - v3(pbx));
+  const V3 h{sbx.x * 0.5f, sbx.y * 0.5f, sbx.z * 0.5f};
+  const V3 o{fmaxf(fabsf(l.x) - h.x, 0.f), fmaxf(fabsf(l.y) - h.y, 0.f), fmaxf(fabsf(l.z) - h.z, 0.f)};
+  const float margin = 1e-3f + 1e-5f * (fabsf(pc.x) + fabsf(pc.y) + fabsf(pc.z) + fabsf(pbx.x) + fabsf(pbx.y) + fabsf(pbx.z));
+  const float reach = r + margin;
+  return dot(o, o) > reach * reach;
+}
+
 #ifndef AVBD_NP_SPHERE_MINB
 #define AVBD_NP_SPHERE_MINB 5  // blocks per SM the register allocation must allow
 #endif
@@ -1025,7 +1040,9 @@ __global__ void __launch_bounds__(128, AVBD_NP_SPHERE_MINB) k_np_sphere(BodyPtrs
     M33 basis{V3{0, 0, 0}, V3{0, 0, 0}, V3{0, 0, 0}};
     uint32_t feat[1] = {1u};  // feature i + 1
     V3 rA[1], rB[1];
-    const int nc = gen::collide<BOTH_ROUND>(pA, qA, sA, shA, pB, qB, sB, shB, basis, rA[0], rB[0]);
+    const int nc = (!BOTH_ROUND && sphere_box_apart(pA, qA, sA, shA, pB, qB, sB))
+                       ? 0
+                       : gen::collide<BOTH_ROUND>(pA, qA, sA, shA, pB, qB, sB, shB, basis, rA[0], rB[0]);
     finish_pair(bd, W, t, bd.meta[a].x, cur, p, key, pA, qA, sA, pB, qB, sB, true, nc, basis, feat, rA, rB);
   }
 }

@@ -105,3 +105,38 @@ def test_ground_created_last_owns_its_pairs(pipe, broadphase):
     ground = sc.n_bodies - 1
     assert int(np.sum(w.readPairs()[:, 0] == ground)) > 64
     w.destroy()
+
+
+def test_sphere_box_pairs_around_the_touching_distance(pipe):
+    # spheres placed at distances from 2 cm inside to 2 cm outside rotated boxes (face, edge and
+    # corner regions): contact counts, poses and velocities as the oracle's one step
+    from avbd_gb300 import AvbdScene3D
+    rng = np.random.default_rng(8)
+    sc = AvbdScene3D(timeStep=1 / 60, iterations=10, gravity=0)
+    for k in range(60):
+        c = np.array([6.0 * (k % 10), 0.0, 6.0 * (k // 10)])
+        q = rng.normal(size=4)
+        q /= np.linalg.norm(q)
+        h = rng.uniform(0.3, 1.0, 3)
+        sc.addBox(list(2 * h), position=list(c), rotation=list(q), density=0)
+        local = rng.normal(size=3) * h * 2.5  # a point around the box, in its frame
+        nearest = np.clip(local, -h, h)
+        d = local - nearest
+        if np.linalg.norm(d) < 1e-3:
+            d = np.array([1.0, 0.0, 0.0]) * h[0]
+            nearest = np.array([h[0], 0.0, 0.0])
+        r = 0.4
+        gap = rng.uniform(-0.02, 0.02)
+        p_local = nearest + d / np.linalg.norm(d) * (r + gap)
+        x, y, z, w = q
+        R = np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)],
+                      [2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)],
+                      [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)]])
+        sc.addSphere(r, position=list(c + R @ p_local))
+    arr = sc.arrays()
+    w = pipe.createSolver(sc)
+    rep = parity.compare_step(w, arr, 0)
+    assert rep["pairs_equal"] and rep["contact_counts_equal"], rep
+    assert rep["max_err_fp32"] <= parity.TOL, rep
+    assert 10 < rep["contacts"] < 60, rep  # both touching and clearly separated pairs
+    w.destroy()
