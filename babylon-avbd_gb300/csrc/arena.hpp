@@ -1768,21 +1768,31 @@ class Arena {
     const int ncolors = ctrHost->ncolors;
     bool sleepy = false;
     for (int w : act) sleepy |= (W[w].dev.flags & FLAG_SLEEP) != 0;
-    for (int it = 0; it < maxIter; it++) {
-      for (int c = 0; c < ncolors; c++) {
-        const int cnt = ctrHost->colorCount[c];
-        if (!cnt) continue;
-        cudaEvent_t a = prof ? mark() : nullptr;
-        launch_primal(B, worlds, J, P, t, T, ctr, c, it, cnt, ctrHost->colorItems[c], sleepy, s);
-        if (prof) {
-          span(P_PRIMAL, a, mark());
-          profPrimalLaunches += 1;
-        }
+    if (nb <= AVBD_COOP_SOLVE_MAX) {
+      // a small tick: the whole loop in one cooperative launch (same order of updates)
+      cudaEvent_t a = prof ? mark() : nullptr;
+      CK(launch_solve_coop(B, worlds, J, P, t, T, ctr, maxIter, nb, sleepy, s));
+      if (prof) {
+        span(P_PRIMAL, a, mark());
+        profPrimalLaunches += 1;
       }
-      if (nj) {
-        cudaEvent_t d = prof ? mark() : nullptr;
-        launch_dual_joints(B, worlds, J, t, it, s);
-        if (prof) span(P_DUAL, d, mark());
+    } else {
+      for (int it = 0; it < maxIter; it++) {
+        for (int c = 0; c < ncolors; c++) {
+          const int cnt = ctrHost->colorCount[c];
+          if (!cnt) continue;
+          cudaEvent_t a = prof ? mark() : nullptr;
+          launch_primal(B, worlds, J, P, t, T, ctr, c, it, cnt, ctrHost->colorItems[c], sleepy, s);
+          if (prof) {
+            span(P_PRIMAL, a, mark());
+            profPrimalLaunches += 1;
+          }
+        }
+        if (nj) {
+          cudaEvent_t d = prof ? mark() : nullptr;
+          launch_dual_joints(B, worlds, J, t, it, s);
+          if (prof) span(P_DUAL, d, mark());
+        }
       }
     }
     bool bounce = false;

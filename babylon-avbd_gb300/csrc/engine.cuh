@@ -265,6 +265,14 @@ __host__ __device__ __forceinline__ int item_iterations(int code) { return code 
 // sleepy: some stepped world has sleeping on (rows of sleeping bodies are skipped: nobody reads them)
 void launch_primal(const BodyPtrs& b, const WorldDev* worlds, JointPtrs j, PairPtrs P, Tick t, Topo topo, const Counters* ctr,
                    int color, int iteration, int nBodiesColor, int nItemsColor, bool sleepy, cudaStream_t s);
+// Ticks of at most this many bodies run their solve loop as one cooperative launch.
+#ifndef AVBD_COOP_SOLVE_MAX
+#define AVBD_COOP_SOLVE_MAX 131072
+#endif
+// The whole solve loop (all iterations, colours and joint duals) in one cooperative launch, for
+// ticks small enough that per-colour launches are latency-bound; same order, same bits.
+cudaError_t launch_solve_coop(const BodyPtrs& b, const WorldDev* worlds, JointPtrs j, PairPtrs P, Tick t, Topo topo, const Counters* ctr,
+                              int maxIter, int nBodies, bool sleepy, cudaStream_t s);
 // Joint duals of one iteration (contact duals run inside launch_primal, see k_primal).
 void launch_dual_joints(const BodyPtrs& b, const WorldDev* worlds, JointPtrs j, Tick t, int iteration, cudaStream_t s);
 void launch_velocities(const BodyPtrs& b, const WorldDev* worlds, Tick t, cudaStream_t s);
