@@ -171,3 +171,20 @@ def test_free_fall_analytic(pipe):
     # lands exactly on the inertial target each step: y_n = y0 - g dt^2 (1 + 2 + ... + n)
     assert abs(y - (5 - 10 * (1 / 60) ** 2 * 3)) < 1e-5, y
     w.destroy()
+
+
+def test_resting_contact_respects_the_floor_margin(pipe):
+    """The reference's canonical check (tests/gpu-canonical.js:38-64): a unit box dropped from
+    z = 4 onto a 100 x 100 x 1 floor rests after 240 steps with its centre at
+    1 - COLLISION_MARGIN within 0.01, on at least four contacts."""
+    from avbd_gb300 import AvbdScene3D
+    sc = AvbdScene3D(timeStep=1 / 60, iterations=10, gravity=-10, up=[0, 0, 1])
+    sc.addBox([100, 100, 1], density=0, friction=0.5, position=[0, 0, 0])
+    box = sc.addBox([1, 1, 1], density=1, friction=0.5, position=[0, 0, 4])
+    w = pipe.createSolver(sc)
+    w.step(240)
+    z = float(w.readBodyState()["position"][box][2])
+    assert abs(z - (1 - 0.01)) < 0.01, z
+    c = w.readCounters()
+    assert c["contacts"] >= 4 and c["conflicts"] == 0
+    w.destroy()
