@@ -4,8 +4,8 @@ Host side of the engine: the scene builder (``AvbdScene3D``), ``createSolverPipe
 its worlds, batches and world servers over the C ABI of ``libavbd_gb300.so``, and the synthetic benchmark
 scenes. The compute path is CUDA only; there is no CPU fallback.
 """
-from .scene import AvbdScene3D, SceneArrays, SceneBuilder, SolverParams  # noqa: F401
+from .scene import AvbdScene3D, Hinge, SceneArrays, SceneBuilder, SolverParams  # noqa: F401
 from .pipeline import Batch, Server, SolverPipeline, World, createSolverPipeline  # noqa: F401
 
-__all__ = ["AvbdScene3D", "SceneArrays", "SceneBuilder", "SolverParams", "createSolverPipeline",
+__all__ = ["AvbdScene3D", "Hinge", "SceneArrays", "SceneBuilder", "SolverParams", "createSolverPipeline",
            "SolverPipeline", "World", "Batch", "Server"]

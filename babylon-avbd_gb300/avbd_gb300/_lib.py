@@ -128,6 +128,10 @@ SIGNATURES = [
     ("avbd_world_set_filters", C.c_int, [C.c_void_p, _up, C.c_int32, _up, _up]),
     ("avbd_world_set_restitution", C.c_int, [C.c_void_p, _up, C.c_int32, _fp]),
     ("avbd_batch_read_joints", C.c_int, [C.c_void_p, C.c_int32, _fp]),
+    ("avbd_world_set_motor", C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_float, C.c_float]),
+    ("avbd_batch_set_motor", C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_float, C.c_float]),
+    ("avbd_world_release_joints", C.c_int, [C.c_void_p, _ip, C.c_int32]),
+    ("avbd_batch_release_joints", C.c_int, [C.c_void_p, C.c_int32, _ip, C.c_int32]),
     ("avbd_batch_cast", C.c_int, [C.c_void_p, C.c_int32, _fp, C.c_int32, C.c_void_p, _fp]),
     ("avbd_server_cast", C.c_int, [C.c_void_p, C.c_int64, _fp, C.c_int32, C.c_void_p, _fp]),
     ("avbd_world_reset_contact_history", C.c_int, [C.c_void_p, _up, C.c_int32]),

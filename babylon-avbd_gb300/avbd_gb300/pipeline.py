@@ -411,6 +411,40 @@ def stage_edits(edits, body_count: int, dt: float, allow_properties: bool = Fals
     return np.stack(words) if words else np.zeros((0, 12), dtype=np.uint32)
 
 
+def _motor_slot(kinds, constraint) -> int:
+    """Joint slot (index among joints, springs and angular rows) of a motor's constraint index."""
+    from .scene import KIND_IGNORE, KIND_MOTOR
+    c = int(constraint)
+    if not 0 <= c < len(kinds) or kinds[c] != KIND_MOTOR:
+        raise ValueError("Motor needs an active motor slot")
+    return int(np.count_nonzero(kinds[:c] != KIND_IGNORE))
+
+
+def _joint_slots(kinds, constraints) -> np.ndarray:
+    """Joint slots of constraint indices (ignore-collision pairs have none)."""
+    from .scene import KIND_IGNORE
+    c = np.asarray(constraints, dtype=np.int64).reshape(-1)
+    if c.size and (c.min() < 0 or c.max() >= len(kinds) or np.any(kinds[c] == KIND_IGNORE)):
+        raise ValueError("A live constraint slot is required")
+    before = np.cumsum(kinds != KIND_IGNORE) - 1
+    return np.ascontiguousarray(before[c].astype(np.int32))
+
+
+def _motor_args(speed, maxTorque):
+    mask, sp, mt = 0, 0.0, 0.0
+    if speed is not None:
+        sp = float(speed)
+        if not math.isfinite(sp):
+            raise ValueError("Motor speed must be finite")
+        mask |= 1
+    if maxTorque is not None:
+        mt = float(maxTorque)
+        if not (math.isfinite(mt) and mt >= 0):
+            raise ValueError("maxTorque must be nonnegative")
+        mask |= 2
+    return mask, sp, mt
+
+
 def _indices(indices, n):
     idx = np.ascontiguousarray(np.asarray(indices, dtype=np.int64).reshape(-1))
     if idx.size and (idx.min() < 0 or idx.max() >= n):
@@ -429,6 +463,7 @@ class World:
         self._h = h
         self.bodyCount = arrays.n_bodies
         self.jointCount = self._packed.n_joints
+        self._kinds = np.asarray(arrays.kind, dtype=np.int32).copy()
         self.dt = float(arrays.params.dt)
         # body slots: creation order, or Morton order with spatialSort (order[slot] = creation index)
         order = getattr(arrays, "order", None)
@@ -509,6 +544,22 @@ class World:
             if p["allowSleep"] is not None:
                 self.setSleepEnabled(p["index"], p["allowSleep"])
         return self
+
+    def setMotor(self, constraint, speed=None, maxTorque=None):
+        """setMotor (src/gpu/appGpuSolver3D.js:547-562): a new speed and/or torque bound of the
+        motor created as constraint index `constraint` (addMotor, or a Hinge's motor); wakes the
+        world."""
+        self._live()
+        slot = _motor_slot(self._kinds, constraint)
+        mask, sp, mt = _motor_args(speed, maxTorque)
+        L.check(L.lib().avbd_world_set_motor(self._h, slot, mask, sp, mt))
+
+    def releaseJoints(self, constraints):
+        """releaseJoints (src/native/cpu/world.js:397-410): the constraints at these constraint
+        indices (joints, springs, motors, limits) stop acting; wakes the world."""
+        self._live()
+        slots = _joint_slots(self._kinds, constraints)
+        L.check(L.lib().avbd_world_release_joints(self._h, L.iptr(slots), int(slots.size)))
 
     def setRestitution(self, indices, values):
         self._live()
@@ -803,6 +854,7 @@ class Batch:
         self.bodyCounts = [a.n_bodies for a in arrays_list]
         self._dts = [float(a.params.dt) for a in arrays_list]
         self._jointCounts = [p.n_joints for p in self._packed]
+        self._kinds = [np.asarray(a.kind, dtype=np.int32).copy() for a in arrays_list]
         self.bodyCount = int(sum(self.bodyCounts))
 
     def step(self, steps: int = 1):
@@ -820,6 +872,21 @@ class Batch:
         L.check(L.lib().avbd_batch_read_state(self._h, int(world), *(L.fptr(out[k]) for k in
                                                                      ("position", "rotation", "velocity", "angular", "prev_velocity"))))
         return out
+
+    def setMotor(self, world: int, constraint, speed=None, maxTorque=None):
+        """World.setMotor for world `world` of the batch."""
+        if not 0 <= world < self.worldCount:
+            raise ValueError("world index out of range")
+        slot = _motor_slot(self._kinds[world], constraint)
+        mask, sp, mt = _motor_args(speed, maxTorque)
+        L.check(L.lib().avbd_batch_set_motor(self._h, int(world), slot, mask, sp, mt))
+
+    def releaseJoints(self, world: int, constraints):
+        """World.releaseJoints for world `world` of the batch."""
+        if not 0 <= world < self.worldCount:
+            raise ValueError("world index out of range")
+        slots = _joint_slots(self._kinds[world], constraints)
+        L.check(L.lib().avbd_batch_release_joints(self._h, int(world), L.iptr(slots), int(slots.size)))
 
     def readJoints(self, world: int) -> np.ndarray:
         if not 0 <= world < self.worldCount:

@@ -23,6 +23,8 @@ SHAPE_SPHERE = 1
 KIND_JOINT = 0
 KIND_SPRING = 1
 KIND_IGNORE = 2
+KIND_MOTOR = 3  # angular rows (src/gpu/angularConstraints.js info types 3 and 4)
+KIND_LIMIT = 4
 
 INF = math.inf
 MASK_ALL = 0xFFFFFFFF
@@ -161,6 +163,10 @@ class SceneBuilder:
         self.cons.append((KIND_SPRING, int(a), int(b), ra, rb, float(stiffness), float(rest), 0.0))
         return len(self.cons) - 1
 
+    def angular(self, kind, a, b, axis_a, axis_b, p0, p1) -> int:
+        self.cons.append((int(kind), -1 if a is None else int(a), int(b), axis_a, axis_b, float(p0), float(p1), 0.0))
+        return len(self.cons) - 1
+
     def ignore(self, a, b) -> int:
         self.cons.append((KIND_IGNORE, int(a), int(b), (0, 0, 0), (0, 0, 0), 0.0, 0.0, 0.0))
         return len(self.cons) - 1
@@ -202,6 +208,37 @@ class SceneBuilder:
             p2=np.array([c[7] for c in self.cons], dtype=np.float64),
             params=self.params,
         )
+
+
+@dataclass(frozen=True)
+class Hinge:
+    """addHinge's handle (scenes.js:620-629): the two ball joints' constraint indices, and the
+    limit's and motor's (None when absent)."""
+    joints: tuple
+    limit: int | None = None
+    motor: int | None = None
+
+
+def _angular_options(kind, axisA=(0, 1, 0), axisB=(0, 1, 0), speed=1.0, maxTorque=100.0, minAngle=-math.pi,
+                     maxAngle=math.pi) -> dict:
+    """angularConstraintOptions (src/gpu/angularConstraints.js:87-120): unit axes, a finite speed
+    and nonnegative torque bound, angles ordered within [-pi, pi]."""
+    def unit(v):
+        a = [float(x) for x in v]
+        ln = math.hypot(*a) if len(a) == 3 else 0.0
+        if len(a) != 3 or not all(math.isfinite(x) for x in a) or ln < 1e-8:
+            raise ValueError("Angular axis requires three finite, nonzero components")
+        return [x / ln for x in a]
+
+    speed, maxTorque = float(speed), float(maxTorque)
+    if not math.isfinite(speed) or not math.isfinite(maxTorque) or maxTorque < 0:
+        raise ValueError("Motor speed must be finite and maxTorque nonnegative")
+    minAngle, maxAngle = float(minAngle), float(maxAngle)
+    if (not math.isfinite(minAngle) or not math.isfinite(maxAngle) or minAngle < -math.pi or maxAngle > math.pi
+            or minAngle > maxAngle):
+        raise ValueError("Hinge angles must be ordered within -PI..PI radians")
+    return {"type": kind, "axisA": unit(axisA), "axisB": unit(axisB), "speed": speed, "maxTorque": maxTorque,
+            "minAngle": minAngle, "maxAngle": maxAngle}
 
 
 def _vector(v, n, name):
@@ -355,30 +392,43 @@ class AvbdScene3D:
         return self._b.joint(a, b, _vector(anchorA, 3, "anchorA"), _vector(anchorB, 3, "anchorB"),
                              linearStiffness, angularStiffness, frac)
 
-    def addHinge(self, a, b, anchorA=(0, 0, 0), anchorB=(0, 0, 0), axisA=(0, 1, 0), axisB=(0, 1, 0), span=1.0,
-                 **options):
-        """A hinge as two ball joints span apart along the axis (scenes.js:587-601); returns their
-        constraint indices. Angle limits and motors (angular constraints) are not supported here."""
+    def addMotor(self, a, b, axisA=(0, 1, 0), axisB=(0, 1, 0), speed=1.0, maxTorque=100.0) -> int:
+        """A torque-limited motor turning b about the hinge axis relative to a at `speed` rad/s
+        (scenes.js:575-582); returns its constraint index."""
         self._editable()
         self._check(a, b)
-        if any(k in options for k in ("minAngle", "maxAngle", "motor")):
-            raise ValueError("hinge angle limits and motors are not supported by the gb300 backend")
+        o = _angular_options("motor", axisA, axisB, speed, maxTorque)
+        return self._b.angular(KIND_MOTOR, a, b, o["axisA"], o["axisB"], o["speed"], o["maxTorque"])
+
+    def addHinge(self, a, b, anchorA=(0, 0, 0), anchorB=(0, 0, 0), axisA=(0, 1, 0), axisB=(0, 1, 0), span=1.0,
+                 minAngle=None, maxAngle=None, motor=None, **options) -> "Hinge":
+        """Two ball joints span apart along the axis, with optional angle stops and a motor
+        (scenes.js:587-630). Anchors and axes are body-local, except the first endpoint's when a
+        is None (world frame)."""
+        self._editable()
+        self._check(a, b)
         if options:
             raise ValueError(f"unknown hinge option {next(iter(options))}")
+        lim = _angular_options("limit", axisA, axisB, minAngle=-math.pi if minAngle is None else minAngle,
+                               maxAngle=math.pi if maxAngle is None else maxAngle)
         span = _positive(span, "span")
-
-        def unit(v):
-            v = _vector(v, 3, "axis")
-            ln = math.sqrt(sum(x * x for x in v))
-            if ln < 1e-8:
-                raise ValueError("Angular axis requires three finite, nonzero components")
-            return [x / ln for x in v]
-
-        ua, ub = unit(axisA), unit(axisB)
+        ua, ub = lim["axisA"], lim["axisB"]
         aa, bb = _vector(anchorA, 3, "anchorA"), _vector(anchorB, 3, "anchorB")
-        return tuple(self.addJoint(a, b, [aa[i] + sign * span * 0.5 * ua[i] for i in range(3)],
-                                   [bb[i] + sign * span * 0.5 * ub[i] for i in range(3)])
-                     for sign in (-1, 1))
+        joints = tuple(self.addJoint(a, b, [aa[i] + sign * span * 0.5 * ua[i] for i in range(3)],
+                                     [bb[i] + sign * span * 0.5 * ub[i] for i in range(3)])
+                       for sign in (-1, 1))
+        limit = None
+        if minAngle is not None or maxAngle is not None:
+            limit = self._b.angular(KIND_LIMIT, a, b, ua, ub, lim["minAngle"], lim["maxAngle"])
+        drive = None
+        if motor is not None:
+            m = dict(motor)
+            unknown = set(m) - {"speed", "maxTorque", "axisA", "axisB"}
+            if unknown:
+                raise ValueError(f"unknown motor option {sorted(unknown)[0]}")
+            drive = self.addMotor(a, b, m.get("axisA", ua), m.get("axisB", ub), m.get("speed", 1.0),
+                                  m.get("maxTorque", 100.0))
+        return Hinge(joints, limit, drive)
 
     def addSpring(self, a, b, anchorA=(0, 0, 0), anchorB=(0, 0, 0), stiffness=1000.0, rest=-1.0) -> int:
         self._editable()

@@ -38,6 +38,7 @@
 
 #include "../../include/avbd_gb300.h"
 #include "engine.cuh"
+#include "angular.cuh"
 
 using namespace avbd;
 
@@ -617,10 +618,28 @@ class Arena {
     }
     for (int c = 0; c < d.n_cons; c++) {
       int k = d.cons_kind[c];
-      if (k != AVBD_CONS_JOINT && k != AVBD_CONS_SPRING && k != AVBD_CONS_IGNORE) throw Error(AVBD_E_INVALID, "unknown constraint kind");
+      if (k != AVBD_CONS_JOINT && k != AVBD_CONS_SPRING && k != AVBD_CONS_IGNORE && k != AVBD_CONS_MOTOR && k != AVBD_CONS_LIMIT)
+        throw Error(AVBD_E_INVALID, "unknown constraint kind");
       int a = d.cons_a[c], b = d.cons_b[c];
       if (b < 0 || b >= d.n_bodies || a < -1 || a >= d.n_bodies || a == b) throw Error(AVBD_E_INVALID, "constraint bodies out of range");
-      if (a < 0 && k != AVBD_CONS_JOINT) throw Error(AVBD_E_INVALID, "only joints may attach to the world");
+      if (a < 0 && (k == AVBD_CONS_SPRING || k == AVBD_CONS_IGNORE)) throw Error(AVBD_E_INVALID, "only joints may attach to the world");
+      if (k == AVBD_CONS_MOTOR || k == AVBD_CONS_LIMIT) checkAngular(k, d.cons_ra + 3 * c, d.cons_rb + 3 * c, d.cons_p0[c], d.cons_p1[c]);
+    }
+  }
+
+  // angularConstraintOptions (src/gpu/angularConstraints.js:87-120): finite nonzero axes; a
+  // finite motor speed and a nonnegative finite torque bound; limits ordered within [-pi, pi].
+  static void checkAngular(int k, const float* ra, const float* rb, float p0, float p1) {
+    for (const float* v : {ra, rb}) {
+      if (!(std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2])) ||
+          !(double(v[0]) * v[0] + double(v[1]) * v[1] + double(v[2]) * v[2] >= 1e-16))
+        throw Error(AVBD_E_INVALID, "Angular axis requires three finite, nonzero components");
+    }
+    if (k == AVBD_CONS_MOTOR) {
+      if (!std::isfinite(p0) || !std::isfinite(p1) || p1 < 0.f)
+        throw Error(AVBD_E_INVALID, "Motor speed must be finite and maxTorque nonnegative");
+    } else if (!(p0 >= -ANG_PI && p1 <= ANG_PI && p0 <= p1)) {
+      throw Error(AVBD_E_INVALID, "Hinge angles must be ordered within -PI..PI radians");
     }
   }
 
@@ -919,6 +938,7 @@ class Arena {
     if (nj) {
       std::vector<int2> jab(nj);
       std::vector<float4> jra(nj), jrb(nj), jst(nj), jz(nj, make_float4(0, 0, 0, 0)), jq(nj, make_float4(0, 0, 0, 1));
+      std::vector<float4> jpl(nj, make_float4(0, 0, 0, 0));
       std::vector<int> jbr(nj, 0);
       size_t j = 0;
       for (int c = 0; c < d.n_cons; c++) {
@@ -927,20 +947,27 @@ class Arena {
         const int a = d.cons_a[c] >= 0 ? int(off) + d.cons_a[c] : -1;
         const int b = int(off) + d.cons_b[c];
         jab[j] = make_int2(a, b);
-        int kk = kind == AVBD_CONS_JOINT ? KIND_JOINT : KIND_SPRING;
+        const bool angular = kind == AVBD_CONS_MOTOR || kind == AVBD_CONS_LIMIT;
+        int kk = kind == AVBD_CONS_JOINT ? KIND_JOINT
+                 : kind == AVBD_CONS_SPRING ? KIND_SPRING
+                 : kind == AVBD_CONS_MOTOR  ? KIND_MOTOR
+                                            : KIND_LIMIT;
         float kf;
         std::memcpy(&kf, &kk, 4);
         jra[j] = make_float4(d.cons_ra[3 * c], d.cons_ra[3 * c + 1], d.cons_ra[3 * c + 2], kf);
         jrb[j] = make_float4(d.cons_rb[3 * c], d.cons_rb[3 * c + 1], d.cons_rb[3 * c + 2], kind == AVBD_CONS_SPRING ? d.cons_p1[c] : 0.f);
         jst[j] = kind == AVBD_CONS_JOINT ? make_float4(d.cons_p0[c], d.cons_p1[c], d.cons_p2[c], 0.f)
+                 : angular               ? make_float4(d.cons_p0[c], d.cons_p1[c], INFINITY, 0.f)
                                          : make_float4(d.cons_p0[c], 0.f, INFINITY, 0.f);
+        if (angular) jpl[j] = make_float4(ANGULAR_PENALTY0, ANGULAR_PENALTY0, 0.f, 0.f);
         j++;
       }
       put(J.ab + joff, jab.data(), nj * 8);
       put(J.rA + joff, jra.data(), nj * 16);
       put(J.rB + joff, jrb.data(), nj * 16);
       put(J.stiff + joff, jst.data(), nj * 16);
-      for (float4* q : {J.penLin, J.penAng, J.lamLin, J.lamAng, J.C0Lin, J.C0Ang}) put(q + joff, jz.data(), nj * 16);
+      put(J.penLin + joff, jpl.data(), nj * 16);
+      for (float4* q : {J.penAng, J.lamLin, J.lamAng, J.C0Lin, J.C0Ang}) put(q + joff, jz.data(), nj * 16);
       put(J.restQ + joff, jq.data(), nj * 16);
       put(J.broken + joff, jbr.data(), nj * 4);
     }
@@ -1545,6 +1572,17 @@ class Arena {
     for (size_t j = 0; j < nj; j++) {
       float* o = out + 32 * j;
       const float4 ra = f[0][j], rb = f[1][j], st = f[2][j];
+      int kind;
+      std::memcpy(&kind, &ra.w, 4);
+      if (kind == KIND_MOTOR || kind == KIND_LIMIT) {  // src/native/cpu/world.js:622-636
+        const float4 pl = f[3][j], ll = f[5][j], c0 = f[7][j], c1 = f[8][j];
+        const float rec[32] = {pl.x, pl.y, 0.f, broken[j] ? 0.f : 1.f, 0.f, 0.f, 0.f, 0.f,
+                               ll.x, ll.y, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f,
+                               c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w,
+                               ra.x, ra.y, ra.z, st.x, rb.x, rb.y, rb.z, st.y};
+        std::memcpy(o, rec, sizeof(rec));
+        continue;
+      }
       const float4 blocks[6] = {f[3][j], f[4][j], f[5][j], f[6][j], f[7][j], f[8][j]};
       for (int b = 0; b < 6; b++) {
         o[4 * b] = blocks[b].x;
@@ -1603,6 +1641,56 @@ class Arena {
     WorldDev& D = W[w].dev;
     D.flags = any ? (D.flags | FLAG_RESTITUTION) : (D.flags & ~FLAG_RESTITUTION);
     uploadWorldDev(w);
+    flush();
+    wakeWorld(w);
+  }
+
+  // setMotor (src/gpu/appGpuSolver3D.js:547-562, src/native/cpu/world.js:360-388): a new speed
+  // and/or torque bound of motor `slot` (joint index); the world wakes. mask bit 0: speed, bit 1:
+  // torque bound.
+  void setMotor(int w, int slot, int mask, float speed, float maxTorque) {
+    if (w < 0 || w >= maxWorlds || !W[w].live) throw Error(AVBD_E_INVALID, "no such world");
+    flushEdits(w);
+    const WorldRec& R = resident(w);
+    if (slot < 0 || slot >= R.nJoints) throw Error(AVBD_E_INVALID, "Motor needs an active motor slot");
+    const size_t j = size_t(R.dev.jointOff) + size_t(slot);
+    const float4 ra = fetch(J.rA, j, 1)[0];
+    float4 st = fetch(J.stiff, j, 1)[0];
+    int kind;
+    std::memcpy(&kind, &ra.w, 4);
+    if (kind != KIND_MOTOR) throw Error(AVBD_E_INVALID, "Motor needs an active motor slot");
+    if ((mask & 1) && !std::isfinite(speed)) throw Error(AVBD_E_INVALID, "Motor speed must be finite");
+    if ((mask & 2) && !(std::isfinite(maxTorque) && maxTorque >= 0.f)) throw Error(AVBD_E_INVALID, "maxTorque must be nonnegative");
+    if (mask & 1) st.x = speed;
+    if (mask & 2) st.y = maxTorque;
+    put(J.stiff + j, &st, 16);
+    flush();
+    wakeWorld(w);
+  }
+
+  // releaseJoints (src/native/cpu/world.js:397-410, src/vendor/three-avbd-lib/solver3D.ts:1173-1193):
+  // the joints, springs or angular rows at `slots` stop acting for good: marked broken (no rows,
+  // no island link, their bodies collide again from the next step) with their penalties and
+  // lambdas zeroed; the world wakes.
+  void releaseJoints(int w, const int32_t* slots, int n) {
+    if (w < 0 || w >= maxWorlds || !W[w].live) throw Error(AVBD_E_INVALID, "no such world");
+    if (n < 0) throw Error(AVBD_E_INVALID, "negative count");
+    flushEdits(w);
+    const WorldRec& R = resident(w);
+    for (int k = 0; k < n; k++)
+      if (slots[k] < 0 || slots[k] >= R.nJoints) throw Error(AVBD_E_INVALID, "A live constraint slot is required");
+    if (n == 0) return;
+    const size_t off = size_t(R.dev.jointOff), nj = size_t(R.nJoints);
+    std::vector<int> broken;
+    getRange(broken, J.broken, off, nj);
+    for (float4* a : {J.penLin, J.penAng, J.lamLin, J.lamAng}) {
+      std::vector<float4> v;
+      getRange(v, a, off, nj);
+      for (int k = 0; k < n; k++) v[slots[k]] = make_float4(0.f, 0.f, 0.f, 0.f);
+      putRange(a, off, v);
+    }
+    for (int k = 0; k < n; k++) broken[slots[k]] = 1;
+    putRange(J.broken, off, broken);
     flush();
     wakeWorld(w);
   }

@@ -459,6 +459,22 @@ int avbd_world_set_restitution(avbd_world* w, const uint32_t* indices, int32_t n
   API_END
 }
 
+int avbd_world_set_motor(avbd_world* w, int32_t slot, int32_t mask, float speed, float max_torque) {
+  API_BEGIN
+  REQUIRE(w, "null world");
+  bind(w->A->ctx);
+  w->A->setMotor(w->w, slot, mask, speed, max_torque);
+  API_END
+}
+
+int avbd_world_release_joints(avbd_world* w, const int32_t* slots, int32_t n) {
+  API_BEGIN
+  REQUIRE(w && (n == 0 || slots), "null argument");
+  bind(w->A->ctx);
+  w->A->releaseJoints(w->w, slots, n);
+  API_END
+}
+
 int avbd_world_cast(avbd_world* w, const float* queries, int32_t n, const avbd_cast_filter* filter, float* hits) {
   API_BEGIN
   REQUIRE(w && (n == 0 || (queries && hits)), "null argument");
@@ -733,6 +749,24 @@ int avbd_batch_read_joints(avbd_batch* b, int32_t world, float* out) {
   REQUIRE(world >= 0 && world < int32_t(b->worlds.size()), "world index out of range");
   bind(b->A->ctx);
   b->A->readJoints(b->worlds[world], out);
+  API_END
+}
+
+int avbd_batch_set_motor(avbd_batch* b, int32_t world, int32_t slot, int32_t mask, float speed, float max_torque) {
+  API_BEGIN
+  REQUIRE(b, "null batch");
+  REQUIRE(world >= 0 && world < int32_t(b->worlds.size()), "world index out of range");
+  bind(b->A->ctx);
+  b->A->setMotor(b->worlds[world], slot, mask, speed, max_torque);
+  API_END
+}
+
+int avbd_batch_release_joints(avbd_batch* b, int32_t world, const int32_t* slots, int32_t n) {
+  API_BEGIN
+  REQUIRE(b && (n == 0 || slots), "null argument");
+  REQUIRE(world >= 0 && world < int32_t(b->worlds.size()), "world index out of range");
+  bind(b->A->ctx);
+  b->A->releaseJoints(b->worlds[world], slots, n);
   API_END
 }
 

@@ -40,6 +40,11 @@ constexpr int SHAPE_BOX = 0;
 constexpr int SHAPE_SPHERE = 1;
 constexpr int KIND_JOINT = 0;
 constexpr int KIND_SPRING = 1;
+// Angular rows about a hinge axis (src/gpu/angularConstraints.js info types 3 and 4): a motor
+// driving the twist at a speed under a torque bound, or lower/upper angle stops. Their records
+// live in the joint arrays (angular.cuh gives the field map).
+constexpr int KIND_MOTOR = 3;
+constexpr int KIND_LIMIT = 4;
 
 constexpr int FLAG_MASS_PENALTY = 1;
 constexpr int FLAG_FACE_BIAS = 2;

@@ -36,6 +36,12 @@ typedef struct avbd_batch avbd_batch;
 #define AVBD_CONS_JOINT 0
 #define AVBD_CONS_SPRING 1
 #define AVBD_CONS_IGNORE 2
+/* Angular rows about a hinge axis (scenes.js:575-630 addMotor / addHinge minAngle, maxAngle;
+ * src/gpu/angularConstraints.js info types 3 and 4): cons_ra / cons_rb carry the unit axis in the
+ * frames of a and b (a = -1: world frame); a motor's cons_p0 / cons_p1 are its speed (rad/s) and
+ * torque bound, a limit's the lower and upper angle within [-pi, pi]. */
+#define AVBD_CONS_MOTOR 3
+#define AVBD_CONS_LIMIT 4
 
 /* Solver parameters: reference/three-avbd/src/avbd3d/ref/solver.ts:347-359 and
  * src/native/cpu/cpuSolver3D.ts:46-79 (massPenalty, faceBias, up). */
@@ -88,10 +94,12 @@ typedef struct avbd_scene_desc {
   const int32_t* cons_kind;      /* n_cons AVBD_CONS_* in creation order */
   const int32_t* cons_a;         /* -1 = world (joints) */
   const int32_t* cons_b;
-  const float* cons_ra;          /* 3 n_cons body-local anchor (world point when a = -1) */
+  const float* cons_ra;          /* 3 n_cons body-local anchor (world point when a = -1); motor/limit: axis */
   const float* cons_rb;          /* 3 n_cons */
-  const float* cons_p0;          /* joint: linear stiffness (INFINITY = hard); spring: stiffness */
-  const float* cons_p1;          /* joint: angular stiffness; spring: rest length (-1: current) */
+  const float* cons_p0;          /* joint: linear stiffness (INFINITY = hard); spring: stiffness;
+                                    motor: speed; limit: lower angle */
+  const float* cons_p1;          /* joint: angular stiffness; spring: rest length (-1: current);
+                                    motor: torque bound; limit: upper angle */
   const float* cons_p2;          /* joint: fracture threshold on |lambda_ang| */
   const float* restitution;      /* n [0] restitution 0..1 (addBox/addSphere option; the velocity
                                     bounce pass of src/native/cpu/restitution.js runs when > 0) */
@@ -268,6 +276,14 @@ int avbd_world_set_filters(avbd_world* w, const uint32_t* indices, int32_t n, co
 /* setRestitution per body (src/native/cpu/world.js:343-351; editBodies' restitution property):
  * values in [0, 1]; the world wakes. */
 int avbd_world_set_restitution(avbd_world* w, const uint32_t* indices, int32_t n, const float* values);
+/* setMotor(slot, {speed, maxTorque}) (src/gpu/appGpuSolver3D.js:547-562, src/native/cpu/world.js:
+ * 360-388): slot is the joint index of an AVBD_CONS_MOTOR constraint; mask bit 0 sets the speed,
+ * bit 1 the torque bound (finite, >= 0). The world wakes. */
+int avbd_world_set_motor(avbd_world* w, int32_t slot, int32_t mask, float speed, float max_torque);
+/* releaseJoints(slots) (src/native/cpu/world.js:397-410; src/vendor/three-avbd-lib/solver3D.ts:
+ * 1173-1193): the joints, springs or angular rows at the given joint indices stop acting (their
+ * records read as released, their bodies collide again); the world wakes. */
+int avbd_world_release_joints(avbd_world* w, const int32_t* slots, int32_t n);
 
 /* Load per-body sleep flags and quiet times (state import for one-step comparisons; NULL skips). */
 int avbd_world_import_sleep_state(avbd_world* w, const int32_t* asleep, const float* quiet_time);
@@ -296,6 +312,10 @@ int avbd_batch_set_velocities(avbd_batch* b, const uint32_t* indices, int32_t n,
 int avbd_batch_edit(avbd_batch* b, int32_t world, const uint32_t* records, int32_t n);
 /* Joint records of world `world` of the batch (as avbd_world_read_joints). */
 int avbd_batch_read_joints(avbd_batch* b, int32_t world, float* out);
+/* setMotor for world `world` of the batch (as avbd_world_set_motor). */
+int avbd_batch_set_motor(avbd_batch* b, int32_t world, int32_t slot, int32_t mask, float speed, float max_torque);
+/* releaseJoints for world `world` of the batch (as avbd_world_release_joints). */
+int avbd_batch_release_joints(avbd_batch* b, int32_t world, const int32_t* slots, int32_t n);
 /* Shape casts against world `world` of the batch (as avbd_world_cast). */
 int avbd_batch_cast(avbd_batch* b, int32_t world, const float* queries, int32_t n, const avbd_cast_filter* filter,
                     float* hits);

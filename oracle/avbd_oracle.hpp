@@ -249,6 +249,14 @@ template <class R> struct Force {
   bool restFrame = false;  // app mode: angular rows relative to the captured rest rotation
   R restQ[4] = {0, 0, 0, 1};
   R rest = 0, stiffness = 0;  // spring
+  // angular rows (src/gpu/angularConstraints.js): 3 motor, 4 limit, 0 none. rA / rB hold the axis
+  // in A's / B's frame; p0, p1 the speed and torque bound (motor) or the lower and upper angle
+  // (limit); ta, tb the reference tangents; c0 the rows' step-start values; penLin[0..1] and
+  // lamLin[0..1] the rows' penalty and lambda.
+  int angular = 0;
+  R p0 = 0, p1 = 0;
+  R ta[3] = {0, 0, 0}, tb[3] = {0, 0, 0};
+  R c0[2] = {0, 0};
 };
 
 struct RawContactD;  // fwd
@@ -351,6 +359,19 @@ template <class R> class Solver {
     return id;
   }
   int addIgnore(int a, int b) { return newForce(F_IGNORE, a, b); }
+  // addMotor / the limit row of addHinge (scenes.js:575-630) as src/gpu/appGpuSolver3D.js:500-526
+  // installs them: initial row penalties 1000, frames captured from the poses at creation.
+  int addAngular(int a, int b, int kind, const R* axisA, const R* axisB, R p0, R p1) {
+    int id = newForce(F_JOINT, a, b);
+    Force<R>& f = *store[id];
+    f.angular = kind;
+    for (int i = 0; i < 3; i++) { f.rA[i] = axisA[i]; f.rB[i] = axisB[i]; }
+    f.p0 = p0;
+    f.p1 = p1;
+    f.penLin[0] = f.penLin[1] = R(1000);
+    angularCapture(f);
+    return id;
+  }
 
   // cpuPhysics3D.js:47-66 (captureCpuFrame3D) applied by prepareCpuForces3D to joints with
   // angular stiffness > 0: angular rows measure rotation relative to the captured rest frame.
@@ -398,6 +419,7 @@ template <class R> class Solver {
     }
   }
   bool jointInitialize(Force<R>& f) {
+    if (f.angular) return angularInitialize(f);
     jointEvalLin(f, f.C0Lin);
     jointEvalAng(f, f.C0Ang);
     for (int i = 0; i < 3; i++) {
@@ -420,6 +442,10 @@ template <class R> class Solver {
   static bool isInf(R x) { return std::isinf(x) && x > 0; }
 
   void jointPrimal(const Force<R>& f, int body, Sys& sys) const {
+    if (f.angular) {
+      angularPrimal(f, body, sys);
+      return;
+    }
     const bool isA = body == f.a;
     R K[9], C[3], F[3], r[3], jLin[9], jAng[9], jLinT[9], jAngT[9], jAngTk[9], tmp[9], H[9], gs[9];
     if (Mt::lengthSq(f.penLin) > 0) {
@@ -485,6 +511,10 @@ template <class R> class Solver {
     }
   }
   void jointDual(Force<R>& f) {
+    if (f.angular) {
+      angularDual(f);
+      return;
+    }
     R K[9], C[3], F[3], r[3];
     if (Mt::lengthSq(f.penLin) > 0) {
       Mt::diagonal(K, f.penLin[0], f.penLin[1], f.penLin[2]);
@@ -516,6 +546,147 @@ template <class R> class Solver {
       for (int i = 0; i < 3; i++) f.penLin[i] = f.penAng[i] = f.lamLin[i] = f.lamAng[i] = 0;
       f.broken = true;
     }
+  }
+  // setMotor (src/native/cpu/world.js:360-388) of the motor with joint id `jid`; mask bit 0:
+  // speed, bit 1: torque bound. Returns false when jid is not a motor.
+  bool setMotor(int jid, int mask, R speed, R torque) {
+    for (auto& p : store) {
+      Force<R>& f = *p;
+      if (f.jid != jid || f.angular != 3) continue;
+      if (mask & 1) f.p0 = speed;
+      if (mask & 2) f.p1 = torque;
+      return true;
+    }
+    return false;
+  }
+  // releaseJoints (src/native/cpu/world.js:397-410): the constraint with joint id `jid` stops
+  // acting at once (broken, state zeroed, gone from the body and solver lists).
+  void releaseJoint(int jid) {
+    for (size_t id = 0; id < store.size(); id++) {
+      Force<R>& f = *store[id];
+      if (f.jid != jid || f.broken) continue;
+      f.broken = true;
+      for (int i = 0; i < 3; i++) f.penLin[i] = f.penAng[i] = f.lamLin[i] = f.lamAng[i] = 0;
+      unlinkFromBodies(int(id));
+      forces.erase(std::remove(forces.begin(), forces.end(), int(id)), forces.end());
+    }
+  }
+  // ------------------------------------------------------------ angular rows
+  // (src/gpu/angularConstraints.js:16-64, frames of src/gpu/angularFrames.wgsl)
+  // atan2 from the half-angle identity atan(t) = 2 atan(t / (1 + sqrt(1 + t^2))) applied twice
+  // (|t| <= tan(pi/16) after it) and the odd Taylor series of atan through t^9; +, -, *, / and
+  // sqrt only, so the float instance repeats the engine's bits.
+  static R angleAtan2(R y, R x) {
+    const R ax = std::fabs(x), ay = std::fabs(y);
+    const R hi = Mt::mx(ax, ay), lo = Mt::mn(ax, ay);
+    if (!(hi > 0)) return 0;
+    const R one = 1, t = lo / hi;
+    const R u = t / (one + std::sqrt(one + t * t));
+    const R v = u / (one + std::sqrt(one + u * u));
+    const R w = v * v;
+    const R s = v * (one + w * (R(-1) / R(3) + w * (R(1) / R(5) + w * (R(-1) / R(7) + w * (R(1) / R(9))))));
+    R a = R(4) * s;
+    if (ay > ax) a = R(1.57079632679489661923) - a;
+    if (x < 0) a = R(3.14159265358979323846) - a;
+    return y < 0 ? -a : a;
+  }
+  // atan2(sin d, cos d) for d in [-2 pi, 2 pi]
+  static R angleWrap(R d) {
+    const R pi = R(3.14159265358979323846), twoPi = R(6.28318530717958647692);
+    return d > pi ? d - twoPi : (d < -pi ? d + twoPi : d);
+  }
+  static void angleTangent(R* o, const R* n) {
+    R t[3];
+    if (std::fabs(n[0]) > std::fabs(n[2])) Mt::set3(t, -n[1], n[0], 0);
+    else Mt::set3(t, 0, -n[2], n[1]);
+    Mt::div3(o, t, Mt::length(t));
+  }
+  const R* rotOfA(const Force<R>& f) const {
+    static const R IDENTITY[4] = {0, 0, 0, 1};
+    return f.a >= 0 ? bodies[f.a].q : IDENTITY;
+  }
+  void angularCapture(Force<R>& f) {
+    angleTangent(f.ta, f.rA);
+    R world[3], nb[3], t[3], p[3];
+    Mt::rotate(world, rotOfA(f), f.ta);
+    Mt::div3(nb, f.rB, Mt::length(f.rB));
+    Mt::rotateInv(t, bodies[f.b].q, world);
+    Mt::scale3(p, nb, Mt::dot(t, nb));
+    Mt::sub3(t, t, p);
+    if (Mt::length(t) < R(1.0e-6)) {
+      if (std::fabs(nb[0]) > std::fabs(nb[2])) Mt::set3(t, -nb[1], nb[0], 0);
+      else Mt::set3(t, 0, -nb[2], nb[1]);
+    }
+    Mt::div3(f.tb, t, Mt::length(t));
+  }
+  R angularAngle(const Force<R>& f, R* axis) const {
+    const R* qa = rotOfA(f);
+    R wa[3], wb[3], c[3];
+    Mt::rotate(axis, qa, f.rA);
+    Mt::rotate(wa, qa, f.ta);
+    Mt::rotate(wb, bodies[f.b].q, f.tb);
+    Mt::cross(c, wa, wb);
+    return angleAtan2(Mt::dot(axis, c), Mt::dot(wa, wb));
+  }
+  void angularRows(const Force<R>& f, R angle, R* C) const {
+    if (f.angular == 3) {
+      C[0] = angleWrap(angle - f.c0[0]) - f.p0 * dt;
+      C[1] = 0;
+    } else {
+      C[0] = (angle - f.p0) - alpha * f.c0[0];
+      C[1] = (angle - f.p1) - alpha * f.c0[1];
+    }
+  }
+  void angularForce(const Force<R>& f, const R* C, R* F) const {
+    const R fx = f.penLin[0] * C[0] + f.lamLin[0], fy = f.penLin[1] * C[1] + f.lamLin[1];
+    if (f.angular == 3) {
+      F[0] = Mt::clamp(fx, -f.p1, f.p1);
+      F[1] = 0;
+    } else {
+      F[0] = Mt::mn(R(0), fx);
+      F[1] = Mt::mx(R(0), fy);
+    }
+  }
+  bool angularInitialize(Force<R>& f) {
+    R axis[3];
+    const R angle = angularAngle(f, axis);
+    const bool motor = f.angular == 3;
+    f.c0[0] = motor ? angle : Mt::mn(R(0), angle - f.p0);
+    f.c0[1] = motor ? R(0) : Mt::mx(R(0), angle - f.p1);
+    const R decay = alpha * gamma;
+    for (int i = 0; i < 2; i++) {
+      f.lamLin[i] = f.lamLin[i] * decay;
+      f.penLin[i] = Mt::clamp(f.penLin[i] * gamma, R(PENALTY_MIN), R(PENALTY_MAX));
+    }
+    return !f.broken;
+  }
+  void angularPrimal(const Force<R>& f, int body, Sys& sys) const {
+    const bool motor = f.angular == 3;
+    if (motor && f.p1 == 0) return;
+    R axis[3], C[2], F[2];
+    const R angle = angularAngle(f, axis);
+    angularRows(f, angle, C);
+    angularForce(f, C, F);
+    if (body == f.a) Mt::neg3(axis, axis);
+    for (int r = 0; r < 2; r++) {
+      const bool on = r == 0 ? (motor || F[0] != 0) : (!motor && F[1] != 0);
+      if (!on) continue;
+      for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) sys.lhsAng[i * 3 + j] += (axis[i] * axis[j]) * f.penLin[r];
+      for (int i = 0; i < 3; i++) sys.rhsAng[i] += axis[i] * F[r];
+    }
+  }
+  void angularDual(Force<R>& f) {
+    const bool motor = f.angular == 3;
+    R axis[3], C[2], F[2];
+    const R angle = angularAngle(f, axis);
+    angularRows(f, angle, C);
+    angularForce(f, C, F);
+    f.lamLin[0] = F[0];
+    f.lamLin[1] = F[1];
+    const R vx = motor ? std::fabs(C[0]) : Mt::mx(R(0), -C[0]), vy = motor ? std::fabs(C[1]) : Mt::mx(R(0), C[1]);
+    f.penLin[0] = Mt::mn(f.penLin[0] + vx * betaAng, R(PENALTY_MAX));
+    f.penLin[1] = Mt::mn(f.penLin[1] + vy * betaAng, R(PENALTY_MAX));
   }
   // ------------------------------------------------------------ springs (forces.ts:260-296)
   void springPrimal(const Force<R>& f, int body, Sys& sys) const {

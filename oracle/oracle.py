@@ -84,6 +84,10 @@ def lib():
         L.oracle_world_sleep_after.argtypes = [C.c_void_p]
         L.oracle_worlds_step_parallel.argtypes = [C.POINTER(C.c_void_p), C.c_int, C.c_int, C.c_int]
         L.oracle_worlds_step_parallel.restype = C.c_int
+        L.oracle_angle_atan2.argtypes = [C.c_int, _dp, _dp, _dp, C.c_int]
+        L.oracle_world_set_motor.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_double]
+        L.oracle_world_set_motor.restype = C.c_int
+        L.oracle_world_release_joints.argtypes = [C.c_void_p, _ip, C.c_int]
         _lib = L
     return _lib
 
@@ -251,11 +255,32 @@ class OracleWorld:
         """The sleeping pass alone (``step`` runs it after the solve when sleeping is on)."""
         lib().oracle_world_sleep_after(self.h)
 
+    def set_motor(self, jid, speed=None, max_torque=None):
+        """setMotor of the motor with joint slot `jid` (speed and/or torque bound)."""
+        mask = (1 if speed is not None else 0) | (2 if max_torque is not None else 0)
+        ok = lib().oracle_world_set_motor(self.h, int(jid), mask, float(speed or 0.0), float(max_torque or 0.0))
+        if not ok:
+            raise ValueError("Motor needs an active motor slot")
+
+    def release_joints(self, jids):
+        """releaseJoints of these joint slots."""
+        j = np.ascontiguousarray(np.asarray(jids, dtype=np.int32).reshape(-1))
+        lib().oracle_world_release_joints(self.h, _ptr(j, C.c_int), j.size)
+
     def edit(self, records):
         """Apply body command records (n x 12 uint32 words, ``src/gpu/bodyCommands2D.js``
         layout) with the CPU world's flushEdits semantics (``src/native/cpu/world.js:229-300``)."""
         r = np.ascontiguousarray(records, dtype=np.uint32).reshape(-1, 12)
         lib().oracle_world_edit(self.h, r.ctypes.data_as(C.POINTER(C.c_uint32)), int(r.shape[0]))
+
+
+def angle_atan2(y, x, fp64=True):
+    """The angular rows' atan2 (half-angle reductions and a Taylor series), elementwise."""
+    y = np.ascontiguousarray(np.asarray(y, dtype=np.float64).reshape(-1))
+    x = np.ascontiguousarray(np.asarray(x, dtype=np.float64).reshape(-1))
+    out = np.zeros_like(y)
+    lib().oracle_angle_atan2(1 if fp64 else 0, _ptr(y, C.c_double), _ptr(x, C.c_double), _ptr(out, C.c_double), y.size)
+    return out
 
 
 def step_parallel(worlds, steps, threads=0) -> int:

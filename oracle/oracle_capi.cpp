@@ -13,7 +13,7 @@ using namespace avbd_oracle;
 
 // Constraint kinds, in the scene's creation order (the order matters: it is the order of the
 // reference's force lists).
-enum { K_JOINT = 0, K_SPRING = 1, K_IGNORE = 2 };
+enum { K_JOINT = 0, K_SPRING = 1, K_IGNORE = 2, K_MOTOR = 3, K_LIMIT = 4 };
 
 struct oracle_scene {
   int n_bodies;
@@ -103,6 +103,8 @@ template <class R> static Solver<R>* build(const oracle_scene* s, const oracle_p
     for (int k = 0; k < 3; k++) { ra[k] = R(s->ra[3 * c + k]); rb[k] = R(s->rb[3 * c + k]); }
     if (s->kind[c] == K_JOINT) w->addJoint(s->ca[c], s->cb[c], ra, rb, R(s->p0[c]), R(s->p1[c]), R(s->p2[c]));
     else if (s->kind[c] == K_SPRING) w->addSpring(s->ca[c], s->cb[c], ra, rb, R(s->p0[c]), R(s->p1[c]));
+    else if (s->kind[c] == K_MOTOR || s->kind[c] == K_LIMIT)
+      w->addAngular(s->ca[c], s->cb[c], s->kind[c], ra, rb, R(s->p0[c]), R(s->p1[c]));
     else w->addIgnore(s->ca[c], s->cb[c]);
   }
   if (w->app) w->prepareApp();
@@ -366,6 +368,21 @@ template <class R> static void import_state(Solver<R>& S, const oracle_state* st
 extern "C" void oracle_world_import(void* h, const oracle_state* st) { DISPATCH(h, import_state(S, st)); }
 
 // src/native/cpu/world.js:229-300 flushEdits over n 12-word body command records
+extern "C" int oracle_world_set_motor(void* h, int jid, int mask, double speed, double torque) {
+  int ok = 0;
+  DISPATCH(h, ok = S.setMotor(jid, mask, decltype(S.dt)(speed), decltype(S.dt)(torque)) ? 1 : 0);
+  return ok;
+}
+extern "C" void oracle_world_release_joints(void* h, const int32_t* jids, int n) {
+  DISPATCH(h, for (int k = 0; k < n; k++) S.releaseJoint(jids[k]));
+}
+
+// The angular rows' atan2 restatement, elementwise (fp64 != 0: double, else float).
+extern "C" void oracle_angle_atan2(int fp64, const double* y, const double* x, double* out, int n) {
+  for (int i = 0; i < n; i++)
+    out[i] = fp64 ? Solver<double>::angleAtan2(y[i], x[i]) : double(Solver<float>::angleAtan2(float(y[i]), float(x[i])));
+}
+
 extern "C" void oracle_world_edit(void* h, const uint32_t* records, int n) { DISPATCH(h, S.applyEdits(records, n)); }
 
 // Step many independent worlds in parallel with OpenMP (the multi-world CPU baseline).

@@ -181,15 +181,47 @@ def test_hinge_is_two_ball_joints_along_the_axis():
     sc = AvbdScene3D()
     a = sc.addBox([1, 1, 1], density=0, position=[0, 2, 0])
     b = sc.addBox([1, 1, 1], position=[0, 3.2, 0])
-    ids = sc.addHinge(a, b, anchorA=[0, 0.6, 0], anchorB=[0, -0.6, 0], axisA=[2, 0, 0], axisB=[1, 0, 0], span=0.8)
+    h = sc.addHinge(a, b, anchorA=[0, 0.6, 0], anchorB=[0, -0.6, 0], axisA=[2, 0, 0], axisB=[1, 0, 0], span=0.8)
     arr = sc.arrays()
-    assert ids == (0, 1) and list(arr.kind) == [0, 0]
+    assert h.joints == (0, 1) and h.limit is None and h.motor is None and list(arr.kind) == [0, 0]
     assert np.allclose(arr.ra, [[-0.4, 0.6, 0], [0.4, 0.6, 0]]) and np.allclose(arr.rb, [[-0.4, -0.6, 0], [0.4, -0.6, 0]])
     assert np.isinf(arr.p0).all() and np.all(arr.p1 == 0)
     with pytest.raises(ValueError):
-        sc.addHinge(a, b, minAngle=-1.0)
-    with pytest.raises(ValueError):
         sc.addHinge(a, b, axisA=[0, 0, 0])
+
+
+def test_hinge_limit_and_motor_records():
+    # scenes.js:587-630 and angularConstraintOptions (src/gpu/angularConstraints.js:87-120): the
+    # limit row (kind 4) carries the unit axes and the stops, the motor (kind 3) speed and torque
+    from avbd_gb300 import AvbdScene3D
+    sc = AvbdScene3D()
+    a = sc.addBox([1, 1, 1], density=0, position=[0, 2, 0])
+    b = sc.addBox([1, 1, 1], position=[0, 3.2, 0])
+    sc.ignoreCollision(a, b)
+    h = sc.addHinge(a, b, axisA=[0, 0, 3], axisB=[0, 0, 1], minAngle=-0.5, maxAngle=0.25,
+                    motor={"speed": 2.0, "maxTorque": 40.0})
+    m = sc.addMotor(None, b, axisA=[1, 0, 0], axisB=[1, 0, 0], speed=-1.0, maxTorque=0.0)
+    arr = sc.arrays()
+    assert h.joints == (1, 2) and h.limit == 3 and h.motor == 4 and m == 5
+    assert list(arr.kind) == [2, 0, 0, 4, 3, 3]
+    assert np.allclose(arr.ra[3], [0, 0, 1]) and np.allclose(arr.rb[3], [0, 0, 1])
+    assert (arr.p0[3], arr.p1[3]) == (-0.5, 0.25) and (arr.p0[4], arr.p1[4]) == (2.0, 40.0)
+    assert arr.ca[5] == -1 and (arr.p0[5], arr.p1[5]) == (-1.0, 0.0)
+    for bad in ({"minAngle": 0.5, "maxAngle": 0.25}, {"minAngle": -4.0}, {"maxAngle": 3.2},
+                {"motor": {"maxTorque": -1.0}}, {"motor": {"speed": float("inf")}}, {"motor": {"torque": 1.0}},
+                {"minAngle": float("nan")}):
+        with pytest.raises(ValueError):
+            sc.addHinge(a, b, **bad)
+    with pytest.raises(ValueError):
+        sc.addMotor(a, b, axisA=[0, 0, 0])
+    from avbd_gb300.pipeline import _motor_args, _motor_slot
+    assert _motor_slot(arr.kind, 4) == 3 and _motor_slot(arr.kind, 5) == 4
+    for c in (0, 1, 3, 6):
+        with pytest.raises(ValueError):
+            _motor_slot(arr.kind, c)
+    assert _motor_args(None, 5.0) == (2, 0.0, 5.0) and _motor_args(1.5, None) == (1, 1.5, 0.0)
+    with pytest.raises(ValueError):
+        _motor_args(None, -1.0)
 
 
 def test_spatial_sort_keeps_statics_first_and_remaps_constraints():
