@@ -338,6 +338,26 @@ napi_value SetRestitution(napi_env env, napi_callback_info info) {  // (w, Uint3
   CALL(avbd_world_set_restitution(w, idx, int32_t(n), e));
   return nullptr;
 }
+napi_value SetMotor(napi_env env, napi_callback_info info) {  // (w, slot, speed|undefined, maxTorque|undefined)
+  WORLD_ARG(4);
+  int32_t mask = 0;
+  double speed = 0, torque = 0;
+  napi_valuetype t;
+  napi_typeof(env, argv[2], &t);
+  if (t == napi_number) { napi_get_value_double(env, argv[2], &speed); mask |= 1; }
+  napi_typeof(env, argv[3], &t);
+  if (t == napi_number) { napi_get_value_double(env, argv[3], &torque); mask |= 2; }
+  CALL(avbd_world_set_motor(w, Int(env, argv[1]), mask, float(speed), float(torque)));
+  return nullptr;
+}
+napi_value ReleaseJoints(napi_env env, napi_callback_info info) {  // (w, Int32Array of joint slots)
+  WORLD_ARG(2);
+  const int32_t* slots;
+  size_t n;
+  if (!Typed(env, argv[1], &slots, &n)) return nullptr;
+  CALL(avbd_world_release_joints(w, slots, int32_t(n)));
+  return nullptr;
+}
 napi_value WatchContacts(napi_env env, napi_callback_info info) {  // (w, Uint32Array|null, maxPairs, maxEvents)
   WORLD_ARG(4);
   const uint32_t* idx;
@@ -540,7 +560,8 @@ napi_value Init(napi_env env, napi_value exports) {
              {"edit", Edit},                   {"flushEdits", FlushEdits},         {"readSelected", ReadSelected},
              {"readState", ReadState},         {"setPoses", SetPoses},             {"setVelocities", SetVelocities},
              {"readCounters", ReadCounters},   {"readJoints", ReadJoints},         {"setFilters", SetFilters},
-             {"setRestitution", SetRestitution}, {"watchContacts", WatchContacts}, {"readContactEvents", ReadContactEvents},
+             {"setRestitution", SetRestitution}, {"setMotor", SetMotor},         {"releaseJoints", ReleaseJoints},
+             {"watchContacts", WatchContacts}, {"readContactEvents", ReadContactEvents},
              {"resetContactHistory", ResetContactHistory}, {"cast", Cast},         {"setSleeping", SetSleeping},
              {"setSleepEnabled", SetSleepEnabled}, {"wakeAll", WakeAll},           {"sleepStats", SleepStats},
              {"createServer", CreateServer},   {"destroyServer", DestroyServer},   {"admit", Admit},

@@ -12,6 +12,7 @@
 import { createRequire } from "node:module";
 import { IgnoreCollision, Joint, Spring } from "../../../reference/three-avbd/src/avbd3d/ref/forces.ts";
 import { isSphere } from "../../../reference/three-avbd/src/avbd3d/shapes.ts";
+import { angularConstraintOptions, initialAngularConstraint } from "../../gpu/angularConstraints.js";
 import { installNativeRuntime } from "../runtime.js";
 
 const require = createRequire(import.meta.url);
@@ -98,7 +99,16 @@ export function packScene(scene, options = {}) {
   cons.forEach((f, c) => {
     a.consA[c] = f.bodyA ? slot.get(f.bodyA) : -1;
     a.consB[c] = slot.get(f.bodyB);
-    if (f instanceof Joint) {
+    const angular = f instanceof Joint ? initialAngularConstraint(f) : undefined;
+    if (angular) {
+      // addMotor / the limit row of addHinge (scenes.js:575-630): kinds 3 and 4 of the C ABI
+      const motor = angular.type === "motor";
+      a.consKind[c] = motor ? 3 : 4;
+      a.consRA.set(angular.axisA, 3 * c);
+      a.consRB.set(angular.axisB, 3 * c);
+      a.consP0[c] = motor ? angular.speed : angular.minAngle;
+      a.consP1[c] = motor ? angular.maxTorque : angular.maxAngle;
+    } else if (f instanceof Joint) {
       a.consKind[c] = 0;
       a.consRA.set(f.rA, 3 * c);
       a.consRB.set(f.rB, 3 * c);
@@ -230,6 +240,18 @@ class Gb300World {
   setRestitution(index, value) {
     this.assertLive();
     addon.setRestitution(this.handle, Uint32Array.of(index), Float32Array.of(value));
+  }
+  /** setMotor(slot, { speed, maxTorque }) (appGpuSolver3D.js:547-562): slot is the joint slot. */
+  setMotor(slot, options = {}) {
+    this.assertLive();
+    const o = angularConstraintOptions({ type: "motor", speed: options.speed ?? 0, maxTorque: options.maxTorque ?? 0 });
+    addon.setMotor(this.handle, slot, options.speed === undefined ? undefined : o.speed,
+      options.maxTorque === undefined ? undefined : o.maxTorque);
+  }
+  /** releaseJoints(slots) (src/native/cpu/world.js:397-410). */
+  releaseJoints(slots) {
+    this.assertLive();
+    addon.releaseJoints(this.handle, Int32Array.from(slots));
   }
   setSensor() {
     throw Error("triggers are not supported by the gb300 backend");
