@@ -561,6 +561,51 @@ class World:
         slots = _joint_slots(self._kinds, constraints)
         L.check(L.lib().avbd_world_release_joints(self._h, L.iptr(slots), int(slots.size)))
 
+    def disableConstraint(self, constraint):
+        """disableConstraint (src/native/cpu/world.js:400-410): releaseJoints of one constraint."""
+        self.releaseJoints([constraint])
+
+    def setSpringMaterial(self, constraint, breakStrain=None, breakForce=None):
+        """setSpringMaterial (src/gpu/appGpuSolver3D.js:810-835): new tear limits of a live spring
+        (positive, or math.inf for none); wakes the world."""
+        self._live()
+        from .scene import KIND_SPRING, spring_material
+        c = int(constraint)
+        if not 0 <= c < len(self._kinds) or self._kinds[c] != KIND_SPRING:
+            raise ValueError("Spring material requires an active spring slot")
+        m = spring_material(math.inf if breakStrain is None else breakStrain,
+                            math.inf if breakForce is None else breakForce)
+        mask = (1 if breakStrain is not None else 0) | (2 if breakForce is not None else 0)
+        slot = int(_joint_slots(self._kinds, [c])[0])
+        L.check(L.lib().avbd_world_set_spring_material(self._h, slot, mask, m["breakStrain"], m["breakForce"]))
+
+    def setWorldAnchor(self, constraint, point):
+        """setWorldAnchor (src/gpu/appGpuSolver3D.js:928-941): move the world point of a joint whose
+        first body is the world (a grab handle); wakes the world."""
+        self._live()
+        p = np.ascontiguousarray(np.asarray(point, dtype=np.float32).reshape(-1))
+        if p.size != 3 or not np.all(np.isfinite(p)):
+            raise ValueError("A world joint and finite xyz anchor are required")
+        slot = int(_joint_slots(self._kinds, [constraint])[0])
+        L.check(L.lib().avbd_world_set_world_anchor(self._h, slot, L.fptr(p)))
+
+    def captureConstraintFrames(self, entries):
+        """captureConstraintFrames (src/native/cpu/world.js:474-492): entries are constraint indices
+        or {"slot": constraint, "spring": bool}; each live joint's rest rotation, or spring's rest
+        length, is taken again from the current poses."""
+        self._live()
+        cons, spring = [], []
+        for e in entries:
+            if isinstance(e, dict):
+                cons.append(int(e["slot"]))
+                spring.append(1 if e.get("spring") else 0)
+            else:
+                cons.append(int(e))
+                spring.append(0)
+        slots = _joint_slots(self._kinds, cons)
+        sp = np.ascontiguousarray(np.asarray(spring, dtype=np.int32))
+        L.check(L.lib().avbd_world_capture_frames(self._h, L.iptr(slots), L.iptr(sp), int(slots.size)))
+
     def setRestitution(self, indices, values):
         self._live()
         idx = np.ascontiguousarray(np.asarray(indices, dtype=np.int64).reshape(-1))

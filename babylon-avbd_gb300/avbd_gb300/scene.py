@@ -84,6 +84,11 @@ class SceneArrays:
     restitution: np.ndarray | None = None  # per body, 0..1 (None: all zero)
     allow_sleep: np.ndarray | None = None  # per body, bool (None: all may sleep)
     order: np.ndarray | None = None  # after a spatial sort: creation index of each body slot
+    p3: np.ndarray | None = None  # per constraint: a spring's breakStrain (None: none anywhere)
+
+    def p3_or_none(self) -> np.ndarray:
+        """Spring strain limits (0: none), one per constraint."""
+        return self.p3 if self.p3 is not None else np.zeros(self.n_cons, dtype=np.float64)
 
     def restitution_or_zero(self) -> np.ndarray:
         return self.restitution if self.restitution is not None else np.zeros(self.n_bodies, dtype=np.float64)
@@ -159,8 +164,9 @@ class SceneBuilder:
                           float(stiff_lin), float(stiff_ang), float(fracture)))
         return len(self.cons) - 1
 
-    def spring(self, a, b, ra, rb, stiffness, rest=-1.0) -> int:
-        self.cons.append((KIND_SPRING, int(a), int(b), ra, rb, float(stiffness), float(rest), 0.0))
+    def spring(self, a, b, ra, rb, stiffness, rest=-1.0, break_strain=INF, break_force=INF) -> int:
+        self.cons.append((KIND_SPRING, int(a), int(b), ra, rb, float(stiffness), float(rest), float(break_force),
+                          float(break_strain)))
         return len(self.cons) - 1
 
     def angular(self, kind, a, b, axis_a, axis_b, p0, p1) -> int:
@@ -206,6 +212,7 @@ class SceneBuilder:
             p0=np.array([c[5] for c in self.cons], dtype=np.float64),
             p1=np.array([c[6] for c in self.cons], dtype=np.float64),
             p2=np.array([c[7] for c in self.cons], dtype=np.float64),
+            p3=np.array([c[8] if len(c) > 8 else 0.0 for c in self.cons], dtype=np.float64),
             params=self.params,
         )
 
@@ -239,6 +246,17 @@ def _angular_options(kind, axisA=(0, 1, 0), axisB=(0, 1, 0), speed=1.0, maxTorqu
         raise ValueError("Hinge angles must be ordered within -PI..PI radians")
     return {"type": kind, "axisA": unit(axisA), "axisB": unit(axisB), "speed": speed, "maxTorque": maxTorque,
             "minAngle": minAngle, "maxAngle": maxAngle}
+
+
+def spring_material(breakStrain=INF, breakForce=INF) -> dict:
+    """springMaterial (src/gpu/springMaterial.js:4-13): each limit positive or infinite."""
+    out = {}
+    for name, v in (("breakStrain", breakStrain), ("breakForce", breakForce)):
+        v = float(v)
+        if v != INF and (not math.isfinite(v) or v <= 0):
+            raise ValueError(f"{name} must be positive or Infinity")
+        out[name] = v
+    return out
 
 
 def _vector(v, n, name):
@@ -430,7 +448,10 @@ class AvbdScene3D:
                                   m.get("maxTorque", 100.0))
         return Hinge(joints, limit, drive)
 
-    def addSpring(self, a, b, anchorA=(0, 0, 0), anchorB=(0, 0, 0), stiffness=1000.0, rest=-1.0) -> int:
+    def addSpring(self, a, b, anchorA=(0, 0, 0), anchorB=(0, 0, 0), stiffness=1000.0, rest=-1.0,
+                  breakStrain=INF, breakForce=INF) -> int:
+        # scenes.js:541-569: a tensile spring that tears past breakStrain (extension / rest) or
+        # breakForce (stiffness x extension)
         self._editable()
         self._check(a, b)
         if a is None:
@@ -438,8 +459,9 @@ class AvbdScene3D:
         _positive(stiffness, "stiffness", True)
         if rest != -1:
             _positive(rest, "rest", True)
+        m = spring_material(breakStrain, breakForce)
         return self._b.spring(a, b, _vector(anchorA, 3, "anchorA"), _vector(anchorB, 3, "anchorB"),
-                              stiffness, rest)
+                              stiffness, rest, m["breakStrain"], m["breakForce"])
 
     def ignoreCollision(self, a, b) -> int:
         """A pair that never gets a contact manifold (``ref/forces.ts:299-306``)."""

@@ -643,6 +643,10 @@ class Arena {
     }
   }
 
+  // A spring's breakStrain / breakForce (src/gpu/springMaterial.js): zero, negative or infinite
+  // means unbreakable, held as INFINITY.
+  static float springLimit(float x) { return x > 0.f && std::isfinite(x) ? x : INFINITY; }
+
   static int jointsOf(const avbd_scene_desc& d) {
     int nj = 0;
     for (int c = 0; c < d.n_cons; c++) nj += d.cons_kind[c] != AVBD_CONS_IGNORE;
@@ -958,7 +962,8 @@ class Arena {
         jrb[j] = make_float4(d.cons_rb[3 * c], d.cons_rb[3 * c + 1], d.cons_rb[3 * c + 2], kind == AVBD_CONS_SPRING ? d.cons_p1[c] : 0.f);
         jst[j] = kind == AVBD_CONS_JOINT ? make_float4(d.cons_p0[c], d.cons_p1[c], d.cons_p2[c], 0.f)
                  : angular               ? make_float4(d.cons_p0[c], d.cons_p1[c], INFINITY, 0.f)
-                                         : make_float4(d.cons_p0[c], 0.f, INFINITY, 0.f);
+                                         : make_float4(d.cons_p0[c], springLimit(d.cons_p3 ? d.cons_p3[c] : 0.f),
+                                                       springLimit(d.cons_p2[c]), 0.f);
         if (angular) jpl[j] = make_float4(ANGULAR_PENALTY0, ANGULAR_PENALTY0, 0.f, 0.f);
         j++;
       }
@@ -1594,6 +1599,11 @@ class Arena {
       o[7] = broken[j] ? 0.f : fin(st.y);
       o[11] = fin(st.z);
       o[15] = st.w;
+      if (kind == KIND_SPRING) {  // stiffness; strain and tension limits (0: none) as appGpuSolver3D.js:826-833
+        o[7] = 0.f;
+        o[11] = st.y < INFINITY ? st.y : 0.f;
+        o[15] = st.z < INFINITY ? st.z : 0.f;
+      }
       o[24] = ra.x; o[25] = ra.y; o[26] = ra.z; o[27] = rb.w;
       o[28] = rb.x; o[29] = rb.y; o[30] = rb.z; o[31] = 0.f;
     }
@@ -1664,6 +1674,79 @@ class Arena {
     if (mask & 1) st.x = speed;
     if (mask & 2) st.y = maxTorque;
     put(J.stiff + j, &st, 16);
+    flush();
+    wakeWorld(w);
+  }
+
+  // setSpringMaterial (src/gpu/appGpuSolver3D.js:810-835, src/native/cpu/world.js:495-501): the
+  // strain and tension limits of the live spring `slot` (positive, or INFINITY: none); the world
+  // wakes. mask bit 0: breakStrain, bit 1: breakForce.
+  void setSpringMaterial(int w, int slot, int mask, float breakStrain, float breakForce) {
+    if (w < 0 || w >= maxWorlds || !W[w].live) throw Error(AVBD_E_INVALID, "no such world");
+    for (int k = 0; k < 2; k++) {
+      const float v = k ? breakForce : breakStrain;
+      if ((mask >> k & 1) && !(v > 0.f)) throw Error(AVBD_E_INVALID, k ? "breakForce must be positive or Infinity" : "breakStrain must be positive or Infinity");
+    }
+    flushEdits(w);
+    const WorldRec& R = resident(w);
+    if (slot < 0 || slot >= R.nJoints) throw Error(AVBD_E_INVALID, "Spring material requires an active spring slot");
+    const size_t j = size_t(R.dev.jointOff) + size_t(slot);
+    const float4 ra = fetch(J.rA, j, 1)[0];
+    float4 st = fetch(J.stiff, j, 1)[0];
+    int kind;
+    std::memcpy(&kind, &ra.w, 4);
+    if (kind != KIND_SPRING || fetch(J.broken, j, 1)[0]) throw Error(AVBD_E_INVALID, "Spring material requires an active spring slot");
+    if (mask & 1) st.y = breakStrain;
+    if (mask & 2) st.z = breakForce;
+    put(J.stiff + j, &st, 16);
+    flush();
+    wakeWorld(w);
+  }
+
+  // setWorldAnchor (src/gpu/appGpuSolver3D.js:928-941): the world point of the live world joint
+  // `slot` (a joint whose first body is the world) moves to `point`; the world wakes.
+  void setWorldAnchor(int w, int slot, const float* point) {
+    if (w < 0 || w >= maxWorlds || !W[w].live) throw Error(AVBD_E_INVALID, "no such world");
+    if (!(std::isfinite(point[0]) && std::isfinite(point[1]) && std::isfinite(point[2])))
+      throw Error(AVBD_E_INVALID, "A world joint and finite xyz anchor are required");
+    flushEdits(w);
+    const WorldRec& R = resident(w);
+    if (slot < 0 || slot >= R.nJoints) throw Error(AVBD_E_INVALID, "A world joint and finite xyz anchor are required");
+    const size_t j = size_t(R.dev.jointOff) + size_t(slot);
+    float4 ra = fetch(J.rA, j, 1)[0];
+    int kind;
+    std::memcpy(&kind, &ra.w, 4);
+    if (kind != KIND_JOINT || fetch(J.ab, j, 1)[0].x >= 0) throw Error(AVBD_E_INVALID, "A world joint and finite xyz anchor are required");
+    ra.x = point[0];
+    ra.y = point[1];
+    ra.z = point[2];
+    put(J.rA + j, &ra, 16);
+    flush();
+    wakeWorld(w);
+  }
+
+  // captureConstraintFrames (src/native/cpu/world.js:474-492): for each entry, the live joint's
+  // rest rotation (spring = 0) or the live spring's rest length (spring = 1) taken again from the
+  // current poses, after queued commands apply; the world wakes.
+  void captureFrames(int w, const int32_t* slots, const int32_t* spring, int n) {
+    if (w < 0 || w >= maxWorlds || !W[w].live) throw Error(AVBD_E_INVALID, "no such world");
+    if (n < 0) throw Error(AVBD_E_INVALID, "negative count");
+    const WorldRec& R = resident(w);
+    if (n == 0) return;
+    const size_t off = size_t(R.dev.jointOff), nj = size_t(R.nJoints);
+    std::vector<float4> ra;
+    std::vector<int> broken;
+    getRange(ra, J.rA, off, nj);
+    getRange(broken, J.broken, off, nj);
+    for (int k = 0; k < n; k++) {
+      int kind = -1;
+      if (slots[k] >= 0 && size_t(slots[k]) < nj) std::memcpy(&kind, &ra[slots[k]].w, 4);
+      if (kind != (spring[k] ? KIND_SPRING : KIND_JOINT) || broken[slots[k]])
+        throw Error(AVBD_E_INVALID, "A live spring or joint slot is required");
+    }
+    flushEdits(w);
+    for (int k = 0; k < n; k++) launch_joint_capture(B, J, int(off) + slots[k], spring[k] ? 1 : 0, s);
+    CK(cudaGetLastError());
     flush();
     wakeWorld(w);
   }
@@ -1822,6 +1905,7 @@ class Arena {
       // every span owns its two events (the pool recycles each event exactly once)
       cudaEvent_t e1 = prof ? mark() : nullptr;
       cudaEvent_t e1b = prof ? mark() : nullptr;
+      launch_spring_tear(B, J, t, s);
       launch_adjacency(B, J, P, t, ctr, T, pairBudget, scanTemp, s);
       launch_coloring(B, worlds, J, P, t, T, rounds, ctr, s);
       launch_items_count(P, t, T, ctr, scanTemp, s);
@@ -1850,6 +1934,7 @@ class Arena {
     ensureItems();
     launch_items_fill(B, worlds, P, t, T, ctr, s);
     cudaEvent_t o0 = prof ? mark() : nullptr;
+    launch_joint_retire(J, t, s);
     launch_joint_warmstart(B, worlds, J, t, s);
     launch_body_warmstart(B, worlds, t, s);
     if (prof) span(P_OTHER, o0, mark());

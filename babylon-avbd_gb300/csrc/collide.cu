@@ -151,7 +151,9 @@ __device__ __forceinline__ bool linked(const NoCollide& nc, const int* jbroken, 
   }
   for (; a < nc.n && nc.keys[a] == key; a++) {
     int j = nc.jid[a];
-    if (j < 0 || !jbroken[j]) return true;
+    // 2: broken in the last step's dual or torn at this step's start, still joining the pair in
+    // this broadphase (the reference drops a broken constraint from the bodies' lists after it)
+    if (j < 0 || jbroken[j] != 1) return true;
   }
   return false;
 }

@@ -475,6 +475,30 @@ int avbd_world_release_joints(avbd_world* w, const int32_t* slots, int32_t n) {
   API_END
 }
 
+int avbd_world_set_spring_material(avbd_world* w, int32_t slot, int32_t mask, float break_strain, float break_force) {
+  API_BEGIN
+  REQUIRE(w, "null world");
+  bind(w->A->ctx);
+  w->A->setSpringMaterial(w->w, slot, mask, break_strain, break_force);
+  API_END
+}
+
+int avbd_world_set_world_anchor(avbd_world* w, int32_t slot, const float* point) {
+  API_BEGIN
+  REQUIRE(w && point, "null argument");
+  bind(w->A->ctx);
+  w->A->setWorldAnchor(w->w, slot, point);
+  API_END
+}
+
+int avbd_world_capture_frames(avbd_world* w, const int32_t* slots, const int32_t* spring, int32_t n) {
+  API_BEGIN
+  REQUIRE(w && (n == 0 || (slots && spring)), "null argument");
+  bind(w->A->ctx);
+  w->A->captureFrames(w->w, slots, spring, n);
+  API_END
+}
+
 int avbd_world_cast(avbd_world* w, const float* queries, int32_t n, const avbd_cast_filter* filter, float* hits) {
   API_BEGIN
   REQUIRE(w && (n == 0 || (queries && hits)), "null argument");

@@ -7,6 +7,8 @@
 //            vel ang vprev size(xyz, friction) mass(m, Ix, Iy, Iz) meta(world, shape, group, mask)
 //   joints   a contiguous range of the joint arrays: body pair, rA(xyz, kind) rB(xyz, rest)
 //            stiff(lin, ang, fracture, torqueArm) penLin penAng lamLin lamAng C0Lin C0Ang restQ, broken
+//            (a spring: stiff(stiffness, strain limit, tension limit, torqueArm), rest length in rB.w;
+//            motors and limits: angular.cuh)
 //   pairs    a region of pair slots, present in two buffers (slot + k * slotStride, k = 0, 1): the
 //            world's previous state lives in buffer which[w], a step writes the other buffer and
 //            flips which[w]. Per slot: (hi, lo) sorted ascending within the world, contact count,
@@ -94,7 +96,7 @@ struct BodyPtrs {
 struct JointPtrs {
   int2* ab;
   float4 *rA, *rB, *stiff, *penLin, *penAng, *lamLin, *lamAng, *C0Lin, *C0Ang, *restQ;
-  int* broken;
+  int* broken;  // 0 live; 1 gone; 2 broken or torn this step, still joining its pair in the broadphase
 };
 
 // Both pair buffers (slots [0, slotStride) and [slotStride, 2 slotStride)).
@@ -244,6 +246,9 @@ void launch_bvh_refit(const BodyPtrs& b, int bodyOff, int n, BvhPool pool, int n
 
 // solve.cu
 void launch_joint_prepare(const BodyPtrs& b, JointPtrs j, int j0, int j1, cudaStream_t s);
+void launch_joint_capture(const BodyPtrs& b, JointPtrs j, int slot, int spring, cudaStream_t s);
+void launch_spring_tear(const BodyPtrs& b, JointPtrs j, Tick t, cudaStream_t s);
+void launch_joint_retire(JointPtrs j, Tick t, cudaStream_t s);
 void launch_joint_warmstart(const BodyPtrs& b, const WorldDev* worlds, JointPtrs j, Tick t, cudaStream_t s);
 void launch_body_warmstart(const BodyPtrs& b, const WorldDev* worlds, Tick t, cudaStream_t s);
 void launch_adjacency(const BodyPtrs& b, JointPtrs j, PairPtrs P, Tick t, const Counters* ctr, Topo topo, int pairBudget,

@@ -100,11 +100,15 @@ typedef struct avbd_scene_desc {
                                     motor: speed; limit: lower angle */
   const float* cons_p1;          /* joint: angular stiffness; spring: rest length (-1: current);
                                     motor: torque bound; limit: upper angle */
-  const float* cons_p2;          /* joint: fracture threshold on |lambda_ang| */
+  const float* cons_p2;          /* joint: fracture threshold on |lambda_ang|; spring: breakForce,
+                                    the tension limit (<= 0 or INFINITY: none) */
   const float* restitution;      /* n [0] restitution 0..1 (addBox/addSphere option; the velocity
                                     bounce pass of src/native/cpu/restitution.js runs when > 0) */
   const int32_t* allow_sleep;    /* n [1] allowSleep option (scenes.js:235-240): 0 keeps the body's
                                     island awake */
+  const float* cons_p3;          /* n_cons [none] spring: breakStrain, the strain limit (<= 0 or
+                                    INFINITY: none). A spring past either limit at the start of
+                                    a step tears for good (src/gpu/springMaterial.js) */
 } avbd_scene_desc;
 
 /* readCounters() of src/vendor/three-avbd-lib/solver3D.ts:1460-1463 plus engine state. */
@@ -284,6 +288,17 @@ int avbd_world_set_motor(avbd_world* w, int32_t slot, int32_t mask, float speed,
  * 1173-1193): the joints, springs or angular rows at the given joint indices stop acting (their
  * records read as released, their bodies collide again); the world wakes. */
 int avbd_world_release_joints(avbd_world* w, const int32_t* slots, int32_t n);
+/* setSpringMaterial(slot, {breakStrain, breakForce}) (src/gpu/appGpuSolver3D.js:810-835): limits
+ * of a live spring (positive, or INFINITY: none); mask bit 0 sets breakStrain, bit 1 breakForce.
+ * The world wakes. */
+int avbd_world_set_spring_material(avbd_world* w, int32_t slot, int32_t mask, float break_strain, float break_force);
+/* setWorldAnchor(slot, point) (src/gpu/appGpuSolver3D.js:928-941): moves the world point of a live
+ * joint attached to the world (a grab handle); the world wakes. */
+int avbd_world_set_world_anchor(avbd_world* w, int32_t slot, const float* point);
+/* captureConstraintFrames(entries) (src/native/cpu/world.js:474-492): per entry, a live joint's rest
+ * rotation (spring[k] = 0) or a live spring's rest length (spring[k] != 0) is taken again from the
+ * current poses, after queued commands; the world wakes. */
+int avbd_world_capture_frames(avbd_world* w, const int32_t* slots, const int32_t* spring, int32_t n);
 
 /* Load per-body sleep flags and quiet times (state import for one-step comparisons; NULL skips). */
 int avbd_world_import_sleep_state(avbd_world* w, const int32_t* asleep, const float* quiet_time);

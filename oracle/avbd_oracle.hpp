@@ -253,6 +253,8 @@ template <class R> struct Force {
   // in A's / B's frame; p0, p1 the speed and torque bound (motor) or the lower and upper angle
   // (limit); ta, tb the reference tangents; c0 the rows' step-start values; penLin[0..1] and
   // lamLin[0..1] the rows' penalty and lambda.
+  // spring fracture (src/gpu/springMaterial.js): strain and tension limits, infinite for none
+  R breakStrain = std::numeric_limits<R>::infinity(), breakForce = std::numeric_limits<R>::infinity();
   int angular = 0;
   R p0 = 0, p1 = 0;
   R ta[3] = {0, 0, 0}, tb[3] = {0, 0, 0};
@@ -689,6 +691,60 @@ template <class R> class Solver {
     f.penLin[1] = Mt::mn(f.penLin[1] + vy * betaAng, R(PENALTY_MAX));
   }
   // ------------------------------------------------------------ springs (forces.ts:260-296)
+  // Tensile fracture at the step start (cpuPhysics3D.js:276-299): a spring stretched past its
+  // strain or tension limit tears for good.
+  bool springInitialize(Force<R>& f) {
+    if (f.broken) return false;
+    if (f.breakStrain < std::numeric_limits<R>::infinity() || f.breakForce < std::numeric_limits<R>::infinity()) {
+      R pA[3], pB[3], d[3];
+      Mt::transform(pA, bodies[f.a].pos, bodies[f.a].q, f.rA);
+      Mt::transform(pB, bodies[f.b].pos, bodies[f.b].q, f.rB);
+      Mt::sub3(d, pA, pB);
+      const R ext = Mt::mx(R(0), Mt::length(d) - f.rest);
+      if (ext / Mt::mx(f.rest, R(1.0e-6)) > f.breakStrain || ext * f.stiffness > f.breakForce) {
+        f.broken = true;
+        return false;
+      }
+    }
+    return true;
+  }
+  // setSpringMaterial / setWorldAnchor / captureConstraintFrames by joint id (world.js:474-501,
+  // appGpuSolver3D.js:810-841). Each returns false when jid is not a live constraint of that kind.
+  Force<R>* liveJid(int jid) {
+    for (auto& p : store)
+      if (p->jid == jid && !p->broken) return p.get();
+    return nullptr;
+  }
+  bool setSpringMaterial(int jid, int mask, R strain, R force) {
+    Force<R>* f = liveJid(jid);
+    if (!f || f->type != F_SPRING) return false;
+    if (mask & 1) f->breakStrain = strain;
+    if (mask & 2) f->breakForce = force;
+    return true;
+  }
+  bool setWorldAnchor(int jid, const R* point) {
+    Force<R>* f = liveJid(jid);
+    if (!f || f->type != F_JOINT || f->angular || f->a >= 0) return false;
+    for (int i = 0; i < 3; i++) f->rA[i] = point[i];
+    return true;
+  }
+  bool captureFrame(int jid, bool spring) {
+    Force<R>* f = liveJid(jid);
+    if (!f || f->angular || f->type != (spring ? F_SPRING : F_JOINT)) return false;
+    if (spring) {
+      R pA[3], pB[3], d[3];
+      Mt::transform(pA, bodies[f->a].pos, bodies[f->a].q, f->rA);
+      Mt::transform(pB, bodies[f->b].pos, bodies[f->b].q, f->rB);
+      Mt::sub3(d, pA, pB);
+      f->rest = Mt::length(d);
+    } else {
+      static const R IDENTITY[4] = {0, 0, 0, 1};
+      R inv[4];
+      Mt::qinverse(inv, f->a >= 0 ? bodies[f->a].q : IDENTITY);
+      Mt::qmul(f->restQ, inv, bodies[f->b].q);
+    }
+    return true;
+  }
   void springPrimal(const Force<R>& f, int body, Sys& sys) const {
     const Body<R>& A = bodies[f.a];
     const Body<R>& B = bodies[f.b];
@@ -1078,6 +1134,7 @@ template <class R> class Solver {
       bool keep = true;
       if (f.type == F_MANIFOLD) keep = manifoldInitialize(f);
       else if (f.type == F_JOINT) keep = jointInitialize(f);
+      else if (f.type == F_SPRING) keep = springInitialize(f);
       if (keep) kept.push_back(id);
       else unlinkFromBodies(id);
     }

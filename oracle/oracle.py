@@ -26,7 +26,7 @@ class _Scene(C.Structure):
                 ("friction", _dp), ("radius", _dp), ("shape", _ip), ("group", _up), ("mask", _up),
                 ("n_cons", C.c_int), ("kind", _ip), ("ca", _ip), ("cb", _ip), ("ra", _dp),
                 ("rb", _dp), ("p0", _dp), ("p1", _dp), ("p2", _dp), ("restitution", _dp),
-                ("allow_sleep", _ip)]
+                ("allow_sleep", _ip), ("p3", _dp)]
 
 
 class _Params(C.Structure):
@@ -88,6 +88,12 @@ def lib():
         L.oracle_world_set_motor.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_double]
         L.oracle_world_set_motor.restype = C.c_int
         L.oracle_world_release_joints.argtypes = [C.c_void_p, _ip, C.c_int]
+        L.oracle_world_set_spring_material.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_double]
+        L.oracle_world_set_spring_material.restype = C.c_int
+        L.oracle_world_set_world_anchor.argtypes = [C.c_void_p, C.c_int, _dp]
+        L.oracle_world_set_world_anchor.restype = C.c_int
+        L.oracle_world_capture_frame.argtypes = [C.c_void_p, C.c_int, C.c_int]
+        L.oracle_world_capture_frame.restype = C.c_int
         _lib = L
     return _lib
 
@@ -127,7 +133,8 @@ class OracleWorld:
                    d(scene.friction), d(scene.radius), i32(scene.shape), u32(scene.group),
                    u32(scene.mask), scene.n_cons, i32(scene.kind), i32(scene.ca), i32(scene.cb),
                    d(scene.ra), d(scene.rb), d(scene.p0), d(scene.p1), d(scene.p2),
-                   d(scene.restitution_or_zero()), i32(scene.allow_sleep_or_one()))
+                   d(scene.restitution_or_zero()), i32(scene.allow_sleep_or_one()),
+                   d(scene.p3_or_none() if hasattr(scene, "p3_or_none") else np.zeros(scene.n_cons)))
         prm = _Params(p.dt, p.gravity, (C.c_double * 3)(*p.up), p.iterations, p.alpha, p.beta_lin,
                       p.beta_ang, p.gamma, int(app), int(p.mass_penalty), int(p.face_bias),
                       int(colored), int(p.color_rounds), int(bool(p.sleeping)), float(p.sleep_speed),
@@ -266,6 +273,25 @@ class OracleWorld:
         """releaseJoints of these joint slots."""
         j = np.ascontiguousarray(np.asarray(jids, dtype=np.int32).reshape(-1))
         lib().oracle_world_release_joints(self.h, _ptr(j, C.c_int), j.size)
+
+    def set_spring_material(self, jid, break_strain=None, break_force=None):
+        mask = (1 if break_strain is not None else 0) | (2 if break_force is not None else 0)
+        inf = float("inf")
+        ok = lib().oracle_world_set_spring_material(self.h, int(jid), mask, float(inf if break_strain is None else break_strain),
+                                                    float(inf if break_force is None else break_force))
+        if not ok:
+            raise ValueError("Spring material requires an active spring slot")
+
+    def set_world_anchor(self, jid, point):
+        p = np.ascontiguousarray(np.asarray(point, dtype=np.float64).reshape(3))
+        if not lib().oracle_world_set_world_anchor(self.h, int(jid), _ptr(p, C.c_double)):
+            raise ValueError("A world joint and finite xyz anchor are required")
+
+    def capture_frames(self, entries):
+        """entries: (joint slot, spring) pairs."""
+        for jid, spring in entries:
+            if not lib().oracle_world_capture_frame(self.h, int(jid), int(bool(spring))):
+                raise ValueError("A live spring or joint slot is required")
 
     def edit(self, records):
         """Apply body command records (n x 12 uint32 words, ``src/gpu/bodyCommands2D.js``

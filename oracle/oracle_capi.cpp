@@ -41,6 +41,7 @@ struct oracle_scene {
   const double* p2;  // joint: fracture
   const double* restitution;  // n (null: 0)
   const int32_t* allow_sleep;  // n (null: 1)
+  const double* p3;            // n_cons spring: breakStrain (null, <= 0 or inf: none); p2: breakForce
 };
 
 struct oracle_params {
@@ -102,7 +103,12 @@ template <class R> static Solver<R>* build(const oracle_scene* s, const oracle_p
     R ra[3], rb[3];
     for (int k = 0; k < 3; k++) { ra[k] = R(s->ra[3 * c + k]); rb[k] = R(s->rb[3 * c + k]); }
     if (s->kind[c] == K_JOINT) w->addJoint(s->ca[c], s->cb[c], ra, rb, R(s->p0[c]), R(s->p1[c]), R(s->p2[c]));
-    else if (s->kind[c] == K_SPRING) w->addSpring(s->ca[c], s->cb[c], ra, rb, R(s->p0[c]), R(s->p1[c]));
+    else if (s->kind[c] == K_SPRING) {
+      int id = w->addSpring(s->ca[c], s->cb[c], ra, rb, R(s->p0[c]), R(s->p1[c]));
+      auto limit = [](double x) { return x > 0 && std::isfinite(float(x)) ? R(float(x)) : std::numeric_limits<R>::infinity(); };
+      w->store[id]->breakForce = limit(s->p2[c]);
+      w->store[id]->breakStrain = limit(s->p3 ? s->p3[c] : 0.0);
+    }
     else if (s->kind[c] == K_MOTOR || s->kind[c] == K_LIMIT)
       w->addAngular(s->ca[c], s->cb[c], s->kind[c], ra, rb, R(s->p0[c]), R(s->p1[c]));
     else w->addIgnore(s->ca[c], s->cb[c]);
@@ -335,11 +341,14 @@ template <class R> static void import_state(Solver<R>& S, const oracle_state* st
       f.lamLin[k] = R(st->jlam_lin[3 * j + k]);
       f.lamAng[k] = R(st->jlam_ang[3 * j + k]);
     }
-    bool broken = st->jbroken[j] != 0;
-    if (broken && !f.broken) {
+    // the engine's flag: 1 gone; 2 broken in the last step (still in the bodies' lists until
+    // the next initialize pass, after the broadphase)
+    if (st->jbroken[j] != 0 && !f.broken) {
       f.broken = true;
-      auto it = std::find(S.forces.begin(), S.forces.end(), int(&fp - &S.store[0]));
-      if (it != S.forces.end()) { S.unlinkFromBodies(*it); S.forces.erase(it); }
+      if (st->jbroken[j] == 1) {
+        auto it = std::find(S.forces.begin(), S.forces.end(), int(&fp - &S.store[0]));
+        if (it != S.forces.end()) { S.unlinkFromBodies(*it); S.forces.erase(it); }
+      }
     }
   }
   int c = 0;
@@ -375,6 +384,25 @@ extern "C" int oracle_world_set_motor(void* h, int jid, int mask, double speed, 
 }
 extern "C" void oracle_world_release_joints(void* h, const int32_t* jids, int n) {
   DISPATCH(h, for (int k = 0; k < n; k++) S.releaseJoint(jids[k]));
+}
+
+extern "C" int oracle_world_set_spring_material(void* h, int jid, int mask, double strain, double force) {
+  int ok = 0;
+  DISPATCH(h, ok = S.setSpringMaterial(jid, mask, decltype(S.dt)(strain), decltype(S.dt)(force)) ? 1 : 0);
+  return ok;
+}
+extern "C" int oracle_world_set_world_anchor(void* h, int jid, const double* point) {
+  int ok = 0;
+  DISPATCH(h, {
+    decltype(S.dt) p[3] = {decltype(S.dt)(point[0]), decltype(S.dt)(point[1]), decltype(S.dt)(point[2])};
+    ok = S.setWorldAnchor(jid, p) ? 1 : 0;
+  });
+  return ok;
+}
+extern "C" int oracle_world_capture_frame(void* h, int jid, int spring) {
+  int ok = 0;
+  DISPATCH(h, ok = S.captureFrame(jid, spring != 0) ? 1 : 0);
+  return ok;
 }
 
 // The angular rows' atan2 restatement, elementwise (fp64 != 0: double, else float).
