@@ -158,6 +158,7 @@ bool Scene(napi_env env, napi_value s, napi_value p, avbd_scene_desc* d, avbd_pa
   d->cons_p2 = Field<float>(env, s, "consP2");
   d->restitution = Field<float>(env, s, "restitution");
   d->allow_sleep = Field<int32_t>(env, s, "allowSleep");
+  d->cons_p3 = Field<float>(env, s, "consP3");
   q->dt = float(Number(env, p, "dt", 1.0 / 60.0));
   q->gravity = float(Number(env, p, "gravity", -10.0));
   const float* up = Field<float>(env, p, "up");
@@ -348,6 +349,36 @@ napi_value SetMotor(napi_env env, napi_callback_info info) {  // (w, slot, speed
   napi_typeof(env, argv[3], &t);
   if (t == napi_number) { napi_get_value_double(env, argv[3], &torque); mask |= 2; }
   CALL(avbd_world_set_motor(w, Int(env, argv[1]), mask, float(speed), float(torque)));
+  return nullptr;
+}
+napi_value SetSpringMaterial(napi_env env, napi_callback_info info) {  // (w, slot, breakStrain|undefined, breakForce|undefined)
+  WORLD_ARG(4);
+  int32_t mask = 0;
+  double v[2] = {0, 0};
+  for (int k = 0; k < 2; k++) {
+    napi_valuetype t;
+    napi_typeof(env, argv[2 + k], &t);
+    if (t == napi_number) { napi_get_value_double(env, argv[2 + k], &v[k]); mask |= 1 << k; }
+  }
+  CALL(avbd_world_set_spring_material(w, Int(env, argv[1]), mask, float(v[0]), float(v[1])));
+  return nullptr;
+}
+napi_value SetWorldAnchor(napi_env env, napi_callback_info info) {  // (w, slot, Float32Array(3))
+  WORLD_ARG(3);
+  const float* p;
+  size_t n;
+  if (!Typed(env, argv[2], &p, &n)) return nullptr;
+  if (n != 3) return Throw(env, "A world joint and finite xyz anchor are required");
+  CALL(avbd_world_set_world_anchor(w, Int(env, argv[1]), p));
+  return nullptr;
+}
+napi_value CaptureFrames(napi_env env, napi_callback_info info) {  // (w, Int32Array slots, Int32Array spring)
+  WORLD_ARG(3);
+  const int32_t *slots, *spring;
+  size_t n, ns;
+  if (!Typed(env, argv[1], &slots, &n) || !Typed(env, argv[2], &spring, &ns)) return nullptr;
+  if (ns != n) return Throw(env, "one spring flag per slot");
+  CALL(avbd_world_capture_frames(w, slots, spring, int32_t(n)));
   return nullptr;
 }
 napi_value ReleaseJoints(napi_env env, napi_callback_info info) {  // (w, Int32Array of joint slots)
@@ -561,6 +592,8 @@ napi_value Init(napi_env env, napi_value exports) {
              {"readState", ReadState},         {"setPoses", SetPoses},             {"setVelocities", SetVelocities},
              {"readCounters", ReadCounters},   {"readJoints", ReadJoints},         {"setFilters", SetFilters},
              {"setRestitution", SetRestitution}, {"setMotor", SetMotor},         {"releaseJoints", ReleaseJoints},
+             {"setSpringMaterial", SetSpringMaterial}, {"setWorldAnchor", SetWorldAnchor},
+             {"captureFrames", CaptureFrames},
              {"watchContacts", WatchContacts}, {"readContactEvents", ReadContactEvents},
              {"resetContactHistory", ResetContactHistory}, {"cast", Cast},         {"setSleeping", SetSleeping},
              {"setSleepEnabled", SetSleepEnabled}, {"wakeAll", WakeAll},           {"sleepStats", SleepStats},

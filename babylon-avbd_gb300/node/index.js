@@ -13,6 +13,7 @@ import { createRequire } from "node:module";
 import { IgnoreCollision, Joint, Spring } from "../../../reference/three-avbd/src/avbd3d/ref/forces.ts";
 import { isSphere } from "../../../reference/three-avbd/src/avbd3d/shapes.ts";
 import { angularConstraintOptions, initialAngularConstraint } from "../../gpu/angularConstraints.js";
+import { initialSpringMaterial, springMaterial } from "../../gpu/springMaterial.js";
 import { installNativeRuntime } from "../runtime.js";
 
 const require = createRequire(import.meta.url);
@@ -95,6 +96,7 @@ export function packScene(scene, options = {}) {
     consKind: new Int32Array(m), consA: new Int32Array(m), consB: new Int32Array(m),
     consRA: new Float32Array(3 * m), consRB: new Float32Array(3 * m),
     consP0: new Float32Array(m), consP1: new Float32Array(m), consP2: new Float32Array(m),
+    consP3: new Float32Array(m),
   });
   cons.forEach((f, c) => {
     a.consA[c] = f.bodyA ? slot.get(f.bodyA) : -1;
@@ -121,6 +123,10 @@ export function packScene(scene, options = {}) {
       a.consRB.set(f.rB, 3 * c);
       a.consP0[c] = f.stiffness;
       a.consP1[c] = f.rest;
+      // tear limits (springMaterial.js; 0 = none): breakForce in p2, breakStrain in p3
+      const material = initialSpringMaterial(f);
+      a.consP2[c] = Number.isFinite(material?.breakForce) ? material.breakForce : 0;
+      a.consP3[c] = Number.isFinite(material?.breakStrain) ? material.breakStrain : 0;
     } else {
       a.consKind[c] = 2;
     }
@@ -247,6 +253,27 @@ class Gb300World {
     const o = angularConstraintOptions({ type: "motor", speed: options.speed ?? 0, maxTorque: options.maxTorque ?? 0 });
     addon.setMotor(this.handle, slot, options.speed === undefined ? undefined : o.speed,
       options.maxTorque === undefined ? undefined : o.maxTorque);
+  }
+  /** setSpringMaterial(slot, { breakStrain, breakForce }) (appGpuSolver3D.js:810-835). */
+  setSpringMaterial(slot, options = {}) {
+    this.assertLive();
+    const m = springMaterial(options);
+    addon.setSpringMaterial(this.handle, slot, options.breakStrain === undefined ? undefined : m.breakStrain,
+      options.breakForce === undefined ? undefined : m.breakForce);
+  }
+  /** setWorldAnchor(slot, point) (appGpuSolver3D.js:928-941): move a world joint's anchor. */
+  setWorldAnchor(slot, point) {
+    this.assertLive();
+    addon.setWorldAnchor(this.handle, slot, Float32Array.from(point));
+  }
+  /** captureConstraintFrames([{ slot, spring }]) (src/native/cpu/world.js:474-492). */
+  captureConstraintFrames(entries) {
+    this.assertLive();
+    const list = Array.from(entries);
+    addon.captureFrames(this.handle, Int32Array.from(list, (e) => e.slot), Int32Array.from(list, (e) => (e.spring ? 1 : 0)));
+  }
+  disableConstraint(slot) {
+    this.releaseJoints([slot]);
   }
   /** releaseJoints(slots) (src/native/cpu/world.js:397-410). */
   releaseJoints(slots) {
