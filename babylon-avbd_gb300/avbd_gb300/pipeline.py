@@ -452,6 +452,69 @@ def _indices(indices, n):
     return idx.astype(np.uint32)
 
 
+class Body:
+    """A handle on the body in slot `index` of a world (``world.body(i)``; NativeBody of
+    src/native/runtime.js:169-237): the world's per-body commands, each returning the handle."""
+
+    def __init__(self, world: "World", index: int):
+        self.world = world
+        self.index = int(index)
+
+    @property
+    def gpuIndex(self) -> int:
+        """The body's slot (the index every world call takes)."""
+        return self.index
+
+    def setLinearVelocity(self, v):
+        self.world.setLinearVelocity(self.index, v)
+        return self
+
+    def setAngularVelocity(self, v):
+        self.world.setAngularVelocity(self.index, v)
+        return self
+
+    def applyImpulse(self, v, p=None):
+        self.world.applyImpulse(self.index, v, p)
+        return self
+
+    def applyForce(self, v, p=None):
+        self.world.applyForce(self.index, v, p)
+        return self
+
+    def applyAngularImpulse(self, v):
+        self.world.applyAngularImpulse(self.index, v)
+        return self
+
+    def applyTorque(self, v):
+        self.world.applyTorque(self.index, v)
+        return self
+
+    def teleport(self, position, rotation=None):
+        self.world.teleport(self.index, position, rotation)
+        return self
+
+    def setRestitution(self, value):
+        self.world.setRestitution([self.gpuIndex], [value])
+        return self
+
+    def setCollisionGroups(self, group, collidesWith=0xFFFFFFFF):
+        self.world.setFilters([self.gpuIndex], [group], [collidesWith])
+        return self
+
+    def setSleepEnabled(self, enabled):
+        self.world.setSleepEnabled(self.index, enabled)
+        return self
+
+    def wakeUp(self):
+        self.world.wakeUp(self.index)
+        return self
+
+    def readState(self) -> dict:
+        """Position, rotation, velocity, angular and previous velocity of this body."""
+        st = self.world.readBodyState()
+        return {k: v[self.gpuIndex].copy() for k, v in st.items()}
+
+
 class World:
     """One world (``pipeline.createSolver(scene)``)."""
 
@@ -544,6 +607,12 @@ class World:
             if p["allowSleep"] is not None:
                 self.setSleepEnabled(p["index"], p["allowSleep"])
         return self
+
+    def body(self, index) -> Body:
+        """A handle on the body in slot `index` (runtime.js:345-350; gpuIndex maps a creation index)."""
+        if not 0 <= int(index) < self.bodyCount:
+            raise ValueError("A live body index is required")
+        return Body(self, int(index))
 
     def setMotor(self, constraint, speed=None, maxTorque=None):
         """setMotor (src/gpu/appGpuSolver3D.js:547-562): a new speed and/or torque bound of the

@@ -112,3 +112,25 @@ def test_property_edits_apply_after_commands(pipe):
     with pytest.raises(ValueError):
         w.editBodies([{"body": ball, "restitution": 2.0}])
     w.destroy()
+
+
+def test_body_handles_route_to_the_world_commands(pipe):
+    # runtime.js:169-237: body(i) handles give the world's per-body commands on slot i
+    from avbd_gb300 import AvbdScene3D
+    sc = AvbdScene3D(timeStep=1 / 60, iterations=10, gravity=0)
+    a = sc.addBox([1, 1, 1], position=[0, 0, 0])
+    b = sc.addBox([1, 1, 1], position=[5, 0, 0])
+    w = pipe.createSolver(sc)
+    h = w.body(b)
+    assert h.gpuIndex == b and h.setLinearVelocity([1, 0, 0]) is h
+    h.setAngularVelocity([0, 2, 0]).setRestitution(0.5)
+    w.step(1)
+    st = h.readState()
+    assert np.allclose(st["velocity"], [1, 0, 0], atol=1e-6) and np.allclose(st["angular"], [0, 2, 0], atol=1e-6)
+    assert np.allclose(w.body(a).readState()["velocity"], 0)
+    h.teleport([9, 0, 0])
+    w.step(1)
+    assert 9 - 1e-4 <= h.readState()["position"][0] <= 9 + 1 / 60 + 1e-4
+    with pytest.raises(ValueError):
+        w.body(5)
+    w.destroy()
