@@ -197,3 +197,42 @@ def test_angular_argument_errors(pipe):
     bad.p0[2], bad.p1[2] = 0.5, 0.25  # limit stops out of order
     with pytest.raises(AvbdError):
         pipe.createSolver(bad)
+
+
+def test_hinges_and_springs_survive_eviction(pipe):
+    # a served world with motors, stops and tearable springs, evicted to host memory and restored
+    # between its requests, steps to the same bits as the world stepped alone
+    sc, d, m, z = _door_scene()
+    a = sc.addBox([0.3, 0.3, 0.3], density=0, position=[-8, 4, 0])
+    b = sc.addBox([0.5, 0.5, 0.5], position=[-8, 3, 0])
+    sc.addSpring(a, b, stiffness=150.0, rest=1.0, breakForce=20.0)
+    alone = pipe.createSolver(sc)
+    alone.step(50)
+    ref = alone.readBodyState()
+    alone.destroy()
+    server = pipe.createServer(budgetBytes=1 << 30)
+    wid = server.admit(sc)
+    other = server.admit(_rotor()[0])
+    for chunk in (10, 15, 25):
+        server.advance(wid, chunk)
+        server.advance(other, chunk)
+        for _ in range(chunk):
+            server.tick()
+        server.evict(wid)
+    got = server.readBodyState(wid)
+    for k in KEYS:
+        assert np.array_equal(got[k], ref[k]), k
+    server.destroy()
+
+
+def test_motor_change_wakes_a_sleeping_hinge(pipe):
+    # a rotor held by a motor at rest falls asleep; setMotor wakes the world and it turns
+    sc, b, h = _rotor(minAngle=None, maxAngle=None, motor={"speed": 0.0, "maxTorque": 5.0})
+    w = pipe.createSolver(sc, {"sleeping": True})
+    w.step(90)
+    assert w.readSleepState()[0][b]
+    w.setMotor(h.motor, speed=1.0)
+    assert not w.readSleepState()[0][b]
+    w.step(30)
+    assert w.readBodyState()["angular"][b, 2] > 0.5
+    w.destroy()
