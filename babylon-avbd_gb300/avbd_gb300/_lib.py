@@ -34,7 +34,7 @@ class SceneDesc(C.Structure):
                 ("shape", _ip), ("group", _up), ("collides_with", _up), ("n_cons", C.c_int32),
                 ("cons_kind", _ip), ("cons_a", _ip), ("cons_b", _ip), ("cons_ra", _fp),
                 ("cons_rb", _fp), ("cons_p0", _fp), ("cons_p1", _fp), ("cons_p2", _fp), ("restitution", _fp),
-                ("allow_sleep", _ip), ("cons_p3", _fp)]
+                ("allow_sleep", _ip), ("cons_p3", _fp), ("is_trigger", _ip)]
 
 
 class CastFilter(C.Structure):
@@ -131,6 +131,7 @@ SIGNATURES = [
     ("avbd_world_set_motor", C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_float, C.c_float]),
     ("avbd_batch_set_motor", C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_float, C.c_float]),
     ("avbd_world_release_joints", C.c_int, [C.c_void_p, _ip, C.c_int32]),
+    ("avbd_world_set_sensor", C.c_int, [C.c_void_p, _up, C.c_int32, C.c_int32]),
     ("avbd_world_set_spring_material", C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_float, C.c_float]),
     ("avbd_world_set_world_anchor", C.c_int, [C.c_void_p, C.c_int32, _fp]),
     ("avbd_world_capture_frames", C.c_int, [C.c_void_p, _ip, _ip, C.c_int32]),
@@ -206,13 +207,13 @@ class PackedScene:
                      f32(s.mass), f32(s.moment), f32(s.friction), f32(s.radius), i32(s.shape),
                      u32(s.group), u32(s.mask), i32(s.kind), i32(s.ca), i32(s.cb), f32(s.ra),
                      f32(s.rb), f32(s.p0), f32(s.p1), f32(s.p2), f32(s.restitution_or_zero()),
-                     i32(s.allow_sleep_or_one()), f32(s.p3_or_none())]
+                     i32(s.allow_sleep_or_one()), f32(s.p3_or_none()), i32(s.is_trigger_or_zero())]
         k = self.keep
         self.desc = SceneDesc(s.n_bodies, fptr(k[0]), fptr(k[1]), fptr(k[2]), fptr(k[3]), fptr(k[4]),
                               fptr(k[5]), fptr(k[6]), fptr(k[7]), fptr(k[8]), fptr(k[9]), iptr(k[10]),
                               uptr(k[11]), uptr(k[12]), s.n_cons, iptr(k[13]), iptr(k[14]),
                               iptr(k[15]), fptr(k[16]), fptr(k[17]), fptr(k[18]), fptr(k[19]),
-                              fptr(k[20]), fptr(k[21]), iptr(k[22]), fptr(k[23]))
+                              fptr(k[20]), fptr(k[21]), iptr(k[22]), fptr(k[23]), iptr(k[24]))
         p = s.params
         self.params = Params(p.dt, p.gravity, (C.c_float * 3)(*p.up), p.iterations, p.alpha,
                              p.beta_lin, p.beta_ang, p.gamma, int(p.mass_penalty), int(p.face_bias),

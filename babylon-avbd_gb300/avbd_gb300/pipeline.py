@@ -96,7 +96,7 @@ def spatial_sort(arrays: SceneArrays) -> SceneArrays:
     for k in ("pos", "quat", "size", "vel", "angvel", "prev_vel", "mass", "moment", "friction", "radius",
               "shape", "group", "mask"):
         setattr(out, k, np.asarray(getattr(arrays, k))[order])
-    for k in ("restitution", "allow_sleep"):
+    for k in ("restitution", "allow_sleep", "is_trigger"):
         v = getattr(arrays, k)
         setattr(out, k, None if v is None else np.asarray(v)[order])
     if arrays.n_cons:
@@ -152,7 +152,7 @@ def _read_events(fn, *args) -> dict:
     f = ev.view(np.float32)
     events = [{"type": "begin" if r[0] == 1 else "end", "kind": int(r[0]), "a": int(r[1]), "b": int(r[2]),
                "step": int(r[3]), "point": [float(x) for x in f[k, 4:7]], "impulse": float(f[k, 7]),
-               "normal": [float(x) for x in f[k, 8:11]], "isTrigger": False}
+               "normal": [float(x) for x in f[k, 8:11]], "isTrigger": bool(f[k, 11] != 0)}
               for k, r in enumerate(ev)]
     return {"events": events, "dropped": raw["dropped"], "full": raw["full"]}
 
@@ -345,8 +345,8 @@ def stage_properties(edits, body_count: int) -> list:
         index = edit.get("body")
         if not isinstance(index, (int, np.integer)) or not 0 <= int(index) < body_count:
             raise ValueError("A live body index is required")
-        if "isTrigger" in edit:
-            raise ValueError("triggers are not supported by the gb300 backend")
+        if "isTrigger" in edit and not isinstance(edit["isTrigger"], bool):
+            raise ValueError("isTrigger must be a boolean")
         if "allowSleep" in edit and not isinstance(edit["allowSleep"], bool):
             raise ValueError("allowSleep must be a boolean")
         e = edit.get("restitution")
@@ -358,7 +358,8 @@ def stage_properties(edits, body_count: int) -> list:
             if k in edit:
                 _mask(edit[k])
         out.append({"index": int(index), "restitution": e, "group": edit.get("group"),
-                    "collidesWith": edit.get("collidesWith", 0xFFFFFFFF), "allowSleep": edit.get("allowSleep")})
+                    "collidesWith": edit.get("collidesWith", 0xFFFFFFFF), "allowSleep": edit.get("allowSleep"),
+                    "isTrigger": edit.get("isTrigger")})
     return out
 
 
@@ -369,7 +370,7 @@ def stage_edits(edits, body_count: int, dt: float, allow_properties: bool = Fals
     (restitution, group, collidesWith, allowSleep) are left to ``stage_properties`` when
     ``allow_properties``, else refused."""
     words = []
-    unsupported = {"isTrigger"} if allow_properties else {"isTrigger", "restitution", "allowSleep", "group", "collidesWith"}
+    unsupported = set() if allow_properties else {"isTrigger", "restitution", "allowSleep", "group", "collidesWith"}
 
     def record(index, kind, value, point):
         w = np.zeros(12, dtype=np.uint32)
@@ -497,6 +498,10 @@ class Body:
         self.world.setRestitution([self.gpuIndex], [value])
         return self
 
+    def setTrigger(self, enabled):
+        self.world.setSensor(self.index, enabled)
+        return self
+
     def setCollisionGroups(self, group, collidesWith=0xFFFFFFFF):
         self.world.setFilters([self.gpuIndex], [group], [collidesWith])
         return self
@@ -606,6 +611,8 @@ class World:
                 self.setFilters([p["index"]], [p["group"]], [p["collidesWith"]])
             if p["allowSleep"] is not None:
                 self.setSleepEnabled(p["index"], p["allowSleep"])
+            if p["isTrigger"] is not None:
+                self.setSensor(p["index"], p["isTrigger"])
         return self
 
     def body(self, index) -> Body:
@@ -674,6 +681,15 @@ class World:
         slots = _joint_slots(self._kinds, cons)
         sp = np.ascontiguousarray(np.asarray(spring, dtype=np.int32))
         L.check(L.lib().avbd_world_capture_frames(self._h, L.iptr(slots), L.iptr(sp), int(slots.size)))
+
+    def setSensor(self, index, enabled):
+        """setSensor (src/native/cpu/world.js:342-350): the body becomes (or stops being) a
+        trigger: its contacts are reported but apply no forces; wakes the world."""
+        self._live()
+        if not isinstance(enabled, bool):
+            raise ValueError("isTrigger must be a boolean")
+        idx = _indices([index], self.bodyCount)
+        L.check(L.lib().avbd_world_set_sensor(self._h, L.uptr(idx), 1, int(enabled)))
 
     def setRestitution(self, indices, values):
         self._live()

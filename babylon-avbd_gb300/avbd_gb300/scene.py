@@ -85,6 +85,12 @@ class SceneArrays:
     allow_sleep: np.ndarray | None = None  # per body, bool (None: all may sleep)
     order: np.ndarray | None = None  # after a spatial sort: creation index of each body slot
     p3: np.ndarray | None = None  # per constraint: a spring's breakStrain (None: none anywhere)
+    is_trigger: np.ndarray | None = None  # per body, bool (None: no triggers)
+
+    def is_trigger_or_zero(self) -> np.ndarray:
+        if self.is_trigger is None:
+            return np.zeros(self.n_bodies, dtype=np.int32)
+        return np.asarray(self.is_trigger).astype(np.int32)
 
     def p3_or_none(self) -> np.ndarray:
         """Spring strain limits (0: none), one per constraint."""
@@ -109,7 +115,7 @@ class SceneArrays:
 
 class _Body:
     __slots__ = ("pos", "quat", "size", "vel", "angvel", "prev_vel", "mass", "moment",
-                 "friction", "radius", "shape", "group", "mask", "restitution", "allow_sleep")
+                 "friction", "radius", "shape", "group", "mask", "restitution", "allow_sleep", "is_trigger")
 
     def __init__(self, size, density, friction, position, velocity=(0.0, 0.0, 0.0)):
         # body.ts:32-54
@@ -132,6 +138,7 @@ class _Body:
         self.mask = MASK_ALL
         self.restitution = 0.0
         self.allow_sleep = True
+        self.is_trigger = False
 
 
 class SceneBuilder:
@@ -209,6 +216,7 @@ class SceneBuilder:
             rb=np.array([c[4] for c in self.cons], dtype=np.float64).reshape(m, 3),
             restitution=np.array([b.restitution for b in B], dtype=np.float64),
             allow_sleep=np.array([b.allow_sleep for b in B], dtype=bool),
+            is_trigger=np.array([b.is_trigger for b in B], dtype=bool),
             p0=np.array([c[5] for c in self.cons], dtype=np.float64),
             p1=np.array([c[6] for c in self.cons], dtype=np.float64),
             p2=np.array([c[7] for c in self.cons], dtype=np.float64),
@@ -340,8 +348,8 @@ class AvbdScene3D:
             e = options["restitution"]
             if not isinstance(e, (int, float)) or not math.isfinite(e) or e < 0 or e > 1:
                 raise ValueError("restitution must be between 0 and 1")
-        if options.get("isTrigger", False):
-            raise ValueError("triggers are not supported by the gb300 backend")
+        if "isTrigger" in options and not isinstance(options["isTrigger"], bool):
+            raise ValueError("isTrigger must be a boolean")
 
     def addBox(self, size, **options) -> int:
         self._editable()
@@ -370,6 +378,7 @@ class AvbdScene3D:
         b.mask = _mask(options.get("collidesWith", MASK_ALL))
         b.restitution = float(options.get("restitution", 0.0))
         b.allow_sleep = bool(options.get("allowSleep", True))
+        b.is_trigger = bool(options.get("isTrigger", False))
         if options.get("allowSleep") is True:  # scenes.js:240 sleepOptIn
             self._b.params.sleeping = True
         if "mass" in options:

@@ -150,6 +150,7 @@ struct Snapshot {
 
 struct WorldRec {
   bool live = false, resident = false;
+  bool triggers = false;  // some body is a trigger (isTrigger)
   WorldDev dev{};
   int nBodies = 0, nJoints = 0;
   int which = 0;
@@ -215,6 +216,7 @@ class Arena {
   int rounds = 64;
   // the last tick (its lists stay valid until the next tick)
   std::vector<int> lastActive;
+  bool tickTriggers = false;  // a world of the tick being built has trigger bodies
   int lastPairs = 0, lastJoints = 0;
   long long steps = 0, regrowths = 0, evictions = 0, restores = 0;
   bool haveStats = false;
@@ -596,6 +598,7 @@ class Arena {
     t.maxWorlds = maxWorlds;
     t.slotStride = slotCap;
     t.bodyStride = bodyCap;
+    t.triggerBits = tickTriggers ? B.sleep : nullptr;
     return t;
   }
 
@@ -914,6 +917,10 @@ class Arena {
         mass[i] = make_float4(d.mass[i], d.moment[3 * i], d.moment[3 * i + 1], d.moment[3 * i + 2]);
         rest[i] = d.restitution ? d.restitution[i] : 0.f;
         sleepBits[i] = (d.allow_sleep && d.allow_sleep[i] == 0) ? 0 : SLEEP_ALLOW;
+        if (d.is_trigger && d.is_trigger[i]) {
+          sleepBits[i] |= BODY_TRIGGER;
+          R.triggers = true;
+        }
         const uint32_t grp = d.group ? d.group[i] : 0xffffffffu, msk = d.collides_with ? d.collides_with[i] : 0xffffffffu;
         meta[i] = make_int4(w, d.shape[i], int(grp), int(msk));
       }
@@ -1678,6 +1685,28 @@ class Arena {
     wakeWorld(w);
   }
 
+  // setSensor (src/native/cpu/world.js:342-350): the bodies become (enabled) or stop being
+  // triggers; the world wakes.
+  void setSensor(int w, const uint32_t* idx, int n, bool enabled) {
+    if (w < 0 || w >= maxWorlds || !W[w].live) throw Error(AVBD_E_INVALID, "no such world");
+    if (n < 0) throw Error(AVBD_E_INVALID, "negative count");
+    flushEdits(w);
+    WorldRec& R = W[w];
+    resident(w);
+    for (int k = 0; k < n; k++)
+      if (idx[k] >= uint32_t(R.nBodies)) throw Error(AVBD_E_INVALID, "A live body index is required");
+    if (n == 0) return;
+    const size_t nb = size_t(R.nBodies), off = size_t(R.dev.bodyOff);
+    std::vector<int> bits;
+    getRange(bits, B.sleep, off, nb);
+    for (int k = 0; k < n; k++) bits[idx[k]] = enabled ? (bits[idx[k]] | BODY_TRIGGER) : (bits[idx[k]] & ~BODY_TRIGGER);
+    putRange(B.sleep, off, bits);
+    R.triggers = false;
+    for (int b : bits) R.triggers |= (b & BODY_TRIGGER) != 0;
+    flush();
+    wakeWorld(w);
+  }
+
   // setSpringMaterial (src/gpu/appGpuSolver3D.js:810-835, src/native/cpu/world.js:495-501): the
   // strain and tension limits of the live spring `slot` (positive, or INFINITY: none); the world
   // wakes. mask bit 0: breakStrain, bit 1: breakForce.
@@ -1807,6 +1836,7 @@ class Arena {
     f.collidesWith = filt.collides_with;
     f.membership = filt.membership;
     f.hasMembership = filt.has_membership != 0;
+    f.includeTriggers = filt.include_triggers != 0;
     f.nIgnore = filt.n_ignore;
     for (int k = 0; k < filt.n_ignore; k++) f.ignore[k] = filt.ignore[k];
     const size_t qb = align256(size_t(n) * sizeof(CastQuery)), bb = align256(size_t(n) * 8);
@@ -1859,8 +1889,10 @@ class Arena {
     for (int w : lastActive) wactiveHost[w] = -1;
     lastActive.clear();
     int nb = 0, nj = 0, maxIter = 0;
+    tickTriggers = false;
     for (size_t a = 0; a < act.size(); a++) {
       const WorldRec& R = W[act[a]];
+      tickTriggers |= R.triggers;
       activeHost[a] = make_int4(act[a], nb, nj, 0);
       wactiveHost[act[a]] = int(a);
       nb += R.nBodies;

@@ -46,7 +46,7 @@ __global__ void k_read_selected(BodyPtrs bd, const WorldDev* __restrict__ worlds
     const WorldDev& W = worlds[meta.x];
     o[0] = p.x; o[1] = p.y; o[2] = p.z; o[3] = sz.w;
     o[4] = q.x; o[5] = q.y; o[6] = q.z; o[7] = q.w;
-    o[8] = p0.x; o[9] = p0.y; o[10] = p0.z; o[11] = 0.f;
+    o[8] = p0.x; o[9] = p0.y; o[10] = p0.z; o[11] = (bd.sleep[i] & BODY_TRIGGER) ? 1.f : 0.f;  // isTrigger
     o[12] = q0.x; o[13] = q0.y; o[14] = q0.z; o[15] = q0.w;
     o[16] = sz.x; o[17] = sz.y; o[18] = sz.z; o[19] = (bd.sleep[i] & SLEEP_ASLEEP) ? 0.f : m.x;  // effective mass
     o[20] = m.y; o[21] = m.z; o[22] = m.w; o[23] = p.w;
@@ -456,6 +456,14 @@ int avbd_world_set_restitution(avbd_world* w, const uint32_t* indices, int32_t n
   REQUIRE(w && (n == 0 || (indices && values)), "null argument");
   bind(w->A->ctx);
   w->A->setRestitution(w->w, indices, n, values);
+  API_END
+}
+
+int avbd_world_set_sensor(avbd_world* w, const uint32_t* indices, int32_t n, int32_t enabled) {
+  API_BEGIN
+  REQUIRE(w && (n == 0 || indices), "null argument");
+  bind(w->A->ctx);
+  w->A->setSensor(w->w, indices, n, enabled != 0);
   API_END
 }
 

@@ -55,7 +55,14 @@ constexpr int FLAG_RESTITUTION = 8;  // some body has restitution > 0: run the b
 constexpr int FLAG_SLEEP = 16;       // island sleeping after each step (sleep.cu)
 constexpr int SLEEP_ASLEEP = 1;      // the body sleeps: the solve leaves it where it is
 constexpr int SLEEP_ALLOW = 2;       // allowSleep (a body without it keeps its island awake)
+constexpr int BODY_TRIGGER = 4;      // isTrigger: its contacts are reported but apply no forces
 constexpr int FLAG_EVENTS = 32;      // contact begin/end events after each step (events.cu)
+// A pair with a trigger body (src/native/cpu/cpuPhysics3D.js:148-156, sleeping.js:54,
+// restitution.js:68): its manifold and contacts exist (events, queries) but it joins no constraint
+// list (no primal or dual rows, no colouring edge, no bounce) and links no sleeping island.
+__host__ __device__ __forceinline__ bool trigger_pair(const int* bits, int a, int b) {
+  return bits && (((a >= 0 ? bits[a] : 0) | bits[b]) & BODY_TRIGGER);
+}
 // A watch word: bit 0 = the body reports its contacts; the bits above count its lifetimes
 // (resetContactHistory adds 2), so a changed word restarts the body's contact history.
 constexpr uint32_t WATCH_ON = 1u;
@@ -82,7 +89,7 @@ struct BodyPtrs {
   float4 *vel, *ang, *vprev, *size, *mass;
   int4* meta;
   float* restitution;  // per body (0 for most)
-  int* sleep;          // per body: SLEEP_ASLEEP | SLEEP_ALLOW
+  int* sleep;          // per body: SLEEP_ASLEEP | SLEEP_ALLOW | BODY_TRIGGER
   float* sleepTime;    // per body: seconds its island has been quiet (FLAG_SLEEP worlds)
   uint32_t *watch, *watchPrev;  // per body: contact-event watch word now and at the last event pass
   __host__ __device__ __forceinline__ float4& pos(int i) const { return pose[2 * size_t(i)]; }
@@ -121,6 +128,7 @@ struct Tick {
   int* pairPrefix;      // [nActive + 1] scanned pair counts of the active worlds
   int* pairN;           // [2 * maxWorlds]: pairs of world w in buffer k at [k * maxWorlds + w]
   int* wover;           // world -> pair slots needed when its region overflowed (0: fits)
+  const int* triggerBits;  // the per-body words when a stepped world has trigger bodies, else null
   int maxWorlds;
   int slotStride;       // pair slots per buffer
   int bodyStride;       // colour entries per buffer
@@ -304,7 +312,7 @@ struct CastQuery {
 };
 struct CastFilter {
   uint32_t collidesWith, membership;
-  int hasMembership, nIgnore;
+  int hasMembership, nIgnore, includeTriggers;
   uint32_t ignore[16];
 };
 // nearest hit of each query among bodies [off, off + nb): out[2q] = (normal, distance or -1),

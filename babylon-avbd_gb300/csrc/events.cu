@@ -22,14 +22,14 @@ namespace avbd {
 namespace {
 
 __device__ __forceinline__ void emit(const EventBufs& ev, int w, uint32_t kind, int a, int b, int step, V3 point,
-                                     float impulse, V3 n) {
+                                     float impulse, V3 n, bool trigger) {
   const int e = atomicAdd(&ev.count[w], 1);
   if (e >= ev.cap[w]) return;
   float4* r = ev.region[w] + size_t(EVENT_FLOAT4) * e;
   r[0] = make_float4(__uint_as_float(kind), __uint_as_float(uint32_t(a)), __uint_as_float(uint32_t(b)),
                      __uint_as_float(uint32_t(step)));
   r[1] = f4(point, impulse);
-  r[2] = f4(n, 0.f);
+  r[2] = f4(n, trigger ? 1.f : 0.f);  // isTrigger
 }
 
 __global__ void k_events_begin(BodyPtrs bd, const WorldDev* __restrict__ worlds, PairPtrs P, Tick t,
@@ -60,8 +60,10 @@ __global__ void k_events_begin(BodyPtrs bd, const WorldDev* __restrict__ worlds,
       point = point + (rotate(qA, v3(c4[0])) + v3(pA));
       force += c4[3].x;
     }
-    emit(ev, w, EVENT_BEGIN, a - W.bodyOff, b - W.bodyOff, ev.step[w] + 1, vdiv(point, float(nc)), fabsf(force) * W.dt,
-         v3(P.basis[3 * p]));
+    // a trigger pair reports no impulse (src/native/cpu/world.js:757-762)
+    const bool trig = ((bd.sleep[a] | bd.sleep[b]) & BODY_TRIGGER) != 0;
+    emit(ev, w, EVENT_BEGIN, a - W.bodyOff, b - W.bodyOff, ev.step[w] + 1, vdiv(point, float(nc)),
+         trig ? 0.f : fabsf(force) * W.dt, v3(P.basis[3 * p]), trig);
   }
 }
 
@@ -83,7 +85,8 @@ __global__ void k_events_end(BodyPtrs bd, const WorldDev* __restrict__ worlds, P
       if (bd.watch[a] != pa || bd.watch[b] != pb) continue;  // history restarted
       const int cp = ncur > 0 ? find_pair(P.pair, curBase, ncur, pr) : -1;
       if (cp >= 0 && P.count[cp] > 0) continue;  // still touching
-      emit(ev, w, EVENT_END, a - W.bodyOff, b - W.bodyOff, ev.step[w] + 1, V3{0.f, 0.f, 0.f}, 0.f, V3{0.f, 0.f, 0.f});
+      emit(ev, w, EVENT_END, a - W.bodyOff, b - W.bodyOff, ev.step[w] + 1, V3{0.f, 0.f, 0.f}, 0.f, V3{0.f, 0.f, 0.f},
+             ((bd.sleep[a] | bd.sleep[b]) & BODY_TRIGGER) != 0);
     }
   }
 }

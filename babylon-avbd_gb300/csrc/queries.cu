@@ -175,6 +175,7 @@ __device__ Hit trace(const BodyPtrs& bd, int i, const CastQuery& q) {
 __device__ __forceinline__ bool filtered(const BodyPtrs& bd, int i, int local, const CastFilter& f) {
   const int4 m = bd.meta[i];  // (world, shape, group, collidesWith)
   if ((uint32_t(m.z) & f.collidesWith) == 0u) return true;
+  if (!f.includeTriggers && (bd.sleep[i] & BODY_TRIGGER)) return true;  // queries.js:229-233
   if (f.hasMembership && (f.membership == 0u || (uint32_t(m.w) & f.membership) == 0u)) return true;
   for (int k = 0; k < f.nIgnore; k++)
     if (int(f.ignore[k]) == local) return true;

@@ -81,6 +81,7 @@ __device__ __forceinline__ bool sleep_edge(const BodyPtrs& bd, const WorldDev* w
     b = int(key & 0xffffffffull);
     if (t.wactive[bd.meta[b].x] < 0) return false;  // world not stepped this tick
   }
+  if (trigger_pair(t.triggerBits, a, b)) return false;  // sleeping.js:54
   w = bd.meta[b].x;
   return (worlds[w].flags & FLAG_SLEEP) != 0;
 }

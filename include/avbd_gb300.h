@@ -109,6 +109,9 @@ typedef struct avbd_scene_desc {
   const float* cons_p3;          /* n_cons [none] spring: breakStrain, the strain limit (<= 0 or
                                     INFINITY: none). A spring past either limit at the start of
                                     a step tears for good (src/gpu/springMaterial.js) */
+  const int32_t* is_trigger;     /* n [0] isTrigger option (scenes.js:69-75): its contacts are
+                                    reported (events, readSelectedBodies word 11) but apply no
+                                    forces, bounce or sleep links (cpuPhysics3D.js:148-156) */
 } avbd_scene_desc;
 
 /* readCounters() of src/vendor/three-avbd-lib/solver3D.ts:1460-1463 plus engine state. */
@@ -261,7 +264,7 @@ typedef struct avbd_cast_filter {
   uint32_t collides_with;   /* bodies whose group & collides_with != 0 [0xffffffff] */
   uint32_t membership;      /* with has_membership: bodies whose collidesWith & membership != 0 */
   int32_t has_membership;
-  int32_t include_triggers; /* accepted for the interface; this engine has no trigger bodies */
+  int32_t include_triggers; /* trigger bodies are skipped unless nonzero [1 without a filter] */
   int32_t n_ignore;         /* <= 16 body indices skipped */
   uint32_t ignore[16];
 } avbd_cast_filter;
@@ -280,6 +283,9 @@ int avbd_world_set_filters(avbd_world* w, const uint32_t* indices, int32_t n, co
 /* setRestitution per body (src/native/cpu/world.js:343-351; editBodies' restitution property):
  * values in [0, 1]; the world wakes. */
 int avbd_world_set_restitution(avbd_world* w, const uint32_t* indices, int32_t n, const float* values);
+/* setSensor(index, enabled) (src/native/cpu/world.js:342-350; editBodies' isTrigger property): the
+ * bodies become (enabled != 0) or stop being triggers; the world wakes. */
+int avbd_world_set_sensor(avbd_world* w, const uint32_t* indices, int32_t n, int32_t enabled);
 /* setMotor(slot, {speed, maxTorque}) (src/gpu/appGpuSolver3D.js:547-562, src/native/cpu/world.js:
  * 360-388): slot is the joint index of an AVBD_CONS_MOTOR constraint; mask bit 0 sets the speed,
  * bit 1 the torque bound (finite, >= 0). The world wakes. */

@@ -220,6 +220,7 @@ template <class R> struct Body {
   R mass = 0, moment[3] = {0, 0, 0}, friction = 0, radius = 0, restitution = 0;
   int shape = SHAPE_BOX;
   bool sleeping = false, allowSleep = true;  // sleeping: skipped by the solve, as a static body
+  bool isTrigger = false;  // contacts reported, no forces (cpuPhysics3D.js:148-156)
   uint32_t group = 0xffffffffu, mask = 0xffffffffu;
   std::vector<int> forces;  // force ids, in link order (newest last)
 };
@@ -819,6 +820,7 @@ template <class R> class Solver {
     }
   }
   void manifoldPrimal(const Force<R>& f, int body, Sys& sys) const {
+    if (triggerForce(f)) return;
     Disp d;
     computeDisplacements(f, d);
     const bool isA = body == f.a;
@@ -843,6 +845,7 @@ template <class R> class Solver {
     }
   }
   void manifoldDual(Force<R>& f) {
+    if (triggerForce(f)) return;
     Disp d;
     computeDisplacements(f, d);
     Eval e;
@@ -987,12 +990,18 @@ template <class R> class Solver {
   struct Graph { std::vector<int> start, nbr; };
   // Dynamic-neighbour graph and the canonical per-body constraint order (joints by jid, then
   // manifolds by the other body), the order the GPU engine stamps in.
+  // A constraint touching a trigger body (its manifolds apply no forces, no constraint joins a
+  // sleeping island through it; cpuPhysics3D.js:148-156, sleeping.js:54, restitution.js:68).
+  bool triggerForce(const Force<R>& f) const {
+    return (f.a >= 0 && bodies[f.a].isTrigger) || (f.b >= 0 && bodies[f.b].isTrigger);
+  }
   void canonicalLists(std::vector<std::vector<int>>& lists) const {
     const int n = int(bodies.size());
     lists.assign(n, {});
     for (int id : forces) {
       const Force<R>& f = *store[id];
       if (f.type == F_IGNORE) continue;
+      if (f.type == F_MANIFOLD && triggerForce(f)) continue;
       for (int body : {f.a, f.b})
         if (body >= 0 && bodies[body].mass > 0) lists[body].push_back(id);
     }
@@ -1173,7 +1182,7 @@ template <class R> class Solver {
     std::vector<Bounce> bs;
     for (int id : forces) {
       const Force<R>& f = *store[id];
-      if (f.type != F_MANIFOLD || f.contacts.empty()) continue;
+      if (f.type != F_MANIFOLD || f.contacts.empty() || triggerForce(f)) continue;
       const R e = std::max(bodies[f.a].restitution, bodies[f.b].restitution);
       if (!(e > 0)) continue;
       Bounce B;
@@ -1379,7 +1388,7 @@ template <class R> class Solver {
     auto dyn = [&](int i) { return bodies[i].mass > 0; };
     for (int id : forces) {
       const Force<R>& f = *store[id];
-      if (f.broken) continue;
+      if (f.broken || triggerForce(f)) continue;
       if (f.type == F_MANIFOLD && f.contacts.empty()) continue;
       const int a = f.a, b = f.b;
       if (a < 0) support[b] = 1;

@@ -26,7 +26,7 @@ class _Scene(C.Structure):
                 ("friction", _dp), ("radius", _dp), ("shape", _ip), ("group", _up), ("mask", _up),
                 ("n_cons", C.c_int), ("kind", _ip), ("ca", _ip), ("cb", _ip), ("ra", _dp),
                 ("rb", _dp), ("p0", _dp), ("p1", _dp), ("p2", _dp), ("restitution", _dp),
-                ("allow_sleep", _ip), ("p3", _dp)]
+                ("allow_sleep", _ip), ("p3", _dp), ("is_trigger", _ip)]
 
 
 class _Params(C.Structure):
@@ -88,6 +88,7 @@ def lib():
         L.oracle_world_set_motor.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_double]
         L.oracle_world_set_motor.restype = C.c_int
         L.oracle_world_release_joints.argtypes = [C.c_void_p, _ip, C.c_int]
+        L.oracle_world_set_sensor.argtypes = [C.c_void_p, _ip, C.c_int, C.c_int]
         L.oracle_world_set_spring_material.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_double]
         L.oracle_world_set_spring_material.restype = C.c_int
         L.oracle_world_set_world_anchor.argtypes = [C.c_void_p, C.c_int, _dp]
@@ -134,7 +135,8 @@ class OracleWorld:
                    u32(scene.mask), scene.n_cons, i32(scene.kind), i32(scene.ca), i32(scene.cb),
                    d(scene.ra), d(scene.rb), d(scene.p0), d(scene.p1), d(scene.p2),
                    d(scene.restitution_or_zero()), i32(scene.allow_sleep_or_one()),
-                   d(scene.p3_or_none() if hasattr(scene, "p3_or_none") else np.zeros(scene.n_cons)))
+                   d(scene.p3_or_none() if hasattr(scene, "p3_or_none") else np.zeros(scene.n_cons)),
+                   i32(scene.is_trigger_or_zero() if hasattr(scene, "is_trigger_or_zero") else np.zeros(scene.n_bodies)))
         prm = _Params(p.dt, p.gravity, (C.c_double * 3)(*p.up), p.iterations, p.alpha, p.beta_lin,
                       p.beta_ang, p.gamma, int(app), int(p.mass_penalty), int(p.face_bias),
                       int(colored), int(p.color_rounds), int(bool(p.sleeping)), float(p.sleep_speed),
@@ -273,6 +275,10 @@ class OracleWorld:
         """releaseJoints of these joint slots."""
         j = np.ascontiguousarray(np.asarray(jids, dtype=np.int32).reshape(-1))
         lib().oracle_world_release_joints(self.h, _ptr(j, C.c_int), j.size)
+
+    def set_sensor(self, indices, enabled):
+        i = np.ascontiguousarray(np.asarray(indices, dtype=np.int32).reshape(-1))
+        lib().oracle_world_set_sensor(self.h, _ptr(i, C.c_int), i.size, int(bool(enabled)))
 
     def set_spring_material(self, jid, break_strain=None, break_force=None):
         mask = (1 if break_strain is not None else 0) | (2 if break_force is not None else 0)

@@ -42,6 +42,7 @@ struct oracle_scene {
   const double* restitution;  // n (null: 0)
   const int32_t* allow_sleep;  // n (null: 1)
   const double* p3;            // n_cons spring: breakStrain (null, <= 0 or inf: none); p2: breakForce
+  const int32_t* is_trigger;   // n (null: 0)
 };
 
 struct oracle_params {
@@ -97,6 +98,7 @@ template <class R> static Solver<R>* build(const oracle_scene* s, const oracle_p
     b.mask = s->mask ? s->mask[i] : 0xffffffffu;
     b.restitution = s->restitution ? R(s->restitution[i]) : R(0);
     b.allowSleep = s->allow_sleep ? s->allow_sleep[i] != 0 : true;
+    b.isTrigger = s->is_trigger ? s->is_trigger[i] != 0 : false;
     w->addBody(b);
   }
   for (int c = 0; c < s->n_cons; c++) {
@@ -403,6 +405,10 @@ extern "C" int oracle_world_capture_frame(void* h, int jid, int spring) {
   int ok = 0;
   DISPATCH(h, ok = S.captureFrame(jid, spring != 0) ? 1 : 0);
   return ok;
+}
+
+extern "C" void oracle_world_set_sensor(void* h, const int32_t* idx, int n, int enabled) {
+  DISPATCH(h, for (int k = 0; k < n; k++) S.bodies[idx[k]].isTrigger = enabled != 0);
 }
 
 // The angular rows' atan2 restatement, elementwise (fp64 != 0: double, else float).

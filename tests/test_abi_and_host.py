@@ -251,8 +251,9 @@ def test_stage_properties_validation():
     assert [p["index"] for p in props] == [1, 2, 3]
     assert props[0]["restitution"] == 0.5 and props[1]["group"] == 4 and props[2]["allowSleep"] is False
     assert stage_edits(edits, 5, 0.5, allow_properties=True).shape == (1, 12)
+    assert stage_properties([{"body": 4, "isTrigger": True}], 5)[0]["isTrigger"] is True
     for bad in ({"body": 0, "restitution": 1.5}, {"body": 0, "collidesWith": 3}, {"body": 0, "allowSleep": 1},
-                {"body": 0, "isTrigger": True}, {"body": 7, "group": 1}):
+                {"body": 0, "isTrigger": 1}, {"body": 7, "group": 1}):
         with pytest.raises(ValueError):
             stage_properties([bad], 5)
 
