@@ -159,6 +159,7 @@ bool Scene(napi_env env, napi_value s, napi_value p, avbd_scene_desc* d, avbd_pa
   d->restitution = Field<float>(env, s, "restitution");
   d->allow_sleep = Field<int32_t>(env, s, "allowSleep");
   d->cons_p3 = Field<float>(env, s, "consP3");
+  d->is_trigger = Field<int32_t>(env, s, "isTrigger");
   q->dt = float(Number(env, p, "dt", 1.0 / 60.0));
   q->gravity = float(Number(env, p, "gravity", -10.0));
   const float* up = Field<float>(env, p, "up");
@@ -337,6 +338,14 @@ napi_value SetRestitution(napi_env env, napi_callback_info info) {  // (w, Uint3
   if (!Typed(env, argv[1], &idx, &n) || !Typed(env, argv[2], &e, &ne)) return nullptr;
   if (ne != n) return Throw(env, "restitution values must match the indices");
   CALL(avbd_world_set_restitution(w, idx, int32_t(n), e));
+  return nullptr;
+}
+napi_value SetSensor(napi_env env, napi_callback_info info) {  // (w, Uint32Array, enabled)
+  WORLD_ARG(3);
+  const uint32_t* idx;
+  size_t n;
+  if (!Typed(env, argv[1], &idx, &n)) return nullptr;
+  CALL(avbd_world_set_sensor(w, idx, int32_t(n), Int(env, argv[2])));
   return nullptr;
 }
 napi_value SetMotor(napi_env env, napi_callback_info info) {  // (w, slot, speed|undefined, maxTorque|undefined)
@@ -591,7 +600,7 @@ napi_value Init(napi_env env, napi_value exports) {
              {"edit", Edit},                   {"flushEdits", FlushEdits},         {"readSelected", ReadSelected},
              {"readState", ReadState},         {"setPoses", SetPoses},             {"setVelocities", SetVelocities},
              {"readCounters", ReadCounters},   {"readJoints", ReadJoints},         {"setFilters", SetFilters},
-             {"setRestitution", SetRestitution}, {"setMotor", SetMotor},         {"releaseJoints", ReleaseJoints},
+             {"setRestitution", SetRestitution}, {"setSensor", SetSensor},       {"setMotor", SetMotor},         {"releaseJoints", ReleaseJoints},
              {"setSpringMaterial", SetSpringMaterial}, {"setWorldAnchor", SetWorldAnchor},
              {"captureFrames", CaptureFrames},
              {"watchContacts", WatchContacts}, {"readContactEvents", ReadContactEvents},

@@ -68,7 +68,7 @@ export function packScene(scene, options = {}) {
     velocity: new Float32Array(3 * n), angularVelocity: new Float32Array(3 * n), prevVelocity: new Float32Array(3 * n),
     mass: new Float32Array(n), moment: new Float32Array(3 * n), friction: new Float32Array(n), radius: new Float32Array(n),
     shape: new Int32Array(n), group: new Uint32Array(n), collidesWith: new Uint32Array(n),
-    restitution: new Float32Array(n), allowSleep: new Int32Array(n),
+    restitution: new Float32Array(n), allowSleep: new Int32Array(n), isTrigger: new Int32Array(n),
   };
   order.forEach((i, s) => {
     const b = all[i];
@@ -87,7 +87,7 @@ export function packScene(scene, options = {}) {
     a.collidesWith[s] = b.collidesWith ?? 0xffffffff;
     a.restitution[s] = b.restitution ?? 0;
     a.allowSleep[s] = b.allowSleep === false ? 0 : 1;
-    if (b.isTrigger) throw Error("triggers are not supported by the gb300 backend");
+    a.isTrigger[s] = b.isTrigger ? 1 : 0;
   });
   // joints, springs and ignore pairs in creation order (their order is the engine's joint id)
   const cons = ref.forces.filter((f) => f instanceof Joint || f instanceof Spring || f instanceof IgnoreCollision);
@@ -280,8 +280,12 @@ class Gb300World {
     this.assertLive();
     addon.releaseJoints(this.handle, Int32Array.from(slots));
   }
-  setSensor() {
-    throw Error("triggers are not supported by the gb300 backend");
+  /** setSensor(index, enabled) (src/native/cpu/world.js:342-350). */
+  setSensor(index, enabled) {
+    this.liveIndex(index);
+    if (typeof enabled !== "boolean") throw Error("isTrigger must be a boolean");
+    addon.setSensor(this.handle, Uint32Array.of(index), enabled ? 1 : 0);
+    return this;
   }
   setSleepEnabled(index, enabled) {
     this.liveIndex(index);
@@ -321,7 +325,7 @@ class Gb300World {
       events.push({
         type: records[o] === 1 ? "begin" : "end", kind: records[o], a: records[o + 1], b: records[o + 2],
         step: records[o + 3], point: [f[o + 4], f[o + 5], f[o + 6]], impulse: f[o + 7],
-        normal: [f[o + 8], f[o + 9], f[o + 10]], isTrigger: false,
+        normal: [f[o + 8], f[o + 9], f[o + 10]], isTrigger: f[o + 11] !== 0,
       });
     return { events, dropped, full };
   }
