@@ -37,10 +37,11 @@ def touching(state, watch) -> set:
     return out
 
 
-def step_events(prev_set, watch_prev, state, watch, step, dt, normal_of):
+def step_events(prev_set, watch_prev, state, watch, step, dt, normal_of, triggers=None):
     """Events of one step: (list of (kind, a, b, step, point, impulse, normal), this step's set).
     `state` is the world's state exported after the step, `normal_of(a, b)` the manifold normal
-    of the pair in that step."""
+    of the pair in that step. A pair with a trigger body (`triggers[i]`) reports no impulse
+    (src/native/cpu/world.js:757-762)."""
     events = []
     now = set()
     first = np.concatenate([[0], np.cumsum(state["mcount"])])
@@ -59,7 +60,9 @@ def step_events(prev_set, watch_prev, state, watch, step, dt, normal_of):
         for k in range(first[m], first[m + 1]):
             point += _turn(qA, np.asarray(state["cra"][k], dtype=np.float64)) + pA
             force += float(state["clam"][k][0])
-        events.append((BEGIN, a, b, step, point / c, abs(force) * dt, np.asarray(normal_of(a, b), dtype=np.float64)))
+        trig = triggers is not None and bool(triggers[a] or triggers[b])
+        events.append((BEGIN, a, b, step, point / c, 0.0 if trig else abs(force) * dt,
+                       np.asarray(normal_of(a, b), dtype=np.float64)))
     for a, b in sorted(prev_set):
         if not (watch[a] == watch_prev[a] and watch[b] == watch_prev[b]):
             continue

@@ -172,8 +172,9 @@ def trace(pos, quat, size, shape, origin, direction, radius, max_distance):
 
 
 def cast(state, shape, size, group, mask, origin, direction, radius=0.0, max_distance=3e38,
-         collides_with=0xFFFFFFFF, membership=None, ignore=()):
-    """Nearest hit: (index, t, normal, second-best t) or None; state: position, rotation arrays."""
+         collides_with=0xFFFFFFFF, membership=None, ignore=(), triggers=None, include_triggers=True):
+    """Nearest hit: (index, t, normal, second-best t) or None; state: position, rotation arrays.
+    Trigger bodies (`triggers[i]`) are skipped unless include_triggers (queries.js:229-233)."""
     ln = math.sqrt(sum(float(x) ** 2 for x in direction))
     dvec = tuple(float(x) / ln for x in direction)
     o = tuple(float(x) for x in origin)
@@ -185,6 +186,8 @@ def cast(state, shape, size, group, mask, origin, direction, radius=0.0, max_dis
         if membership is not None and (membership == 0 or not (int(mask[i]) & membership)):
             continue
         if i in ignore:
+            continue
+        if triggers is not None and triggers[i] and not include_triggers:
             continue
         t, n = trace(tuple(map(float, state["position"][i])), tuple(map(float, state["rotation"][i])),
                      tuple(map(float, size[i])), int(shape[i]), o, dvec, float(radius), float(max_distance))
