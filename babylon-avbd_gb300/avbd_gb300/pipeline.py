@@ -1018,6 +1018,78 @@ class Batch:
         slots = _joint_slots(self._kinds[world], constraints)
         L.check(L.lib().avbd_batch_release_joints(self._h, int(world), L.iptr(slots), int(slots.size)))
 
+    def _world(self, world: int) -> int:
+        if not 0 <= int(world) < self.worldCount:
+            raise ValueError("world index out of range")
+        return int(world)
+
+    def setFilters(self, world: int, indices, groups, collidesWith):
+        """World.setFilters for world `world` of the batch (world-local body indices)."""
+        w = self._world(world)
+        idx = np.asarray(indices, dtype=np.int64).reshape(-1)
+        g = np.asarray(groups, dtype=np.int64).reshape(-1)
+        m = np.asarray(collidesWith, dtype=np.int64).reshape(-1)
+        if not (idx.size == g.size == m.size):
+            raise ValueError("Filter arrays must have matching lengths")
+        if idx.size and (idx.min() < 0 or idx.max() >= self.bodyCounts[w]):
+            raise ValueError("A live body index is required")
+        for a in (g, m):
+            if a.size and (a.min() < 0 or a.max() > 0xFFFFFFFF):
+                raise ValueError("Collision masks must be unsigned 32-bit integers")
+        ia, ga, ma = (np.ascontiguousarray(a.astype(np.uint32)) for a in (idx, g, m))
+        L.check(L.lib().avbd_batch_set_filters(self._h, w, L.uptr(ia), int(ia.size), L.uptr(ga), L.uptr(ma)))
+
+    def setRestitution(self, world: int, indices, values):
+        """World.setRestitution for world `world` of the batch."""
+        w = self._world(world)
+        idx = _indices(indices, self.bodyCounts[w])
+        val = np.ascontiguousarray(np.asarray(values, dtype=np.float32).reshape(-1))
+        if idx.size != val.size:
+            raise ValueError("Restitution arrays must have matching lengths")
+        if val.size and not (np.all(val >= 0) and np.all(val <= 1)):
+            raise ValueError("restitution must be between 0 and 1")
+        L.check(L.lib().avbd_batch_set_restitution(self._h, w, L.uptr(idx), int(idx.size), L.fptr(val)))
+
+    def setSensor(self, world: int, index, enabled):
+        """World.setSensor for world `world` of the batch."""
+        w = self._world(world)
+        if not isinstance(enabled, bool):
+            raise ValueError("isTrigger must be a boolean")
+        idx = _indices([index], self.bodyCounts[w])
+        L.check(L.lib().avbd_batch_set_sensor(self._h, w, L.uptr(idx), 1, int(enabled)))
+
+    def setSpringMaterial(self, world: int, constraint, breakStrain=None, breakForce=None):
+        """World.setSpringMaterial for world `world` of the batch."""
+        from .scene import KIND_SPRING, spring_material
+        w = self._world(world)
+        kinds = self._kinds[w]
+        c = int(constraint)
+        if not 0 <= c < len(kinds) or kinds[c] != KIND_SPRING:
+            raise ValueError("Spring material requires an active spring slot")
+        m = spring_material(math.inf if breakStrain is None else breakStrain,
+                            math.inf if breakForce is None else breakForce)
+        mask = (1 if breakStrain is not None else 0) | (2 if breakForce is not None else 0)
+        slot = int(_joint_slots(kinds, [c])[0])
+        L.check(L.lib().avbd_batch_set_spring_material(self._h, w, slot, mask, m["breakStrain"], m["breakForce"]))
+
+    def setWorldAnchor(self, world: int, constraint, point):
+        """World.setWorldAnchor for world `world` of the batch."""
+        w = self._world(world)
+        p = np.ascontiguousarray(np.asarray(point, dtype=np.float32).reshape(-1))
+        if p.size != 3 or not np.all(np.isfinite(p)):
+            raise ValueError("A world joint and finite xyz anchor are required")
+        slot = int(_joint_slots(self._kinds[w], [constraint])[0])
+        L.check(L.lib().avbd_batch_set_world_anchor(self._h, w, slot, L.fptr(p)))
+
+    def captureConstraintFrames(self, world: int, entries):
+        """World.captureConstraintFrames for world `world` of the batch."""
+        w = self._world(world)
+        cons = [int(e["slot"]) if isinstance(e, dict) else int(e) for e in entries]
+        spring = [1 if isinstance(e, dict) and e.get("spring") else 0 for e in entries]
+        slots = _joint_slots(self._kinds[w], cons)
+        sp = np.ascontiguousarray(np.asarray(spring, dtype=np.int32))
+        L.check(L.lib().avbd_batch_capture_frames(self._h, w, L.iptr(slots), L.iptr(sp), int(slots.size)))
+
     def readJoints(self, world: int) -> np.ndarray:
         if not 0 <= world < self.worldCount:
             raise ValueError("world index out of range")

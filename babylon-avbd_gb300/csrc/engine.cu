@@ -802,6 +802,60 @@ int avbd_batch_release_joints(avbd_batch* b, int32_t world, const int32_t* slots
   API_END
 }
 
+#define BATCH_WORLD(b, world)                                                   \
+  REQUIRE(b, "null batch");                                                     \
+  REQUIRE(world >= 0 && world < int32_t(b->worlds.size()), "world index out of range"); \
+  bind(b->A->ctx)
+
+int avbd_batch_set_filters(avbd_batch* b, int32_t world, const uint32_t* indices, int32_t n, const uint32_t* groups,
+                           const uint32_t* collides_with) {
+  API_BEGIN
+  BATCH_WORLD(b, world);
+  REQUIRE(n == 0 || (indices && groups && collides_with), "null argument");
+  b->A->setFilters(b->worlds[world], indices, n, groups, collides_with);
+  API_END
+}
+
+int avbd_batch_set_restitution(avbd_batch* b, int32_t world, const uint32_t* indices, int32_t n, const float* values) {
+  API_BEGIN
+  BATCH_WORLD(b, world);
+  REQUIRE(n == 0 || (indices && values), "null argument");
+  b->A->setRestitution(b->worlds[world], indices, n, values);
+  API_END
+}
+
+int avbd_batch_set_sensor(avbd_batch* b, int32_t world, const uint32_t* indices, int32_t n, int32_t enabled) {
+  API_BEGIN
+  BATCH_WORLD(b, world);
+  REQUIRE(n == 0 || indices, "null argument");
+  b->A->setSensor(b->worlds[world], indices, n, enabled != 0);
+  API_END
+}
+
+int avbd_batch_set_spring_material(avbd_batch* b, int32_t world, int32_t slot, int32_t mask, float break_strain,
+                                   float break_force) {
+  API_BEGIN
+  BATCH_WORLD(b, world);
+  b->A->setSpringMaterial(b->worlds[world], slot, mask, break_strain, break_force);
+  API_END
+}
+
+int avbd_batch_set_world_anchor(avbd_batch* b, int32_t world, int32_t slot, const float* point) {
+  API_BEGIN
+  BATCH_WORLD(b, world);
+  REQUIRE(point, "null argument");
+  b->A->setWorldAnchor(b->worlds[world], slot, point);
+  API_END
+}
+
+int avbd_batch_capture_frames(avbd_batch* b, int32_t world, const int32_t* slots, const int32_t* spring, int32_t n) {
+  API_BEGIN
+  BATCH_WORLD(b, world);
+  REQUIRE(n == 0 || (slots && spring), "null argument");
+  b->A->captureFrames(b->worlds[world], slots, spring, n);
+  API_END
+}
+
 int avbd_batch_cast(avbd_batch* b, int32_t world, const float* queries, int32_t n, const avbd_cast_filter* filter,
                     float* hits) {
   API_BEGIN

@@ -337,6 +337,17 @@ int avbd_batch_read_joints(avbd_batch* b, int32_t world, float* out);
 int avbd_batch_set_motor(avbd_batch* b, int32_t world, int32_t slot, int32_t mask, float speed, float max_torque);
 /* releaseJoints for world `world` of the batch (as avbd_world_release_joints). */
 int avbd_batch_release_joints(avbd_batch* b, int32_t world, const int32_t* slots, int32_t n);
+/* The world-local property and constraint edits for world `world` of the batch (as the
+ * avbd_world_* forms: set_filters, set_restitution, set_sensor, set_spring_material,
+ * set_world_anchor, capture_frames). */
+int avbd_batch_set_filters(avbd_batch* b, int32_t world, const uint32_t* indices, int32_t n, const uint32_t* groups,
+                           const uint32_t* collides_with);
+int avbd_batch_set_restitution(avbd_batch* b, int32_t world, const uint32_t* indices, int32_t n, const float* values);
+int avbd_batch_set_sensor(avbd_batch* b, int32_t world, const uint32_t* indices, int32_t n, int32_t enabled);
+int avbd_batch_set_spring_material(avbd_batch* b, int32_t world, int32_t slot, int32_t mask, float break_strain,
+                                   float break_force);
+int avbd_batch_set_world_anchor(avbd_batch* b, int32_t world, int32_t slot, const float* point);
+int avbd_batch_capture_frames(avbd_batch* b, int32_t world, const int32_t* slots, const int32_t* spring, int32_t n);
 /* Shape casts against world `world` of the batch (as avbd_world_cast). */
 int avbd_batch_cast(avbd_batch* b, int32_t world, const float* queries, int32_t n, const avbd_cast_filter* filter,
                     float* hits);

@@ -127,3 +127,44 @@ def test_capture_frames_is_bit_equal(pipe):
     with pytest.raises(ValueError):
         w.setSpringMaterial(weld, breakForce=1.0)
     w.destroy()
+
+
+def test_batch_edits_match_the_world_alone(pipe):
+    # the batch forms of the property and constraint edits give a batched world the bits of the
+    # same world edited alone (the other batched world untouched)
+    def scene():
+        sc = AvbdScene3D(timeStep=DT, iterations=10, gravity=-10)
+        sc.addBox([20, 1, 20], density=0, position=[0, -0.5, 0])
+        top = sc.addBox([0.2, 0.2, 0.2], density=0, position=[0, 5, 0])
+        box = sc.addBox([1, 1, 1], position=[0, 4, 0])
+        s = sc.addSpring(top, box, stiffness=200.0, rest=1.0)
+        ball = sc.addSphere(0.4, position=[3, 2, 0])
+        grab = sc.addJoint(None, ball, anchorA=[3, 2.5, 0], anchorB=[0, 0.4, 0], linearStiffness=3000.0)
+        other = sc.addBox([1, 1, 1], position=[-3, 0.5, 0])
+        return sc, box, s, ball, grab, other
+
+    def edits(obj, w, parts):
+        sc, box, s, ball, grab, other = parts
+        args = () if w is None else (w,)
+        obj.setFilters(*args, [other], [2], [2])
+        obj.setRestitution(*args, [ball], [0.5])
+        obj.setSensor(*args, other, True)
+        obj.setSpringMaterial(*args, s, breakForce=8.0)
+        obj.setWorldAnchor(*args, grab, [3.5, 3.0, 0.0])
+        obj.captureConstraintFrames(*args, [{"slot": s, "spring": True}])
+
+    parts = scene()
+    alone = pipe.createSolver(parts[0])
+    alone.step(10)
+    edits(alone, None, parts)
+    alone.step(30)
+    ref = alone.readBodyState()
+    alone.destroy()
+    batch = pipe.createBatch([scene()[0], parts[0]])
+    batch.step(10)
+    edits(batch, 1, parts)
+    batch.step(30)
+    got = batch.readBodyState(1)
+    for k in ("position", "rotation", "velocity", "angular"):
+        assert np.array_equal(got[k], ref[k]), k
+    batch.destroy()
