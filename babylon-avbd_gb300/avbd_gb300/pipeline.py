@@ -515,9 +515,8 @@ class Body:
         return self
 
     def readState(self) -> dict:
-        """Position, rotation, velocity, angular and previous velocity of this body."""
-        st = self.world.readBodyState()
-        return {k: v[self.gpuIndex].copy() for k, v in st.items()}
+        """This body's state as world.readBodyState(index) gives it (runtime.js:234-236)."""
+        return self.world.readBodyState(self.index)
 
 
 class World:
@@ -572,9 +571,20 @@ class World:
         return count
 
     # reads --------------------------------------------------------------------
-    def readBodyState(self) -> dict:
-        """Positions, rotations, velocities, angular and previous velocities (float32)."""
+    def readBodyState(self, index=None) -> dict:
+        """With a body slot: the reference's state of that body (src/native/cpu/world.js:572-588:
+        position, rotation, linearVelocity, angularVelocity, mass, effectiveMass, sleeping).
+        Without one: positions, rotations, velocities, angular and previous velocities of every
+        body (float32 arrays)."""
         self._live()
+        if index is not None:
+            i = int(_indices([index], self.bodyCount)[0])
+            rec = self.readSelectedBodies([i]).reshape(40)
+            sleeping = bool(self.readSleepState()[0][i])
+            return {"position": [float(x) for x in rec[0:3]], "rotation": [float(x) for x in rec[4:8]],
+                    "linearVelocity": [float(x) for x in rec[32:35]],
+                    "angularVelocity": [float(x) for x in rec[36:39]],
+                    "mass": float(self._packed.keep[6][i]), "effectiveMass": float(rec[19]), "sleeping": sleeping}
         n = self.bodyCount
         out = {k: np.zeros((n, 4 if k == "rotation" else 3), dtype=np.float32)
                for k in ("position", "rotation", "velocity", "angular", "prev_velocity")}

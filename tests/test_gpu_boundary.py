@@ -126,11 +126,29 @@ def test_body_handles_route_to_the_world_commands(pipe):
     h.setAngularVelocity([0, 2, 0]).setRestitution(0.5)
     w.step(1)
     st = h.readState()
-    assert np.allclose(st["velocity"], [1, 0, 0], atol=1e-3) and np.allclose(st["angular"], [0, 2, 0], atol=1e-3)
-    assert np.allclose(w.body(a).readState()["velocity"], 0)
+    assert np.allclose(st["linearVelocity"], [1, 0, 0], atol=1e-3) and np.allclose(st["angularVelocity"], [0, 2, 0], atol=1e-3)
+    assert np.allclose(w.body(a).readState()["linearVelocity"], 0)
     h.teleport([9, 0, 0])
     w.step(1)
     assert 9 - 1e-4 <= h.readState()["position"][0] <= 9 + 1 / 60 + 1e-4
     with pytest.raises(ValueError):
         w.body(5)
+    w.destroy()
+
+
+def test_read_body_state_of_one_body(pipe):
+    # src/native/cpu/world.js:572-588: {position, rotation, linearVelocity, angularVelocity, mass,
+    # effectiveMass, sleeping} of one body
+    from avbd_gb300 import AvbdScene3D
+    sc = AvbdScene3D(timeStep=1 / 60, iterations=10, gravity=0)
+    b = sc.addBox([1, 2, 1], density=2, position=[1, 2, 3], velocity=[0.5, 0, 0])
+    w = pipe.createSolver(sc)
+    w.step(2)
+    st = w.readBodyState(b)
+    assert set(st) == {"position", "rotation", "linearVelocity", "angularVelocity", "mass", "effectiveMass",
+                       "sleeping"}
+    assert st["mass"] == 4.0 and st["effectiveMass"] == 4.0 and st["sleeping"] is False
+    assert np.allclose(st["linearVelocity"], [0.5, 0, 0], atol=1e-4) and abs(st["position"][0] - (1 + 1 / 60)) < 1e-4
+    with pytest.raises(ValueError):
+        w.readBodyState(3)
     w.destroy()
