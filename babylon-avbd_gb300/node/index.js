@@ -147,6 +147,7 @@ class Gb300World {
   constructor(ctx, scene, options) {
     const packed = packScene(scene, options);
     this.handle = addon.createWorld(ctx, packed.arrays, packed.params);
+    this.mass = packed.arrays.mass;  // per slot, for readBodyState(index)
     this.dimension = 3;
     this.bodyCount = packed.order.length;
     this.jointCount = packed.jointCount;
@@ -227,9 +228,19 @@ class Gb300World {
   async readBodies() {
     return this.readSelectedBodies(Uint32Array.from({ length: this.bodyCount }, (_, i) => i));
   }
-  async readBodyState() {
+  /** readBodyState(index) (src/native/cpu/world.js:572-588): one body's state, from its 40-float
+   * record (word 19 is its effective mass, 0 while it sleeps); without an index, every body. */
+  async readBodyState(index) {
     this.assertLive();
-    return addon.readState(this.handle, this.bodyCount);
+    if (index === undefined) return addon.readState(this.handle, this.bodyCount);
+    this.liveIndex(index);
+    const r = addon.readSelected(this.handle, Uint32Array.of(index), false);
+    const mass = this.mass[index];
+    return {
+      position: [r[0], r[1], r[2]], rotation: [r[4], r[5], r[6], r[7]],
+      linearVelocity: [r[32], r[33], r[34]], angularVelocity: [r[36], r[37], r[38]],
+      mass, effectiveMass: r[19], sleeping: mass > 0 && r[19] === 0,
+    };
   }
   async readJoints() {
     this.assertLive();
