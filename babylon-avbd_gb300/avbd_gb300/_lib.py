@@ -135,6 +135,7 @@ SIGNATURES = [
     ("avbd_batch_set_filters", C.c_int, [C.c_void_p, C.c_int32, _up, C.c_int32, _up, _up]),
     ("avbd_batch_set_restitution", C.c_int, [C.c_void_p, C.c_int32, _up, C.c_int32, _fp]),
     ("avbd_batch_set_sensor", C.c_int, [C.c_void_p, C.c_int32, _up, C.c_int32, C.c_int32]),
+    ("avbd_batch_set_sleep_enabled", C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32]),
     ("avbd_batch_set_spring_material", C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_float, C.c_float]),
     ("avbd_batch_set_world_anchor", C.c_int, [C.c_void_p, C.c_int32, C.c_int32, _fp]),
     ("avbd_batch_capture_frames", C.c_int, [C.c_void_p, C.c_int32, _ip, _ip, C.c_int32]),

@@ -1163,12 +1163,25 @@ class Batch:
         L.check(L.lib().avbd_batch_set_velocities(self._h, L.uptr(idx), idx.size, L.fptr(v), L.fptr(a)))
 
     def editBodies(self, world: int, edits):
-        """Body edits (world-local indices) of world ``world``, applied at the next step."""
+        """Body edits (world-local indices) of world ``world``, applied at the next step; property
+        keys (restitution, group/collidesWith, allowSleep, isTrigger) apply at once, as
+        World.editBodies does."""
         if not 0 <= world < self.worldCount:
             raise ValueError("world index out of range")
-        rec = stage_edits(edits, self.bodyCounts[world], self._dts[world])
+        edits = list(edits)
+        props = stage_properties(edits, self.bodyCounts[world])
+        rec = stage_edits(edits, self.bodyCounts[world], self._dts[world], allow_properties=True)
         if len(rec):
             L.check(L.lib().avbd_batch_edit(self._h, int(world), L.uptr(rec), int(rec.shape[0])))
+        for p in props:
+            if p["restitution"] is not None:
+                self.setRestitution(world, [p["index"]], [p["restitution"]])
+            if p["group"] is not None:
+                self.setFilters(world, [p["index"]], [p["group"]], [p["collidesWith"]])
+            if p["allowSleep"] is not None:
+                L.check(L.lib().avbd_batch_set_sleep_enabled(self._h, int(world), p["index"], int(p["allowSleep"])))
+            if p["isTrigger"] is not None:
+                self.setSensor(world, p["index"], p["isTrigger"])
         return self
 
     def profile(self, enable: bool = True):

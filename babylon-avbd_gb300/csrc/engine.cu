@@ -832,6 +832,13 @@ int avbd_batch_set_sensor(avbd_batch* b, int32_t world, const uint32_t* indices,
   API_END
 }
 
+int avbd_batch_set_sleep_enabled(avbd_batch* b, int32_t world, int32_t body, int32_t enabled) {
+  API_BEGIN
+  BATCH_WORLD(b, world);
+  b->A->setSleepAllowed(b->worlds[world], body, enabled != 0);
+  API_END
+}
+
 int avbd_batch_set_spring_material(avbd_batch* b, int32_t world, int32_t slot, int32_t mask, float break_strain,
                                    float break_force) {
   API_BEGIN

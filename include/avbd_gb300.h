@@ -344,6 +344,7 @@ int avbd_batch_set_filters(avbd_batch* b, int32_t world, const uint32_t* indices
                            const uint32_t* collides_with);
 int avbd_batch_set_restitution(avbd_batch* b, int32_t world, const uint32_t* indices, int32_t n, const float* values);
 int avbd_batch_set_sensor(avbd_batch* b, int32_t world, const uint32_t* indices, int32_t n, int32_t enabled);
+int avbd_batch_set_sleep_enabled(avbd_batch* b, int32_t world, int32_t body, int32_t enabled);
 int avbd_batch_set_spring_material(avbd_batch* b, int32_t world, int32_t slot, int32_t mask, float break_strain,
                                    float break_force);
 int avbd_batch_set_world_anchor(avbd_batch* b, int32_t world, int32_t slot, const float* point);

@@ -168,3 +168,32 @@ def test_batch_edits_match_the_world_alone(pipe):
     for k in ("position", "rotation", "velocity", "angular"):
         assert np.array_equal(got[k], ref[k]), k
     batch.destroy()
+
+
+def test_batch_property_edits_match_the_world_alone(pipe):
+    def scene():
+        sc = AvbdScene3D(timeStep=DT, iterations=10, gravity=-10)
+        sc.addBox([20, 1, 20], density=0, position=[0, -0.5, 0])
+        a = sc.addSphere(0.4, position=[0, 3, 0])
+        b = sc.addBox([1, 1, 1], position=[2, 0.5, 0])
+        c = sc.addBox([1, 1, 1], position=[-2, 3, 0])
+        return sc, a, b, c
+
+    sc, a, b, c = scene()
+    edits = [{"body": a, "restitution": 0.7}, {"body": b, "isTrigger": True},
+             {"body": c, "group": 2, "collidesWith": 2, "allowSleep": False, "linearVelocity": [1, 0, 0]}]
+    w = pipe.createSolver(sc)
+    w.step(5)
+    w.editBodies(edits)
+    w.step(40)
+    ref = w.readBodyState()
+    w.destroy()
+    batch = pipe.createBatch([scene()[0], sc])
+    batch.step(5)
+    batch.editBodies(1, edits)
+    batch.step(40)
+    got = batch.readBodyState(1)
+    for k in ("position", "rotation", "velocity", "angular"):
+        assert np.array_equal(got[k], ref[k]), k
+    assert got["position"][b, 1] < 0  # the trigger box fell through the ground
+    batch.destroy()
