@@ -52,7 +52,11 @@ class Profile(C.Structure):
     _fields_ = [("steps", C.c_int32), ("pad", C.c_int32), ("ms_collide", C.c_double),
                 ("ms_topology", C.c_double), ("ms_primal", C.c_double), ("ms_dual", C.c_double),
                 ("ms_other", C.c_double), ("primal_launches", C.c_int64), ("launches", C.c_int64),
-                ("bytes_primal", C.c_double), ("bytes_dual", C.c_double), ("bytes_collide", C.c_double)]
+                ("bytes_primal", C.c_double), ("bytes_dual", C.c_double), ("bytes_collide", C.c_double),
+                ("graph_captures", C.c_int64), ("graph_replays", C.c_int64), ("graphs_on", C.c_int32),
+                ("ticks_held", C.c_int32), ("tuned", C.c_int32), ("solve_queue", C.c_int32),
+                ("solve_waves", C.c_int32), ("solve_blocks", C.c_int32), ("radix_bits", C.c_int32),
+                ("pad2", C.c_int32)]
 
 
 class ServerDesc(C.Structure):

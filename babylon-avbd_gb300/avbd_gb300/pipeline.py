@@ -606,8 +606,9 @@ class World:
 
     # ---- body commands (src/native/runtime.js:46-167, src/native/cpu/world.js:145-166)
     def editBodies(self, edits):
-        """Queue a validated batch of body edits for the next step; property edits (restitution,
-        group/collidesWith, allowSleep) apply after the commands, as runtime.js:157-165 does."""
+        """Queue a validated batch of body edits for the next step; property edits apply after the
+        commands in runtime.js:157-165's order (isTrigger, restitution, group/collidesWith,
+        allowSleep)."""
         self._live()
         edits = list(edits)
         props = stage_properties(edits, self.bodyCount)
@@ -615,14 +616,14 @@ class World:
         if len(rec):
             L.check(L.lib().avbd_world_edit(self._h, L.uptr(rec), int(rec.shape[0])))
         for p in props:
+            if p["isTrigger"] is not None:
+                self.setSensor(p["index"], p["isTrigger"])
             if p["restitution"] is not None:
                 self.setRestitution([p["index"]], [p["restitution"]])
             if p["group"] is not None:
                 self.setFilters([p["index"]], [p["group"]], [p["collidesWith"]])
             if p["allowSleep"] is not None:
                 self.setSleepEnabled(p["index"], p["allowSleep"])
-            if p["isTrigger"] is not None:
-                self.setSensor(p["index"], p["isTrigger"])
         return self
 
     def body(self, index) -> Body:
@@ -966,7 +967,7 @@ class World:
         self._live()
         p = L.Profile()
         L.check(L.lib().avbd_world_profile_read(self._h, C.byref(p)))
-        return {k: getattr(p, k) for k, _ in L.Profile._fields_ if k != "pad"}
+        return {k: getattr(p, k) for k, _ in L.Profile._fields_ if not k.startswith("pad")}
 
     def destroy(self):
         if self._h is None:
@@ -1164,8 +1165,8 @@ class Batch:
 
     def editBodies(self, world: int, edits):
         """Body edits (world-local indices) of world ``world``, applied at the next step; property
-        keys (restitution, group/collidesWith, allowSleep, isTrigger) apply at once, as
-        World.editBodies does."""
+        keys (isTrigger, restitution, group/collidesWith, allowSleep, in runtime.js:157-165's order)
+        apply at once, as World.editBodies does."""
         if not 0 <= world < self.worldCount:
             raise ValueError("world index out of range")
         edits = list(edits)
@@ -1174,14 +1175,14 @@ class Batch:
         if len(rec):
             L.check(L.lib().avbd_batch_edit(self._h, int(world), L.uptr(rec), int(rec.shape[0])))
         for p in props:
+            if p["isTrigger"] is not None:
+                self.setSensor(world, p["index"], p["isTrigger"])
             if p["restitution"] is not None:
                 self.setRestitution(world, [p["index"]], [p["restitution"]])
             if p["group"] is not None:
                 self.setFilters(world, [p["index"]], [p["group"]], [p["collidesWith"]])
             if p["allowSleep"] is not None:
                 L.check(L.lib().avbd_batch_set_sleep_enabled(self._h, int(world), p["index"], int(p["allowSleep"])))
-            if p["isTrigger"] is not None:
-                self.setSensor(world, p["index"], p["isTrigger"])
         return self
 
     def profile(self, enable: bool = True):
@@ -1190,7 +1191,7 @@ class Batch:
     def profileRead(self) -> dict:
         p = L.Profile()
         L.check(L.lib().avbd_batch_profile_read(self._h, C.byref(p)))
-        return {k: getattr(p, k) for k, _ in L.Profile._fields_ if k != "pad"}
+        return {k: getattr(p, k) for k, _ in L.Profile._fields_ if not k.startswith("pad")}
 
     def destroy(self):
         if self._h is None:

@@ -19,6 +19,7 @@ import numpy as np
 
 SHAPE_BOX = 0
 SHAPE_SPHERE = 1
+SHAPE_CAPSULE = 2
 
 KIND_JOINT = 0
 KIND_SPRING = 1
@@ -164,6 +165,23 @@ class SceneBuilder:
         b.moment = [inertia, inertia, inertia]
         b.radius = r
         b.shape = SHAPE_SPHERE
+        return i
+
+    # src/gpu/capsuleShape.js:4-41: along local Y, height tip to tip
+    def capsule(self, r, height, density, friction, position, velocity=(0.0, 0.0, 0.0)) -> int:
+        r, height, density = float(r), float(height), float(density)
+        i = self.rigid((2 * r, height, 2 * r), density, friction, position, velocity)
+        b = self.bodies[i]
+        length = height - 2 * r
+        cylinder = math.pi * r * r * length * density
+        caps = (4 / 3) * math.pi * r ** 3 * density
+        b.mass = cylinder + caps
+        axial = (cylinder * r ** 2) / 2 + (caps * 2 * r ** 2) / 5
+        radial = (cylinder * (length ** 2 / 12 + r ** 2 / 4)
+                  + caps * ((2 * r ** 2) / 5 + length ** 2 / 4 + (3 * length * r) / 8))
+        b.moment = [radial, axial, radial]
+        b.radius = height / 2
+        b.shape = SHAPE_CAPSULE
         return i
 
     def joint(self, a, b, ra, rb, stiff_lin=INF, stiff_ang=0.0, fracture=INF) -> int:
@@ -369,6 +387,19 @@ class AvbdScene3D:
                            _positive(options.get("density", 1), "density", True),
                            _positive(options.get("friction", 0.6), "friction", True),
                            _vector(options.get("position", (0, 0, 0)), 3, "position"))
+        return self._configure(i, options)
+
+    def addCapsule(self, radius, height, **options) -> int:
+        """An analytic capsule along local Y; height is the full tip-to-tip extent
+        (scenes.js:180-193)."""
+        self._editable()
+        self._validate(options)
+        r, h = float(radius), float(height)
+        if not (math.isfinite(r) and r > 0 and math.isfinite(h) and h >= 2 * r):
+            raise ValueError("Capsule height must be at least twice its positive radius")
+        i = self._b.capsule(r, h, _positive(options.get("density", 1), "density", True),
+                            _positive(options.get("friction", 0.6), "friction", True),
+                            _vector(options.get("position", (0, 0, 0)), 3, "position"))
         return self._configure(i, options)
 
     def _configure(self, i, options) -> int:

@@ -164,6 +164,12 @@ def world_mix(n_worlds=4096, target=2_100_000, seed=SEED_BASE + 3):
     return worlds, counts, sigma
 
 
+def world_mix_world(index, n_worlds=4096, target=2_100_000, seed=SEED_BASE + 3) -> SceneArrays:
+    """World `index` of world_mix(...) alone (the same scene, without building the others)."""
+    counts, _ = world_counts(n_worlds, target, seed)
+    return lattice_pile(int(counts[index]), (seed * 7919 + index) & 0xFFFFFFFFFFFF)
+
+
 def cloth_wall(seed=SEED_BASE + 2, grid=256, wall=(100, 2, 50)) -> SceneArrays:
     parts = []
     ground = _static_box((300.0, 2.0, 300.0), (0.0, -1.0, 0.0))

@@ -24,9 +24,12 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <deque>
 #include <functional>
 #include <map>
 #include <memory>
@@ -39,6 +42,7 @@
 #include "../../include/avbd_gb300.h"
 #include "engine.cuh"
 #include "angular.cuh"
+#include "tuner.hpp"
 
 using namespace avbd;
 
@@ -58,16 +62,28 @@ struct Error : std::runtime_error {
     if (e_ != cudaSuccess) throw Error(AVBD_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
   } while (0)
 
+// Every device allocation and free bumps this generation: a recorded launch sequence (a CUDA
+// graph of a tick) is valid only while it is unchanged.
+inline std::atomic<long long>& alloc_generation_counter() {
+  static std::atomic<long long> g{0};
+  return g;
+}
+inline long long alloc_generation() { return alloc_generation_counter().load(std::memory_order_relaxed); }
+
 template <class T> inline T* dalloc(size_t n) {
   void* p = nullptr;
   if (n == 0) n = 1;
   cudaError_t e = cudaMalloc(&p, n * sizeof(T));
   if (e != cudaSuccess) throw Error(AVBD_E_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  alloc_generation_counter().fetch_add(1, std::memory_order_relaxed);
   return static_cast<T*>(p);
 }
 
 inline void dfree(void* p) {
-  if (p) cudaFree(p);
+  if (p) {
+    cudaFree(p);
+    alloc_generation_counter().fetch_add(1, std::memory_order_relaxed);
+  }
 }
 
 // First-fit allocator of index ranges [0, cap).
@@ -165,6 +181,8 @@ struct WorldRec {
   int bvhOff = 0, bvhRebuild = 16, sinceBuild = 0;
   bool built = false;
   std::vector<uint32_t> edits;  // body command records waiting for the next step (12 words each)
+  bool wakePending = false;     // queued commands wake the world when they apply
+  bool pinned = false;          // a held tick of this world is being re-run: not to be evicted
   long long steps = 0;          // steps taken
   // contact events (FLAG_EVENTS): device region of evCap events while resident, events already
   // drained to the host (12 words each), events dropped past the capacity
@@ -173,6 +191,18 @@ struct WorldRec {
   std::vector<uint32_t> evHost;
   long long evDropped = 0;
 };
+
+// Solve schedule overrides from the environment (for tests and measurements): AVBD_SOLVE=queue|
+// barrier, AVBD_SOLVE_WAVES, AVBD_SOLVE_BLOCKS, AVBD_SOLVE_WAIT_CYCLES (the tile queue's wait bound),
+// AVBD_SOLVE_WAIT_PROBE (tests: the queue's waits run out on purpose, see SolveConfig::probe).
+inline SolveConfig solve_config_from_env(SolveConfig c) {
+  if (const char* v = std::getenv("AVBD_SOLVE")) c.queue = std::strcmp(v, "barrier") != 0;
+  if (const char* v = std::getenv("AVBD_SOLVE_WAVES")) c.waves = std::max(1, std::atoi(v));
+  if (const char* v = std::getenv("AVBD_SOLVE_BLOCKS")) c.blocks = std::max(0, std::atoi(v));
+  if (const char* v = std::getenv("AVBD_SOLVE_WAIT_CYCLES")) c.waitCycles = std::max(0LL, std::atoll(v));
+  if (const char* v = std::getenv("AVBD_SOLVE_WAIT_PROBE")) c.probe = std::atoi(v) != 0;
+  return c;
+}
 
 class Arena {
  public:
@@ -208,14 +238,11 @@ class Arena {
   int *activeBodies = nullptr, *activeJoints = nullptr, *activePairs = nullptr, *pairPrefix = nullptr, *pairCount = nullptr;
   Counters* ctr = nullptr;
   Counters* ctrHost = nullptr;
-  int4* activeHost = nullptr;
-  int* wactiveHost = nullptr;
+  int uploadedWorlds = 0;  // world capacity the device's active table was uploaded for
   void* scanTemp = nullptr;
   size_t scanBytes = 0;
   size_t itemCap = 0;
   int rounds = 64;
-  // the last tick (its lists stay valid until the next tick)
-  std::vector<int> lastActive;
   bool tickTriggers = false;  // a world of the tick being built has trigger bodies
   int lastPairs = 0, lastJoints = 0;
   long long steps = 0, regrowths = 0, evictions = 0, restores = 0;
@@ -241,46 +268,108 @@ class Arena {
   // not being stepped) or grow the buffers itself; otherwise the buffers grow here.
   std::function<void(int slots)> onSlotPressure;
 
-  // Host -> device uploads of world set-up go through one pinned staging buffer on the arena's
-  // stream (sources may be temporaries); flush() waits for them and recycles the buffer.
+  // Host -> device uploads go through a pinned staging ring on the arena's stream: put() copies
+  // the source into the ring (the caller's buffer is free at once, sources may be temporaries) and
+  // queues the copy with an event behind it; a region of the ring is reused only once its event
+  // has completed, so an upload waits for the device only when the ring is full.
   char* stage = nullptr;
-  size_t stageCap = 0, stageUsed = 0;
+  size_t stageCap = 0, stageHead = 0;
+  struct StageRegion {
+    size_t a, b;
+    cudaEvent_t e;
+  };
+  std::deque<StageRegion> stageLive;
+  std::vector<cudaEvent_t> stageEvents;
 
+  void stageRetire(bool wait) {
+    while (!stageLive.empty()) {
+      cudaEvent_t e = stageLive.front().e;
+      if (wait) CK(cudaEventSynchronize(e));
+      else if (cudaEventQuery(e) != cudaSuccess) break;
+      stageEvents.push_back(e);
+      stageLive.pop_front();
+    }
+  }
+  size_t stageAlloc(size_t bytes) {
+    const size_t need = (bytes + 255) & ~size_t(255);
+    if (need > stageCap / 2) {
+      CK(cudaStreamSynchronize(s));
+      stageRetire(true);
+      if (stage) cudaFreeHost(stage);
+      stage = nullptr;
+      stageCap = 0;
+      const size_t cap = std::max<size_t>(2 * need, size_t(8) << 20);
+      CK(cudaHostAlloc((void**)&stage, cap, cudaHostAllocDefault));
+      stageCap = cap;
+      stageHead = 0;
+    }
+    for (;;) {
+      stageRetire(false);
+      if (stageLive.empty()) {
+        stageHead = need;
+        return 0;
+      }
+      const size_t start = stageHead + need <= stageCap ? stageHead : 0;
+      const size_t tail = stageLive.front().a;
+      // in use: [tail, head) when head > tail; [tail, cap) and [0, head) otherwise (head == tail:
+      // the whole ring)
+      const bool ok = stageHead > tail ? (start == stageHead || start + need <= tail) : (start == stageHead && start + need <= tail);
+      if (ok) {
+        stageHead = start + need;
+        return start;
+      }
+      stageRetire(true);  // the ring is full: wait for its oldest upload
+    }
+  }
   void put(void* dst, const void* src, size_t bytes) {
     if (bytes == 0) return;
-    if (stageUsed + bytes > stageCap) {
-      flush();
-      if (bytes > stageCap) {
-        if (stage) cudaFreeHost(stage);
-        stage = nullptr;
-        stageCap = 0;
-        const size_t cap = std::max<size_t>(bytes, size_t(4) << 20);
-        CK(cudaHostAlloc((void**)&stage, cap, cudaHostAllocDefault));
-        stageCap = cap;
-      }
+    const size_t at = stageAlloc(bytes);
+    std::memcpy(stage + at, src, bytes);
+    CK(cudaMemcpyAsync(dst, stage + at, bytes, cudaMemcpyHostToDevice, s));
+    cudaEvent_t e;
+    if (!stageEvents.empty()) {
+      e = stageEvents.back();
+      stageEvents.pop_back();
+    } else {
+      CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     }
-    std::memcpy(stage + stageUsed, src, bytes);
-    CK(cudaMemcpyAsync(dst, stage + stageUsed, bytes, cudaMemcpyHostToDevice, s));
-    stageUsed += (bytes + 255) & ~size_t(255);
+    CK(cudaEventRecord(e, s));
+    stageLive.push_back(StageRegion{at, at + ((bytes + 255) & ~size_t(255)), e});
   }
+  // Wait until everything queued on the arena's stream has run.
   void flush() {
     CK(cudaStreamSynchronize(s));
-    stageUsed = 0;
+    stageRetire(true);
   }
+  // Device -> host copy after every queued tick is final (resolve): the result reflects every
+  // step queued so far.
   void get(void* dst, const void* src, size_t bytes) {
+    resolve();
+    getRaw(dst, src, bytes);
+  }
+  void getRaw(void* dst, const void* src, size_t bytes) {
     if (bytes == 0) return;
     CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
-    stageUsed = 0;
   }
 
   Arena(avbd_ctx* c, int bodies, int joints, int slots, int worldsMax) : ctx(c), s(c->stream) {
+    prepare_launches();  // per-device launch geometry, looked up before any stream capture
+    tickEvents.reserve(2 * MAX_IN_FLIGHT + 8);
+    solveCfg = solve_config_from_env(solveCfg);
+    tuner.init(solveCfg);
     allocate(std::max(bodies, 1), std::max(joints, 1), std::max(slots, 1024), std::max(worldsMax, 1));
   }
   ~Arena() {
     cudaStreamSynchronize(s);
     harvest();
     for (cudaEvent_t e : pool) cudaEventDestroy(e);
+    for (auto& r : stageLive) cudaEventDestroy(r.e);
+    for (cudaEvent_t e : stageEvents) cudaEventDestroy(e);
+    for (auto& t : tickLog)
+      if (t.done) cudaEventDestroy(t.done);
+    for (cudaEvent_t e : tickEvents) cudaEventDestroy(e);
+    clearGraphs();
     release();
   }
 
@@ -316,9 +405,6 @@ class Arena {
     CK(cudaMemset(pairN, 0, sizeof(int) * 2 * nw));
     CK(cudaMemset(wover, 0, sizeof(int) * nw));
     CK(cudaMemset(wactive, 0xff, sizeof(int) * nw));
-    CK(cudaHostAlloc((void**)&activeHost, sizeof(int4) * nw, cudaHostAllocDefault));
-    CK(cudaHostAlloc((void**)&wactiveHost, sizeof(int) * nw, cudaHostAllocDefault));
-    for (int w = 0; w < nw; w++) wactiveHost[w] = -1;
     activeBodies = dalloc<int>(N);
     activeJoints = dalloc<int>(NJ);
     pairPrefix = dalloc<int>(size_t(nw) + 1);
@@ -342,11 +428,17 @@ class Arena {
     T.pending = dalloc<unsigned char>(N);
     CK(cudaMemset(T.pending, 0, N));
     T.colorBodies = dalloc<int>(N);
+    T.colorScan = dalloc<int>(color_scan_ints(N));
     T.itemStart = dalloc<int>(N + 1);
     ctr = dalloc<Counters>(1);
     CK(cudaMemset(ctr, 0, sizeof(Counters)));
     CK(cudaHostAlloc((void**)&ctrHost, sizeof(Counters), cudaHostAllocDefault));
     std::memset(ctrHost, 0, sizeof(Counters));
+    queueScratch = dalloc<int>(solve_queue_ints(nw));
+    ctl = dalloc<TickCtl>(1);
+    CK(cudaMemset(ctl, 0, sizeof(TickCtl)));
+    CK(cudaHostAlloc((void**)&ctlHost, sizeof(TickCtl), cudaHostAllocDefault));
+    std::memset((void*)ctlHost, 0, sizeof(TickCtl));
     NC.keys = dalloc<unsigned long long>(1);
     NC.jid = dalloc<int>(1);
     ncCap = 1;
@@ -362,15 +454,14 @@ class Arena {
                     J.rB, J.stiff, J.penLin, J.penAng, J.lamLin, J.lamAng, J.C0Lin, J.C0Ang, J.restQ, J.broken, worlds,
                     which, pairN, wover, wactive, active, activeBodies, activeJoints, pairPrefix, pairCount, G.cellCount,
                     G.cellFill, G.cellBodies, G.cellKey, G.cellPos, G.pairTmp, G.bodyBucket, G.large, T.adjStart, T.adjFill, T.activeIndex, T.color, T.won,
-                    T.pending, T.colorBodies, T.itemStart, T.itemRef, ctr, NC.keys, NC.jid, scanTemp, traffic,
+                    T.pending, T.colorBodies, T.colorScan, T.itemStart, T.itemRef, ctr, NC.keys, NC.jid, scanTemp, traffic,
                     poseStage, P.pair, P.count, P.basis, P.ct, NS.sat, NS.boxList, NS.sphereList, NS.sphere2List, NS.ctr, activePairs,
                     T.adjList, G.bvh.node, G.bvh.parent, G.bvh.escape, G.bvh.minIdx, bsc.keys[0], bsc.keys[1], bsc.hist,
-                    bsc.clusters, bsc.bounds, editRec, editRanges, editTele, io};
+                    bsc.clusters, bsc.bounds, editRec, editRanges, editTele, io, ctl, queueScratch};
     for (void* p : ptrs) dfree(p);
     for (WorldRec& R : W) dfree(R.evDev);
     if (ctrHost) cudaFreeHost(ctrHost);
-    if (activeHost) cudaFreeHost(activeHost);
-    if (wactiveHost) cudaFreeHost(wactiveHost);
+    if (ctlHost) cudaFreeHost(ctlHost);
     if (stage) cudaFreeHost(stage);
   }
 
@@ -405,9 +496,10 @@ class Arena {
     if (slotCap == 0) slotA.init(cap);
     else slotA.grow(cap);
     slotCap = cap;
-    lastPairs = 0;  // the last tick's pair list was in the buffers just replaced
+    statsValid = false;  // the last tick's pair list was in the buffers just replaced
     size_t need = std::max(scan_temp_bytes(int(G.tableMask) + 2), scan_temp_bytes(bodyCap + 2));
     need = std::max(need, scan_temp_bytes(maxWorlds + 2));
+    need = std::max(need, scan_temp_bytes(int(color_scan_ints(size_t(bodyCap)))));
     if (need > scanBytes) {
       dfree(scanTemp);
       scanTemp = dalloc<char>(need);
@@ -424,6 +516,7 @@ class Arena {
     d = n;
   }
   template <class X> void rescratch(X*& d, size_t m) {
+    CK(cudaStreamSynchronize(s));  // queued work may still use the old buffer
     dfree(d);
     d = nullptr;
     d = dalloc<X>(m);
@@ -431,6 +524,7 @@ class Arena {
   void ensureScan() {
     size_t need = std::max(scan_temp_bytes(int(G.tableMask) + 2), scan_temp_bytes(bodyCap + 2));
     need = std::max(need, scan_temp_bytes(maxWorlds + 2));
+    need = std::max(need, scan_temp_bytes(int(color_scan_ints(size_t(bodyCap)))));
     if (need > scanBytes) {
       rescratch(reinterpret_cast<char*&>(scanTemp), need);
       scanBytes = need;
@@ -464,6 +558,7 @@ class Arena {
     rescratch(T.pending, N);
     CK(cudaMemset(T.pending, 0, N));
     for (int** p : {&T.activeIndex, &T.won, &T.colorBodies, &activeBodies, &G.cellBodies, &G.bodyBucket}) rescratch(*p, N);
+    rescratch(T.colorScan, color_scan_ints(N));
     rescratch(G.cellKey, N);
     rescratch(G.cellPos, N);
     rescratch(G.pairTmp, N * PAIR_TMP);
@@ -514,16 +609,8 @@ class Arena {
     rescratch(wactive, N);
     rescratch(active, N);
     rescratch(pairPrefix, N + 1);
-    int4* ah = nullptr;
-    int* wh = nullptr;
-    CK(cudaHostAlloc((void**)&ah, sizeof(int4) * N, cudaHostAllocDefault));
-    CK(cudaHostAlloc((void**)&wh, sizeof(int) * N, cudaHostAllocDefault));
-    std::memcpy(wh, wactiveHost, o * 4);
-    for (size_t w = o; w < N; w++) wh[w] = -1;
-    cudaFreeHost(activeHost);
-    cudaFreeHost(wactiveHost);
-    activeHost = ah;
-    wactiveHost = wh;
+    actUploaded.clear();  // the active table is uploaded again at the next tick
+    rescratch(queueScratch, solve_queue_ints(int(N)));
     W.resize(N);
     for (int w = nw - 1; w >= int(o); w--) freeSlots.insert(freeSlots.begin(), w);
     maxWorlds = nw;
@@ -536,7 +623,7 @@ class Arena {
   size_t scratchBytes() const { return itemCap * sizeof(int4); }
   static size_t scratchReserve(long long nb) { return size_t(nb) * 512; }
   size_t footprint(long long nb, long long nj, long long slots, long long nw) const {
-    const size_t perBody = 12 * 16 + 2 * 4 + 1 + 16 * 4 + 32 + 4 * PAIR_TMP;
+    const size_t perBody = 12 * 16 + 2 * 4 + 1 + 16 * 4 + 32 + 4 * PAIR_TMP + 1;
     const size_t perJoint = 8 + 10 * 16 + 4 + 4 + 8;
     const size_t perSlot = 2 * (8 + 4 + 3 * 16 + MAX_CONTACTS * 64) + 16 + 4 * 4 + 8;
     const size_t perWorld = sizeof(WorldDev) + 4 * 4 + 16 + 4 + MAX_LARGE * 4;
@@ -599,6 +686,7 @@ class Arena {
     t.slotStride = slotCap;
     t.bodyStride = bodyCap;
     t.triggerBits = tickTriggers ? B.sleep : nullptr;
+    t.ctl = ctl;
     return t;
   }
 
@@ -613,7 +701,8 @@ class Arena {
     if (p.iterations <= 0) throw Error(AVBD_E_INVALID, "iterations must be a positive integer");
     if (!std::isfinite(p.gravity)) throw Error(AVBD_E_INVALID, "gravity must be finite");
     for (int i = 0; i < d.n_bodies; i++) {
-      if (d.shape[i] != AVBD_SHAPE_BOX && d.shape[i] != AVBD_SHAPE_SPHERE) throw Error(AVBD_E_INVALID, "unknown body shape");
+      if (d.shape[i] != AVBD_SHAPE_BOX && d.shape[i] != AVBD_SHAPE_SPHERE && d.shape[i] != AVBD_SHAPE_CAPSULE)
+        throw Error(AVBD_E_INVALID, "unknown body shape");
       for (int k = 0; k < 3; k++) {
         if (!std::isfinite(d.position[3 * i + k])) throw Error(AVBD_E_INVALID, "position must be finite");
         if (!(d.size[3 * i + k] > 0.f)) throw Error(AVBD_E_INVALID, "size must be positive");
@@ -874,6 +963,7 @@ class Arena {
 
   // Add a world (with rebuild = false, call rebuildNoCollide after a batch of additions).
   int addWorld(const avbd_scene_desc& d, const avbd_params& p, bool rebuild = true) {
+    resolve();
     validate(d, p);
     ensureRoom(d.n_bodies, jointsOf(d), initialPairCap(d.n_bodies));  // may move W: before any reference into it
     const int w = takeSlot();
@@ -1008,6 +1098,7 @@ class Arena {
   }
 
   void removeWorld(int w) {
+    resolve();
     if (w < 0 || w >= maxWorlds || !W[w].live) throw Error(AVBD_E_INVALID, "no such world");
     CK(cudaStreamSynchronize(s));
     WorldRec& R = W[w];
@@ -1035,6 +1126,7 @@ class Arena {
 
   // Move a resident world's state to host memory and free its ranges.
   void evict(int w) {
+    resolve();
     WorldRec& R = W[w];
     if (!R.live || !R.resident) throw Error(AVBD_E_INVALID, "world is not resident");
     CK(cudaStreamSynchronize(s));
@@ -1090,6 +1182,7 @@ class Arena {
     return std::max(initialPairCap(W[w].nBodies), np + np / 4 + 64);
   }
   void restore(int w) {
+    resolve();
     if (w < 0 || w >= maxWorlds || !W[w].live || W[w].resident || !W[w].snap) throw Error(AVBD_E_INVALID, "world is not evicted");
     ensureRoom(W[w].nBodies, W[w].nJoints, restoreSlots(w), false);  // may move W: before any reference into it
     WorldRec& R = W[w];
@@ -1183,6 +1276,7 @@ class Arena {
   char* io = nullptr;
   size_t ioCap = 0;
   char* ioBuffer(size_t bytes) {
+    resolve();
     if (bytes > ioCap) {
       CK(cudaStreamSynchronize(s));  // earlier calls may still read the old buffer
       ioCap = bytes + bytes / 2 + 4096;
@@ -1199,7 +1293,9 @@ class Arena {
   size_t editCap = 0;
 
   // Validate n 12-word records (src/native/runtime.js:59-167 stages the same checks) and queue
-  // them for world w's next step.
+  // them for world w's next step. Nothing reaches the device here: the records (and the wake that
+  // queued commands cause, src/native/cpu/world.js:132-133) apply at the world's next step, or at
+  // a read or flushEdits, before anything else touches its state.
   void queueEdits(int w, const uint32_t* rec, int n) {
     if (w < 0 || w >= maxWorlds || !W[w].live) throw Error(AVBD_E_INVALID, "no such world");
     if (n < 0) throw Error(AVBD_E_INVALID, "negative record count");
@@ -1216,29 +1312,24 @@ class Arena {
         throw Error(AVBD_E_INVALID, "rotation must be nonzero");
     }
     W[w].edits.insert(W[w].edits.end(), rec, rec + 12 * size_t(n));
-    if (n > 0) wakeWorld(w);  // queued commands wake the world (src/native/cpu/world.js:132-133)
+    if (n > 0) W[w].wakePending = true;
   }
 
-  // Apply world w's queued records (the reference applies them at its next step, or at
-  // flushEdits): grouped by body in record order, one thread per body; teleported bodies lose
-  // the warm start of their pairs.
-  void flushEdits(int w) {
-    WorldRec& R = W[w];
-    if (R.edits.empty()) return;
-    if (!R.resident) throw Error(AVBD_E_STATE, "world is evicted");
-    const int n = int(R.edits.size() / 12);
+  // Upload records (word 0: body index relative to bodyOff) grouped by body in record order and
+  // apply them, one thread per body (k_apply_edits).
+  void uploadCommands(const std::vector<uint32_t>& recs, int bodyOff) {
+    const int n = int(recs.size() / 12);
+    if (n == 0) return;
     std::vector<int> order(n);
     for (int k = 0; k < n; k++) order[k] = k;
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return R.edits[12 * size_t(a)] < R.edits[12 * size_t(b)]; });
-    std::vector<uint32_t> sorted(R.edits.size());
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return recs[12 * size_t(a)] < recs[12 * size_t(b)]; });
+    std::vector<uint32_t> sorted(recs.size());
     std::vector<int2> ranges;
-    std::vector<uint32_t> tele;
     for (int k = 0; k < n; k++) {
-      const uint32_t* u = R.edits.data() + 12 * size_t(order[k]);
+      const uint32_t* u = recs.data() + 12 * size_t(order[k]);
       std::memcpy(sorted.data() + 12 * size_t(k), u, 48);
       if (ranges.empty() || sorted[12 * size_t(ranges.back().x)] != u[0]) ranges.push_back(make_int2(k, 0));
       ranges.back().y++;
-      if (u[1] == 4u && (tele.empty() || tele.back() != u[0])) tele.push_back(u[0]);
     }
     if (size_t(n) > editCap) {
       editCap = size_t(n) + size_t(n) / 2 + 64;
@@ -1248,14 +1339,51 @@ class Arena {
     }
     put(editRec, sorted.data(), sorted.size() * 4);
     put(editRanges, ranges.data(), ranges.size() * sizeof(int2));
-    launch_apply_edits(B, editRec, editRanges, int(ranges.size()), R.dev.bodyOff, s);
-    if (!tele.empty()) {
-      put(editTele, tele.data(), tele.size() * 4);
-      const int np = prevPairs(w);
-      launch_drop_contacts(P, size_t(R.which) * slotCap + R.dev.pairOff, np, editTele, int(tele.size()), R.dev.bodyOff, s);
+    launch_apply_edits(B, editRec, editRanges, int(ranges.size()), bodyOff, ctl, s);
+  }
+  // Teleported bodies of world w (records with world-local indices) lose the warm start of their
+  // pairs in the world's last pair region.
+  void dropTeleported(int w, const std::vector<uint32_t>& recs) {
+    std::vector<uint32_t> tele;
+    for (size_t k = 0; k < recs.size() / 12; k++)
+      if (recs[12 * k + 1] == 4u) tele.push_back(recs[12 * k]);
+    if (tele.empty()) return;
+    std::sort(tele.begin(), tele.end());
+    tele.erase(std::unique(tele.begin(), tele.end()), tele.end());
+    const WorldRec& R = W[w];
+    if (tele.size() > editCap) {
+      editCap = tele.size() + tele.size() / 2 + 64;
+      rescratch(editRec, 12 * editCap);
+      rescratch(editRanges, editCap);
+      rescratch(editTele, editCap);
     }
-    flush();
-    R.edits.clear();
+    put(editTele, tele.data(), tele.size() * 4);
+    launch_drop_contacts(P, size_t(R.which) * slotCap + R.dev.pairOff, pairN + size_t(R.which) * maxWorlds + w, R.dev.pairCap,
+                         editTele, int(tele.size()), R.dev.bodyOff, ctl, s);
+  }
+
+  // Every queued tick final, then world w's queued commands applied: the start of every call
+  // that reads or changes world w's state outside a step.
+  void touch(int w) {
+    resolve();
+    flushEdits(w);
+  }
+
+  // Apply world w's queued records now (the reference applies them at its next step, or at
+  // flushEdits and before reads, src/native/cpu/world.js:566-575): grouped by body in record order,
+  // one thread per body; teleported bodies lose the warm start of their pairs.
+  void flushEdits(int w) {
+    WorldRec& R = W[w];
+    if (R.edits.empty() && !R.wakePending) return;
+    if (!R.resident) throw Error(AVBD_E_STATE, "world is evicted");
+    resolve();
+    if (R.wakePending && (R.dev.flags & FLAG_SLEEP) && R.nBodies) launch_sleep_wake(B, R.dev.bodyOff, R.nBodies, ctl, s);
+    R.wakePending = false;
+    std::vector<uint32_t> recs;
+    recs.swap(R.edits);
+    uploadCommands(recs, R.dev.bodyOff);
+    dropTeleported(w, recs);
+    CK(cudaGetLastError());
   }
 
   // ------------------------------------------------------------------ profiling
@@ -1285,6 +1413,7 @@ class Arena {
     recs.clear();
   }
   void profile(bool on) {
+    resolve();
     CK(cudaStreamSynchronize(s));
     harvest();
     prof = on;
@@ -1295,6 +1424,7 @@ class Arena {
     if (!traffic) traffic = dalloc<unsigned long long>(3);
   }
   void profileRead(avbd_profile* o) {
+    resolve();
     CK(cudaStreamSynchronize(s));
     harvest();
     std::memset(o, 0, sizeof(*o));
@@ -1309,6 +1439,18 @@ class Arena {
     o->bytes_primal = profBytes[0];
     o->bytes_dual = profBytes[1];
     o->bytes_collide = profBytes[2];
+    o->graph_captures = graphCaptures;
+    o->graph_replays = graphReplays;
+    o->graphs_on = graphsOn ? 1 : 0;
+    o->ticks_held = int32_t(ticksHeld);
+    std::vector<cudaEvent_t> freed;
+    tuner.harvest(true, freed);
+    for (cudaEvent_t ev : freed) pool.push_back(ev);
+    o->tuned = lastTuned ? 1 : 0;
+    o->solve_queue = solveCfg.queue;
+    o->solve_waves = solveCfg.waves;
+    o->solve_blocks = solveCfg.blocks;
+    o->radix_bits = radixBits;
   }
 
   // ------------------------------------------------------------------ ticks
@@ -1339,7 +1481,8 @@ class Arena {
     WorldRec& R = W[w];
     if (!(R.dev.flags & FLAG_SLEEP) || R.nBodies == 0) return;
     if (R.resident) {
-      launch_sleep_wake(B, R.dev.bodyOff, R.nBodies, s);
+      resolve();
+      launch_sleep_wake(B, R.dev.bodyOff, R.nBodies, ctl, s);
       CK(cudaGetLastError());
     } else if (R.snap) {
       for (int& b : R.snap->sleep) b &= ~SLEEP_ASLEEP;
@@ -1350,6 +1493,7 @@ class Arena {
   // Sleeping on/off for world w (enableSleeping / disableSleeping of src/native/cpu/world.js:
   // 869-878); turning it off or changing the thresholds wakes the world first.
   void setSleeping(int w, bool on, float speed, float delay) {
+    resolve();
     if (w < 0 || w >= maxWorlds || !W[w].live) throw Error(AVBD_E_INVALID, "no such world");
     if (on && (!(speed > 0.f) || !(delay > 0.f) || !std::isfinite(speed) || !std::isfinite(delay)))
       throw Error(AVBD_E_INVALID, "Sleep thresholds must be positive and finite");
@@ -1366,6 +1510,7 @@ class Arena {
   // allowSleep of one body (setSleepEnabled, src/native/cpu/world.js:859-867): enabling it turns
   // sleeping on with the default thresholds if it was off; the world wakes.
   void setSleepAllowed(int w, int body, bool allowed) {
+    resolve();
     if (w < 0 || w >= maxWorlds || !W[w].live) throw Error(AVBD_E_INVALID, "no such world");
     WorldRec& R = W[w];
     if (body < 0 || body >= R.nBodies) throw Error(AVBD_E_INVALID, "body index out of range");
@@ -1386,6 +1531,7 @@ class Arena {
   int sleepState(int w, int32_t* asleep, float* time) {
     if (w < 0 || w >= maxWorlds || !W[w].live) throw Error(AVBD_E_INVALID, "no such world");
     WorldRec& R = W[w];
+    if (R.resident) touch(w);  // queued commands (and the wake they cause) apply before a read
     const size_t n = size_t(R.nBodies);
     std::vector<int> bits(n);
     std::vector<float> t(n);
@@ -1462,6 +1608,7 @@ class Arena {
   // maxEvents per read and watches every body unless `select`; with `select`, exactly the given
   // bodies are watched. A newly watched body begins its current contacts at the next step.
   void watchContacts(int w, const uint32_t* idx, int n, int maxEvents, bool select) {
+    resolve();
     if (w < 0 || w >= maxWorlds || !W[w].live) throw Error(AVBD_E_INVALID, "no such world");
     if (maxEvents < 1) throw Error(AVBD_E_INVALID, "Contact capacities must be positive integers");
     WorldRec& R = W[w];
@@ -1499,6 +1646,7 @@ class Arena {
   // resetContactHistory (src/vendor/three-avbd-lib/contacts.ts resetBodies): new lifetimes for
   // the given bodies (ascending, unique): their contacts begin afresh, none of the old ones end.
   void resetContactHistory(int w, const uint32_t* idx, int n) {
+    resolve();
     if (w < 0 || w >= maxWorlds || !W[w].live) throw Error(AVBD_E_INVALID, "no such world");
     WorldRec& R = W[w];
     long long prev = -1;
@@ -1571,7 +1719,7 @@ class Arena {
   // (w: torque arm), C0 lin, C0 ang, rA (w: spring rest length), rB.
   void readJoints(int w, float* out) {
     if (w < 0 || w >= maxWorlds || !W[w].live) throw Error(AVBD_E_INVALID, "no such world");
-    flushEdits(w);
+    touch(w);
     const WorldRec& R = resident(w);
     const size_t nj = size_t(R.nJoints), off = size_t(R.dev.jointOff);
     if (!nj) return;
@@ -1667,7 +1815,7 @@ class Arena {
   // torque bound.
   void setMotor(int w, int slot, int mask, float speed, float maxTorque) {
     if (w < 0 || w >= maxWorlds || !W[w].live) throw Error(AVBD_E_INVALID, "no such world");
-    flushEdits(w);
+    touch(w);
     const WorldRec& R = resident(w);
     if (slot < 0 || slot >= R.nJoints) throw Error(AVBD_E_INVALID, "Motor needs an active motor slot");
     const size_t j = size_t(R.dev.jointOff) + size_t(slot);
@@ -1690,7 +1838,7 @@ class Arena {
   void setSensor(int w, const uint32_t* idx, int n, bool enabled) {
     if (w < 0 || w >= maxWorlds || !W[w].live) throw Error(AVBD_E_INVALID, "no such world");
     if (n < 0) throw Error(AVBD_E_INVALID, "negative count");
-    flushEdits(w);
+    touch(w);
     WorldRec& R = W[w];
     resident(w);
     for (int k = 0; k < n; k++)
@@ -1716,7 +1864,7 @@ class Arena {
       const float v = k ? breakForce : breakStrain;
       if ((mask >> k & 1) && !(v > 0.f)) throw Error(AVBD_E_INVALID, k ? "breakForce must be positive or Infinity" : "breakStrain must be positive or Infinity");
     }
-    flushEdits(w);
+    touch(w);
     const WorldRec& R = resident(w);
     if (slot < 0 || slot >= R.nJoints) throw Error(AVBD_E_INVALID, "Spring material requires an active spring slot");
     const size_t j = size_t(R.dev.jointOff) + size_t(slot);
@@ -1738,7 +1886,7 @@ class Arena {
     if (w < 0 || w >= maxWorlds || !W[w].live) throw Error(AVBD_E_INVALID, "no such world");
     if (!(std::isfinite(point[0]) && std::isfinite(point[1]) && std::isfinite(point[2])))
       throw Error(AVBD_E_INVALID, "A world joint and finite xyz anchor are required");
-    flushEdits(w);
+    touch(w);
     const WorldRec& R = resident(w);
     if (slot < 0 || slot >= R.nJoints) throw Error(AVBD_E_INVALID, "A world joint and finite xyz anchor are required");
     const size_t j = size_t(R.dev.jointOff) + size_t(slot);
@@ -1773,7 +1921,7 @@ class Arena {
       if (kind != (spring[k] ? KIND_SPRING : KIND_JOINT) || broken[slots[k]])
         throw Error(AVBD_E_INVALID, "A live spring or joint slot is required");
     }
-    flushEdits(w);
+    touch(w);
     for (int k = 0; k < n; k++) launch_joint_capture(B, J, int(off) + slots[k], spring[k] ? 1 : 0, s);
     CK(cudaGetLastError());
     flush();
@@ -1787,7 +1935,7 @@ class Arena {
   void releaseJoints(int w, const int32_t* slots, int n) {
     if (w < 0 || w >= maxWorlds || !W[w].live) throw Error(AVBD_E_INVALID, "no such world");
     if (n < 0) throw Error(AVBD_E_INVALID, "negative count");
-    flushEdits(w);
+    touch(w);
     const WorldRec& R = resident(w);
     for (int k = 0; k < n; k++)
       if (slots[k] < 0 || slots[k] >= R.nJoints) throw Error(AVBD_E_INVALID, "A live constraint slot is required");
@@ -1830,7 +1978,7 @@ class Arena {
       qs[k].d = make_float4(float(q[4] / len), float(q[5] / len), float(q[6] / len), q[7]);
     }
     if (n == 0) return;
-    flushEdits(w);
+    touch(w);
     const WorldRec& R = resident(w);
     CastFilter f{};
     f.collidesWith = filt.collides_with;
@@ -1867,174 +2015,498 @@ class Arena {
     }
   }
 
-  void ensureItems() {
-    const size_t need = size_t(std::max(ctrHost->itemsTotal, 1));
-    if (need > itemCap) {
-      CK(cudaStreamSynchronize(s));
-      const size_t cap = need + need / 4 + 1024;
-      dfree(T.itemRef);
-      T.itemRef = nullptr;
-      T.itemRef = dalloc<int4>(cap);
-      itemCap = cap;
+  // ------------------------------------------------------------------ tick protocol
+  // A tick is queued without waiting for the device (the reference's step never waits either,
+  // src/native/solver3D.js:350-359). Its capacities (pair regions, work items) are chosen on the
+  // host before it is queued; its gate holds it on the device when they do not suffice (TickCtl).
+  // Every queued tick stays in tickLog, with the host state its worlds had before it, until it is
+  // known to have completed: resolve() waits for the stream, and when a tick was held it grows the
+  // capacities and queues the held ticks again from that state, so the results are those of a
+  // run with enough room from the start. Reads and every other call that touches world state
+  // resolve first.
+  TickCtl* ctl = nullptr;      // device
+  TickCtl* ctlHost = nullptr;  // pinned mirror, written by the last copy of every tick
+  struct TickPre {  // a stepped world's host state before the tick, and the commands queued for it
+    int w = 0, which = 0, sinceBuild = 0;
+    long long steps = 0;
+    bool built = false, wake = false;
+    std::vector<uint32_t> edits;
+  };
+  struct TickLog {
+    std::vector<int> act;
+    std::vector<TickPre> pre;
+    cudaEvent_t done = nullptr;
+  };
+  std::deque<TickLog> tickLog;  // queued ticks not yet confirmed, in queue order
+  long long logBase = 0;        // TickCtl::ticksDone before the first entry of tickLog
+  static constexpr size_t MAX_IN_FLIGHT = 24;
+  std::vector<cudaEvent_t> tickEvents;
+  bool statsValid = false;  // the last tick's active-pair list still indexes the pair buffers
+  SolveConfig solveCfg;          // the solve loop's schedule (solve.cu launch_solve)
+  int radixBits = 8;             // digit width of the tree builds' Morton sort
+  Tuner tuner;                   // run-time choice of both (tuner.hpp)
+  bool lastTuned = false;        // the last tick's class had its choices
+  int* queueScratch = nullptr;   // the tile queue's per-world counters (solve_queue_ints)
+
+  bool hostHeld() const { return *(volatile const int*)&ctlHost->held != 0; }
+  cudaEvent_t tickEvent() {
+    if (!tickEvents.empty()) {
+      cudaEvent_t e = tickEvents.back();
+      tickEvents.pop_back();
+      return e;
+    }
+    cudaEvent_t e;
+    CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    return e;
+  }
+  void dropLogFront() {
+    if (tickLog.front().done) tickEvents.push_back(tickLog.front().done);
+    tickLog.pop_front();
+    logBase++;
+  }
+
+  // Work items of a tick: grown ahead when the largest need seen comes close to the capacity
+  // (a tick that still overflows is held and re-run).
+  void growItems(size_t cap) {
+    if (cap <= itemCap) return;
+    CK(cudaStreamSynchronize(s));
+    dfree(T.itemRef);
+    T.itemRef = nullptr;
+    T.itemRef = dalloc<int4>(cap);
+    itemCap = cap;
+  }
+  void ensureItems(int nb) {
+    const size_t seen = size_t(std::max(ctlHost->itemsNeed, 0));
+    if (itemCap < size_t(16) * size_t(nb) + 1024) growItems(size_t(16) * size_t(nb) + 1024);
+    if (seen > itemCap - itemCap / 5) growItems(seen + seen / 2 + 1024);
+  }
+
+  // Confirmed ticks (completed, no hold seen) leave the log; with MAX_IN_FLIGHT ticks queued the
+  // host waits for the oldest (the reference's queue is bounded by its device the same way).
+  void trimLog() {
+    while (!tickLog.empty()) {
+      cudaEvent_t d = tickLog.front().done;
+      if (cudaEventQuery(d) != cudaSuccess) {
+        if (tickLog.size() < MAX_IN_FLIGHT) break;
+        CK(cudaEventSynchronize(d));
+      }
+      if (hostHeld()) {  // the mirror is at least as new as this tick's last copy
+        resolve();
+        return;
+      }
+      dropLogFront();
     }
   }
 
-  // One step of the given resident worlds.
-  void stepWorlds(std::vector<int> act) {
-    std::sort(act.begin(), act.end(), [&](int a, int b) { return W[a].dev.bodyOff < W[b].dev.bodyOff; });
-    act.erase(std::unique(act.begin(), act.end()), act.end());
-    for (int w : act)
-      if (w < 0 || w >= maxWorlds || !W[w].live || !W[w].resident) throw Error(AVBD_E_INVALID, "stepping a world that is not resident");
-    for (int w : act) flushEdits(w);  // queued body commands apply before the step
-    for (int w : lastActive) wactiveHost[w] = -1;
-    lastActive.clear();
-    int nb = 0, nj = 0, maxIter = 0;
-    tickTriggers = false;
-    for (size_t a = 0; a < act.size(); a++) {
-      const WorldRec& R = W[act[a]];
-      tickTriggers |= R.triggers;
-      activeHost[a] = make_int4(act[a], nb, nj, 0);
-      wactiveHost[act[a]] = int(a);
-      nb += R.nBodies;
-      nj += R.nJoints;
-      maxIter = std::max(maxIter, R.dev.iterations);
-    }
-    const int na = int(act.size());
-    if (na) CK(cudaMemcpyAsync(active, activeHost, sizeof(int4) * na, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(wactive, wactiveHost, sizeof(int) * maxWorlds, cudaMemcpyHostToDevice, s));
-    lastActive = act;
-    // broadphase trees: rebuild every bvhRebuild steps, refit in between (before the pair passes;
-    // an overflow re-run below reuses them, the poses being unchanged)
-    {
-      cudaEvent_t b0 = nullptr;
-      for (int w : act) {
-        WorldRec& R = W[w];
-        if (!R.bvh || R.nBodies == 0) continue;
-        if (prof && !b0) b0 = mark();
-        if (!R.built || R.sinceBuild >= R.bvhRebuild) {
-          ensureBvhScratch(R);
-          launch_bvh_build(B, R.dev.bodyOff, R.nBodies, G.bvh, R.bvhOff, R.tree, bsc, scanTemp, s);
-          R.built = true;
-          R.sinceBuild = 0;
-        } else {
-          launch_bvh_refit(B, R.dev.bodyOff, R.nBodies, G.bvh, R.bvhOff, R.tree, s);
-        }
-        R.sinceBuild++;
-      }
-      if (b0) span(P_COLLIDE, b0, mark());
-    }
-    long long budget = 0;
-    for (int attempt = 0;; attempt++) {
-      budget = 0;
-      for (int w : act) budget += W[w].dev.pairCap;
-      const int pairBudget = int(std::min<long long>(budget, slotCap));
-      Tick t = tick(na, nb, nj);
-      cudaEvent_t e0 = prof ? mark() : nullptr;
-      launch_tick_begin(t, T, worlds, s);
-      launch_grid_build(B, worlds, t, G, scanTemp, s);
-      launch_pairs(B, worlds, t, G, NC, J.broken, pairCount, P, ctr, scanTemp, s);
-      launch_narrowphase(B, worlds, t, P, NS, ctr, pairBudget, s);
-      // every span owns its two events (the pool recycles each event exactly once)
-      cudaEvent_t e1 = prof ? mark() : nullptr;
-      cudaEvent_t e1b = prof ? mark() : nullptr;
-      launch_spring_tear(B, J, t, s);
-      launch_adjacency(B, J, P, t, ctr, T, pairBudget, scanTemp, s);
-      launch_coloring(B, worlds, J, P, t, T, rounds, ctr, s);
-      launch_items_count(P, t, T, ctr, scanTemp, s);
-      if (prof) {
-        cudaEvent_t e2 = mark();
-        span(P_COLLIDE, e0, e1);
-        span(P_TOPO, e1b, e2);
-      }
-      CK(cudaMemcpyAsync(ctrHost, ctr, sizeof(Counters), cudaMemcpyDeviceToHost, s));
+  // Wait for every queued tick without growing anything: false when a tick was held (making it
+  // final needs growth, which allocates).
+  bool settle() {
+    CK(cudaStreamSynchronize(s));
+    if (hostHeld()) return false;
+    while (!tickLog.empty()) dropLogFront();
+    logBase = ctlHost->ticksDone;
+    return true;
+  }
+
+  // Make every queued tick final: wait for the stream; if a tick was held, grow what overflowed
+  // and queue the held ticks again (bounded: a capacity that fails to converge is an error).
+  void resolve() {
+    if (tickLog.empty() && !hostHeld()) return;
+    for (int round = 0;; round++) {
       CK(cudaStreamSynchronize(s));
-      CK(cudaGetLastError());
-      if (prof) harvest();
-      if (ctrHost->overflowWorlds == 0) break;
-      if (attempt > 8) throw Error(AVBD_E_CAPACITY, "pair regions did not converge");
+      stageRetire(true);
+      TickCtl c;
+      std::memcpy(&c, (const void*)ctlHost, sizeof(c));
+      if (c.waitFail) {
+        // a bounded wait of the tile queue ran out: the tick's solve is incomplete; the flag stays
+        // set (ticks keep stopping at it) and every later call reports it
+        while (!tickLog.empty()) dropLogFront();
+        logBase = c.ticksDone;
+        throw Error(AVBD_E_STATE, "the persistent solve's wait limit ran out (TickCtl::waitFail); the world state is not valid");
+      }
+      if (!c.held) {
+        while (!tickLog.empty()) dropLogFront();
+        logBase = c.ticksDone;
+        break;
+      }
+      if (round >= 8) throw Error(AVBD_E_CAPACITY, "pair regions or work items did not converge");
+      // timings of held ticks (whose solve did nothing) must not reach the autotuner
+      for (auto& pt : tuner.pending)
+        for (cudaEvent_t ev : {pt.a, pt.b, pt.c, pt.d})
+          if (ev) pool.push_back(ev);
+      tuner.pending.clear();
+      const long long good = c.ticksDone - logBase;
+      ticksHeld += (long long)tickLog.size() - good;
+      if (good < 0 || good >= (long long)tickLog.size()) throw Error(AVBD_E_STATE, "tick protocol out of step");
+      for (long long k = 0; k < good; k++) dropLogFront();
+      std::vector<TickLog> again;
+      while (!tickLog.empty()) {
+        again.push_back(std::move(tickLog.front()));
+        tickLog.pop_front();
+      }
+      // the held ticks' worlds go back to their state before the first held tick that stepped them
+      for (auto it = again.rbegin(); it != again.rend(); ++it)
+        for (const TickPre& pr : it->pre) {
+          WorldRec& R = W[pr.w];
+          R.which = pr.which;
+          R.steps = pr.steps;
+          R.sinceBuild = pr.sinceBuild;
+          R.built = pr.built;
+        }
+      // the first held tick's commands ran before its gate held it: they are not applied again
+      for (TickPre& pr : again.front().pre) {
+        pr.edits.clear();
+        pr.wake = false;
+      }
+      // clear the hold before growing (growth may read the device, which resolves: nothing is
+      // queued now)
+      TickCtl reset = c;
+      reset.held = 0;
+      reset.itemsNeed = 0;
+      CK(cudaMemcpyAsync(ctl, &reset, sizeof(TickCtl), cudaMemcpyHostToDevice, s));
+      CK(cudaStreamSynchronize(s));
+      std::memcpy((void*)ctlHost, &reset, sizeof(reset));
+      logBase = c.ticksDone;
+      for (const TickLog& e : again)
+        for (const TickPre& pr : e.pre) W[pr.w].pinned = true;
       std::vector<int> over(maxWorlds);
-      get(over.data(), wover, sizeof(int) * maxWorlds);
-      for (int w : act)
-        if (over[w] > 0) {
+      getRaw(over.data(), wover, sizeof(int) * maxWorlds);
+      for (int w = 0; w < maxWorlds; w++)
+        if (over[w] > 0 && W[w].live && W[w].resident) {
           growRegion(w, over[w]);
           const int zero = 0;
           put(wover + w, &zero, 4);
         }
+      if (size_t(c.itemsNeed) > itemCap) growItems(size_t(c.itemsNeed) + size_t(c.itemsNeed) / 4 + 1024);
+      for (const TickLog& e : again)
+        for (const TickPre& pr : e.pre) W[pr.w].pinned = false;
+      regrowths++;
+      for (TickLog& e : again) {
+        if (e.done) tickEvents.push_back(e.done);
+        e.done = nullptr;
+        tickLog.push_back(std::move(e));
+        queueTick(tickLog.back());
+      }
     }
-    const int pairBudget = int(std::min<long long>(budget, slotCap));
-    Tick t = tick(na, nb, nj);
-    ensureItems();
+  }
+
+  // CUDA graphs of tick launch sequences. A sequence depends only on host values fixed when it is
+  // queued (the active table, sizes, capacities, flags, tree rebuilds) and on the device buffers;
+  // a graph is replayed while all of those are unchanged (any allocation drops every graph).
+  struct TickPlan {
+    Tick t{};
+    int na = 0, nb = 0, nj = 0, maxIter = 0, pairBudget = 0;
+    long long itemCap = 0;
+    bool bounce = false, sleeping = false, events = false, sleepy = false;
+    int radixBits = 8;
+    cudaEvent_t tune[4] = {nullptr, nullptr, nullptr, nullptr};  // autotuner timing: solve (0, 1), tree builds (2, 3)
+    std::vector<std::pair<int, int>> trees;  // (world, rebuild)
+  };
+  struct GraphEntry {
+    std::vector<long long> key;
+    cudaGraphExec_t exec = nullptr;
+    long long launches = 0;
+    unsigned long long use = 0;
+  };
+  std::vector<GraphEntry> graphs;
+  bool graphsOn = true;
+  std::string graphsOff;  // why graphs were turned off
+  long long graphGen = -1;
+  unsigned long long graphClock = 0;
+  long long graphReplays = 0, graphCaptures = 0, ticksHeld = 0;
+  long long actVersion = 0;
+  std::vector<int> actUploaded;  // the active worlds whose table the device holds
+
+  void clearGraphs() {
+    for (GraphEntry& g : graphs)
+      if (g.exec) cudaGraphExecDestroy(g.exec);
+    graphs.clear();
+  }
+  std::vector<long long> planKey(const TickPlan& p) const {
+    std::vector<long long> k = {actVersion, p.na, p.nb, p.nj, p.maxIter, p.pairBudget, p.itemCap,
+                                (p.bounce ? 1 : 0) | (p.sleeping ? 2 : 0) | (p.events ? 4 : 0) | (p.sleepy ? 8 : 0) |
+                                    (p.t.triggerBits ? 16 : 0),
+                                rounds, slotCap, bodyCap, maxWorlds, solveCfg.queue, solveCfg.blocks, solveCfg.waves,
+                                solveCfg.waitCycles, solveCfg.probe, p.radixBits};
+    for (auto& tr : p.trees) {
+      k.push_back(tr.first);
+      k.push_back(tr.second);
+    }
+    return k;
+  }
+
+  // The launch sequence of one tick (direct, or recorded into a graph by stream capture).
+  void launchTick(const TickPlan& p) {
+    const Tick& t = p.t;
+    cudaEvent_t b0 = (prof && !p.trees.empty()) ? mark() : nullptr;
+    if (p.tune[2]) CK(cudaEventRecord(p.tune[2], s));
+    for (auto& tr : p.trees) {
+      WorldRec& R = W[tr.first];
+      if (tr.second) launch_bvh_build(B, R.dev.bodyOff, R.nBodies, G.bvh, R.bvhOff, R.tree, bsc, scanTemp, p.radixBits, s);
+      else launch_bvh_refit(B, R.dev.bodyOff, R.nBodies, G.bvh, R.bvhOff, R.tree, s);
+    }
+    if (p.tune[3]) CK(cudaEventRecord(p.tune[3], s));
+    if (b0) span(P_COLLIDE, b0, mark());
+    cudaEvent_t e0 = prof ? mark() : nullptr;
+    launch_tick_begin(t, T, worlds, s);
+    launch_grid_build(B, worlds, t, G, scanTemp, s);
+    launch_pairs(B, worlds, t, G, NC, J.broken, pairCount, P, ctr, scanTemp, s);
+    launch_narrowphase(B, worlds, t, P, NS, ctr, p.pairBudget, s);
+    // every span owns its two events (the pool recycles each event exactly once)
+    cudaEvent_t e1 = prof ? mark() : nullptr;
+    cudaEvent_t e1b = prof ? mark() : nullptr;
+    launch_spring_tear(B, J, t, s);
+    launch_adjacency(B, J, P, t, ctr, T, p.pairBudget, scanTemp, s);
+    launch_coloring(B, worlds, J, P, t, T, rounds, ctr, scanTemp, s);
+    launch_items_count(P, t, T, ctr, scanTemp, s);
+    launch_tick_gate(t, ctr, p.itemCap, s);
+    if (prof) {
+      cudaEvent_t e2 = mark();
+      span(P_COLLIDE, e0, e1);
+      span(P_TOPO, e1b, e2);
+    }
     launch_items_fill(B, worlds, P, t, T, ctr, s);
     cudaEvent_t o0 = prof ? mark() : nullptr;
     launch_joint_retire(J, t, s);
     launch_joint_warmstart(B, worlds, J, t, s);
     launch_body_warmstart(B, worlds, t, s);
     if (prof) span(P_OTHER, o0, mark());
-    const int ncolors = ctrHost->ncolors;
-    bool sleepy = false;
-    for (int w : act) sleepy |= (W[w].dev.flags & FLAG_SLEEP) != 0;
-    if (nb <= AVBD_COOP_SOLVE_MAX) {
-      // a small tick: the whole loop in one cooperative launch (same order of updates)
-      cudaEvent_t a = prof ? mark() : nullptr;
-      CK(launch_solve_coop(B, worlds, J, P, t, T, ctr, maxIter, nb, sleepy, s));
-      if (prof) {
-        span(P_PRIMAL, a, mark());
-        profPrimalLaunches += 1;
-      }
-    } else {
-      for (int it = 0; it < maxIter; it++) {
-        for (int c = 0; c < ncolors; c++) {
-          const int cnt = ctrHost->colorCount[c];
-          if (!cnt) continue;
-          cudaEvent_t a = prof ? mark() : nullptr;
-          launch_primal(B, worlds, J, P, t, T, ctr, c, it, cnt, ctrHost->colorItems[c], sleepy, s);
-          if (prof) {
-            span(P_PRIMAL, a, mark());
-            profPrimalLaunches += 1;
-          }
-        }
-        if (nj) {
-          cudaEvent_t d = prof ? mark() : nullptr;
-          launch_dual_joints(B, worlds, J, t, it, s);
-          if (prof) span(P_DUAL, d, mark());
-        }
-      }
-    }
-    bool bounce = false;
-    for (int w : act) bounce |= (W[w].dev.flags & FLAG_RESTITUTION) != 0;
-    if (bounce) ensureBounce();
-    cudaEvent_t v0 = prof ? mark() : nullptr;
-    if (bounce) launch_bounce_capture(B, t, BB, s);
-    launch_velocities(B, worlds, t, s);
-    if (bounce) launch_bounce(B, P, t, T, ctr, pairBudget, BB, worlds, s);
-    bool sleeping = false;
-    for (int w : act) sleeping |= (W[w].dev.flags & FLAG_SLEEP) != 0;
-    if (sleeping) {
-      ensureSleep();
-      launch_sleep(B, worlds, J, P, NC, t, ctr, pairBudget, SB, maxWorlds, s);
-    }
-    bool events = false;
-    for (int w : act) events |= (W[w].dev.flags & FLAG_EVENTS) != 0;
-    if (events) launch_events(B, worlds, P, t, ctr, pairBudget, EV, s);
-    if (prof) span(P_OTHER, v0, mark());
+    cudaEvent_t a = prof ? mark() : nullptr;
+    if (p.tune[0]) CK(cudaEventRecord(p.tune[0], s));
+    CK(launch_solve(B, worlds, J, P, t, T, ctr, p.maxIter, p.nb, p.sleepy, solveCfg, queueScratch, s));
+    if (p.tune[1]) CK(cudaEventRecord(p.tune[1], s));
     if (prof) {
+      span(P_PRIMAL, a, mark());
+      profPrimalLaunches += 1;
+    }
+    cudaEvent_t v0 = prof ? mark() : nullptr;
+    if (p.bounce) launch_bounce_capture(B, t, BB, s);
+    launch_velocities(B, worlds, t, s);
+    if (p.bounce) launch_bounce(B, P, t, T, ctr, p.pairBudget, BB, worlds, s);
+    if (p.sleeping) launch_sleep(B, worlds, J, P, NC, t, ctr, p.pairBudget, SB, maxWorlds, s);
+    if (p.events) launch_events(B, worlds, P, t, ctr, p.pairBudget, EV, s);
+    if (prof) span(P_OTHER, v0, mark());
+    launch_tick_end(t, s);
+    CK(cudaMemcpyAsync(ctlHost, ctl, sizeof(TickCtl), cudaMemcpyDeviceToHost, s));
+  }
+
+  void runTick(const TickPlan& p) {
+    if (prof || !graphsOn || p.tune[0] || p.tune[2]) {
+      launchTick(p);
+      return;
+    }
+    if (graphGen != alloc_generation()) {
+      clearGraphs();
+      graphGen = alloc_generation();
+    }
+    const std::vector<long long> key = planKey(p);
+    GraphEntry* hit = nullptr;
+    for (GraphEntry& g : graphs)
+      if (g.key == key) hit = &g;
+    if (!hit) {
+      const long long before = launches_total();
+      cudaGraph_t g = nullptr;
+      CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+      try {
+        launchTick(p);
+      } catch (...) {
+        cudaStreamEndCapture(s, &g);
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();
+        throw;
+      }
+      cudaError_t e = cudaStreamEndCapture(s, &g);
+      cudaGraphExec_t x = nullptr;
+      if (e == cudaSuccess) e = cudaGraphInstantiate(&x, g, 0);
+      if (g) cudaGraphDestroy(g);
+      const long long n = launches_total() - before;
+      note_launches(int(-n));  // recorded, not run
+      if (e != cudaSuccess) {
+        cudaGetLastError();
+        graphsOn = false;
+        graphsOff = std::string("graph capture failed: ") + cudaGetErrorString(e);
+        std::fprintf(stderr, "avbd_gb300: %s; ticks are launched directly\n", graphsOff.c_str());
+        launchTick(p);
+        return;
+      }
+      if (graphs.size() >= 8) {
+        auto lru = std::min_element(graphs.begin(), graphs.end(), [](const GraphEntry& a, const GraphEntry& b) { return a.use < b.use; });
+        cudaGraphExecDestroy(lru->exec);
+        graphs.erase(lru);
+      }
+      graphs.push_back(GraphEntry{key, x, n, 0});
+      hit = &graphs.back();
+      graphCaptures++;
+    } else {
+      graphReplays++;
+    }
+    hit->use = ++graphClock;
+    CK(cudaGraphLaunch(hit->exec, s));
+    note_launches(int(hit->launches));
+  }
+
+  // Body commands and wakes queued for the tick's worlds (kernels that do nothing when held):
+  // one upload and one launch for all of them, records addressed by global body index.
+  void applyTickCommands(const TickLog& e) {
+    for (const TickPre& pr : e.pre) {
+      const WorldRec& R = W[pr.w];
+      if (pr.wake && (R.dev.flags & FLAG_SLEEP) && R.nBodies) launch_sleep_wake(B, R.dev.bodyOff, R.nBodies, ctl, s);
+    }
+    size_t total = 0;
+    for (const TickPre& pr : e.pre) total += pr.edits.size() / 12;
+    if (total == 0) return;
+    std::vector<uint32_t> recs;
+    recs.reserve(12 * total);
+    for (const TickPre& pr : e.pre) {
+      const uint32_t off = uint32_t(W[pr.w].dev.bodyOff);
+      const size_t n = pr.edits.size() / 12;
+      for (size_t k = 0; k < n; k++) {
+        const uint32_t* u = pr.edits.data() + 12 * k;
+        recs.insert(recs.end(), u, u + 12);
+        recs[recs.size() - 12] = u[0] + off;
+      }
+    }
+    uploadCommands(recs, 0);
+    for (const TickPre& pr : e.pre) dropTeleported(pr.w, pr.edits);
+  }
+
+  // One step of the given resident worlds, queued on the arena's stream without waiting.
+  void stepWorlds(std::vector<int> act) {
+    std::sort(act.begin(), act.end(), [&](int a, int b) { return W[a].dev.bodyOff < W[b].dev.bodyOff; });
+    act.erase(std::unique(act.begin(), act.end()), act.end());
+    for (int w : act)
+      if (w < 0 || w >= maxWorlds || !W[w].live || !W[w].resident) throw Error(AVBD_E_INVALID, "stepping a world that is not resident");
+    if (hostHeld()) resolve();  // a held tick: grow and re-run it before queueing more
+    trimLog();
+    TickLog e;
+    e.act = act;
+    e.pre.reserve(act.size());
+    for (int w : act) {
+      WorldRec& R = W[w];
+      TickPre pr;
+      pr.w = w;
+      pr.which = R.which;
+      pr.sinceBuild = R.sinceBuild;
+      pr.steps = R.steps;
+      pr.built = R.built;
+      pr.wake = R.wakePending;
+      pr.edits.swap(R.edits);
+      R.wakePending = false;
+      e.pre.push_back(std::move(pr));
+    }
+    tickLog.push_back(std::move(e));
+    queueTick(tickLog.back());
+  }
+
+  void queueTick(TickLog& e) {
+    const std::vector<int>& act = e.act;
+    applyTickCommands(e);
+    int nb = 0, nj = 0, maxIter = 0;
+    tickTriggers = false;
+    TickPlan p;
+    for (int w : act) {
+      const WorldRec& R = W[w];
+      tickTriggers |= R.triggers;
+      nb += R.nBodies;
+      nj += R.nJoints;
+      maxIter = std::max(maxIter, R.dev.iterations);
+      p.bounce |= (R.dev.flags & FLAG_RESTITUTION) != 0;
+      p.sleeping |= (R.dev.flags & FLAG_SLEEP) != 0;
+      p.events |= (R.dev.flags & FLAG_EVENTS) != 0;
+    }
+    p.sleepy = p.sleeping;
+    const int na = int(act.size());
+    if (act != actUploaded || uploadedWorlds != maxWorlds) {
+      std::vector<int4> table(size_t(std::max(na, 1)));
+      std::vector<int> wtab(size_t(maxWorlds), -1);
+      int b0 = 0, j0 = 0;
+      for (int a = 0; a < na; a++) {
+        table[a] = make_int4(act[a], b0, j0, 0);
+        wtab[act[a]] = a;
+        b0 += W[act[a]].nBodies;
+        j0 += W[act[a]].nJoints;
+      }
+      if (na) put(active, table.data(), sizeof(int4) * na);
+      put(wactive, wtab.data(), sizeof(int) * maxWorlds);
+      actUploaded = act;
+      uploadedWorlds = maxWorlds;
+      actVersion++;
+    }
+    long long budget = 0;
+    for (int w : act) budget += W[w].dev.pairCap;
+    ensureItems(nb);
+    if (p.bounce) ensureBounce();
+    if (p.sleeping) ensureSleep();
+    for (int w : act) {
+      WorldRec& R = W[w];
+      if (!R.bvh || R.nBodies == 0) continue;
+      const bool rebuild = !R.built || R.sinceBuild >= R.bvhRebuild;
+      if (rebuild) ensureBvhScratch(R);
+      p.trees.push_back({w, rebuild ? 1 : 0});
+    }
+    // the autotuner's choice for this class of tick (or a candidate to time)
+    {
+      std::vector<cudaEvent_t> freed;
+      tuner.harvest(false, freed);
+      for (cudaEvent_t ev : freed) pool.push_back(ev);
+      bool rebuild = false;
+      for (auto& tr : p.trees) rebuild |= tr.second != 0;
+      int sizeLog2 = 0;
+      while ((1LL << sizeLog2) < (long long)std::max(nb, 1)) sizeLog2++;
+      const TuneKey key{ctx->device, sizeLog2, nj > 0 ? 1 : 0, maxIter};
+      int sc = -1, rc = -1;
+      tuner.pick(key, rebuild, device_sms(), solveCfg, radixBits, sc, rc);
+      p.radixBits = radixBits;
+      if ((sc >= 0 || rc >= 0) && !prof) {
+        if (sc >= 0) {
+          p.tune[0] = event();
+          p.tune[1] = event();
+        }
+        if (rc >= 0) {
+          p.tune[2] = event();
+          p.tune[3] = event();
+        }
+        tuner.pending.push_back(Tuner::Pending{key, sc, rc, p.tune[0], p.tune[1], p.tune[2], p.tune[3]});
+      }
+      lastTuned = tuner.settled(key, !p.trees.empty());
+    }
+    p.t = tick(na, nb, nj);
+    p.na = na;
+    p.nb = nb;
+    p.nj = nj;
+    p.maxIter = maxIter;
+    p.pairBudget = int(std::min<long long>(budget, slotCap));
+    p.itemCap = (long long)itemCap;
+    // host state of the stepped worlds after this tick
+    for (auto& tr : p.trees) {
+      WorldRec& R = W[tr.first];
+      if (tr.second) {
+        R.built = true;
+        R.sinceBuild = 0;
+      }
+      R.sinceBuild++;
+    }
+    for (int w : act) {
+      W[w].which ^= 1;
+      W[w].steps++;
+    }
+    runTick(p);
+    e.done = tickEvent();
+    CK(cudaEventRecord(e.done, s));
+    if (prof) {  // the tick's algorithmic bytes (profiling runs only)
       CK(cudaMemsetAsync(traffic, 0, 3 * sizeof(unsigned long long), s));
-      launch_traffic(B, J, P, t, T, ctr, pairBudget, traffic, s);
+      launch_traffic(B, J, P, p.t, T, ctr, p.pairBudget, traffic, s);
       unsigned long long tb[3];
       CK(cudaMemcpyAsync(tb, traffic, sizeof(tb), cudaMemcpyDeviceToHost, s));
       CK(cudaStreamSynchronize(s));
+      harvest();
       profBytes[0] += double(tb[0]) * maxIter;
       profBytes[1] += double(tb[1]) * maxIter;
       profBytes[2] += double(tb[2]);
       profSteps++;
     }
-    launch_tick_end(t, s);
-    for (int w : act) {
-      W[w].which ^= 1;
-      W[w].steps++;
-    }
-    lastPairs = ctrHost->activePairs;
     lastJoints = nj;
+    statsValid = true;
     steps++;
     haveStats = false;
     CK(cudaGetLastError());
@@ -2042,7 +2514,11 @@ class Arena {
 
   // ------------------------------------------------------------------ reads
   void syncStats() {
+    resolve();
     if (haveStats) return;
+    int np = 0;
+    getRaw(&np, &ctr->activePairs, sizeof(int));
+    lastPairs = statsValid ? np : 0;
     launch_count_active(J, P, activePairs, lastPairs, activeJoints, lastJoints, ctr, s);
     CK(cudaMemcpyAsync(ctrHost, ctr, sizeof(Counters), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
@@ -2062,6 +2538,7 @@ class Arena {
   }
 
   template <class X> std::vector<X> fetch(const X* d, size_t off, size_t n) {
+    resolve();
     std::vector<X> h(n);
     if (n) CK(cudaMemcpyAsync(h.data(), d + off, n * sizeof(X), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
@@ -2076,6 +2553,7 @@ class Arena {
 
   void readState(int w, float* position, float* rotation, float* velocity, float* angular, float* prevVel) {
     const WorldRec& R = resident(w);
+    touch(w);  // queued commands apply before a read (src/native/solver3D.js:223-227,245,249)
     const size_t off = R.dev.bodyOff, n = R.nBodies;
     auto put3 = [&](float* out, const float4* d) {
       if (!out) return;

@@ -116,43 +116,53 @@ __global__ void k_bvh_morton(BvhPool b, int nodeOff, int n, const float4* __rest
   keys[i] = make_uint2(code, uint32_t(i));
 }
 
-// Radix sort pass 1: per-block digit counts, digit-major (hist[digit * blocks + block]).
+// Radix sort of the (code, leaf) keys by code, BITS bits per pass (4, 6 or 8: the autotuner's
+// digit-width candidates; every width gives the same stable order).
+// Pass 1: per-block digit counts, digit-major (hist[digit * blocks + block]).
+template <int BITS>
 __global__ void __launch_bounds__(RADIX_THREADS) k_radix_hist(const uint2* __restrict__ in, int n, int shift, int* hist) {
-  __shared__ int cnt[256];
-  cnt[threadIdx.x] = 0;
+  constexpr int DIGITS = 1 << BITS;
+  constexpr uint32_t MASK = DIGITS - 1;
+  __shared__ int cnt[DIGITS];
+  for (int q = threadIdx.x; q < DIGITS; q += RADIX_THREADS) cnt[q] = 0;
   __syncthreads();
   const int base = blockIdx.x * RADIX_ITEMS;
   for (int k = threadIdx.x; k < RADIX_ITEMS; k += RADIX_THREADS) {
     const int e = base + k;
-    if (e < n) atomicAdd(&cnt[(in[e].x >> shift) & 255u], 1);
+    if (e < n) atomicAdd(&cnt[(in[e].x >> shift) & MASK], 1);
   }
   __syncthreads();
-  hist[threadIdx.x * gridDim.x + blockIdx.x] = cnt[threadIdx.x];
+  for (int q = threadIdx.x; q < DIGITS; q += RADIX_THREADS) hist[q * gridDim.x + blockIdx.x] = cnt[q];
 }
 
-// Radix sort pass 2: stable scatter. Each round ranks 256 consecutive keys (warp match for the
-// rank inside a warp, per-warp digit counts for the warps before) after the block's earlier
-// rounds, so equal digits keep their input order.
+// Pass 2: stable scatter. Each round ranks RADIX_THREADS consecutive keys (warp match for the rank
+// inside a warp, per-warp digit counts for the warps before) after the block's earlier rounds,
+// so equal digits keep their input order.
+template <int BITS>
 __global__ void __launch_bounds__(RADIX_THREADS) k_radix_scatter(const uint2* __restrict__ in, uint2* __restrict__ out, int n, int shift,
                                                                  const int* __restrict__ offsets) {
+  constexpr int DIGITS = 1 << BITS;
+  constexpr uint32_t MASK = DIGITS - 1;
   constexpr int WARPS = RADIX_THREADS / 32;
-  __shared__ int warpCnt[WARPS][256];
-  __shared__ int running[256];
-  __shared__ int start[256];
+  __shared__ int warpCnt[WARPS][DIGITS];
+  __shared__ int running[DIGITS];
+  __shared__ int start[DIGITS];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  start[threadIdx.x] = offsets[threadIdx.x * gridDim.x + blockIdx.x];
-  running[threadIdx.x] = 0;
-  for (int w = 0; w < WARPS; w++) warpCnt[w][threadIdx.x] = 0;
+  for (int q = threadIdx.x; q < DIGITS; q += RADIX_THREADS) {
+    start[q] = offsets[q * gridDim.x + blockIdx.x];
+    running[q] = 0;
+    for (int w = 0; w < WARPS; w++) warpCnt[w][q] = 0;
+  }
   __syncthreads();
   const int base = blockIdx.x * RADIX_ITEMS;
   for (int round = 0; round < RADIX_ITEMS / RADIX_THREADS; round++) {
     const int e = base + round * RADIX_THREADS + threadIdx.x;
     const bool valid = e < n;
     uint2 v = make_uint2(0u, 0u);
-    uint32_t d = 256u;  // out-of-range keys form their own (unused) digit
+    uint32_t d = uint32_t(DIGITS);  // out-of-range keys form their own (unused) digit
     if (valid) {
       v = in[e];
-      d = (v.x >> shift) & 255u;
+      d = (v.x >> shift) & MASK;
     }
     const unsigned peers = __match_any_sync(0xffffffffu, d);
     const int rankInWarp = __popc(peers & ((1u << lane) - 1u));
@@ -164,14 +174,31 @@ __global__ void __launch_bounds__(RADIX_THREADS) k_radix_scatter(const uint2* __
       out[start[d] + before + rankInWarp] = v;
     }
     __syncthreads();
-    int total = 0;
-    for (int w = 0; w < WARPS; w++) {
-      total += warpCnt[w][threadIdx.x];
-      warpCnt[w][threadIdx.x] = 0;
+    for (int q = threadIdx.x; q < DIGITS; q += RADIX_THREADS) {
+      int total = 0;
+      for (int w = 0; w < WARPS; w++) {
+        total += warpCnt[w][q];
+        warpCnt[w][q] = 0;
+      }
+      running[q] += total;
     }
-    running[threadIdx.x] += total;
     __syncthreads();
   }
+}
+
+template <int BITS>
+static int radix_passes(const uint2*& keysOut, BvhScratch sc, int n, int rb, void* scanTemp, cudaStream_t s) {
+  constexpr int PASSES = (30 + BITS - 1) / BITS;  // codes have 30 bits
+  for (int pass = 0; pass < PASSES; pass++) {
+    const uint2* in = sc.keys[pass & 1];
+    uint2* out = sc.keys[(pass & 1) ^ 1];
+    k_radix_hist<BITS><<<rb, RADIX_THREADS, 0, s>>>(in, n, BITS * pass, sc.hist);
+    scan_exclusive(sc.hist, (1 << BITS) * rb, nullptr, scanTemp, s);
+    k_radix_scatter<BITS><<<rb, RADIX_THREADS, 0, s>>>(in, out, n, BITS * pass, sc.hist);
+    note_launches(2);
+  }
+  keysOut = sc.keys[PASSES & 1];
+  return PASSES;
 }
 
 __global__ void k_bvh_seed(const uint2* __restrict__ keys, int n, uint32_t* clusters) {
@@ -321,32 +348,28 @@ size_t bvh_scratch_hist(int n) { return size_t(256) * size_t(blocks_of(n, RADIX_
 size_t bvh_scratch_bounds(int n) { return size_t(2) * size_t(blocks_of(n, 256)) + 2; }
 
 void launch_bvh_build(const BodyPtrs& bd, int bodyOff, int n, BvhPool b, int nodeOff, const BvhLayout& L, BvhScratch sc,
-                      void* scanTemp, cudaStream_t s) {
+                      void* scanTemp, int radixBits, cudaStream_t s) {
   if (n <= 0) return;
   const int lb = blocks_of(n, 256);
-  k_bvh_init_links<<<blocks_of(L.nodes, 256) > 152 * 8 ? 152 * 8 : blocks_of(L.nodes, 256), 256, 0, s>>>(b, nodeOff, L.nodes);
+  k_bvh_init_links<<<blocks_of(L.nodes, 256) > device_sms() * 8 ? device_sms() * 8 : blocks_of(L.nodes, 256), 256, 0, s>>>(b, nodeOff, L.nodes);
   float4* bounds = sc.bounds + 2 * size_t(lb);
   k_bvh_leaves<<<lb, 256, 0, s>>>(bd.pose, bodyOff, n, b, nodeOff, sc.bounds, 1);
   k_bvh_bounds<<<1, 256, 0, s>>>(sc.bounds, lb, bounds);
   k_bvh_morton<<<lb, 256, 0, s>>>(b, nodeOff, n, bounds, sc.keys[0]);
   note_launches(4);
   const int rb = blocks_of(n, RADIX_ITEMS);
-  for (int pass = 0; pass < 4; pass++) {  // codes have 30 bits: four 8-bit digits
-    const uint2* in = sc.keys[pass & 1];
-    uint2* out = sc.keys[(pass & 1) ^ 1];
-    k_radix_hist<<<rb, RADIX_THREADS, 0, s>>>(in, n, 8 * pass, sc.hist);
-    scan_exclusive(sc.hist, 256 * rb, nullptr, scanTemp, s);
-    k_radix_scatter<<<rb, RADIX_THREADS, 0, s>>>(in, out, n, 8 * pass, sc.hist);
-    note_launches(2);
-  }
-  k_bvh_seed<<<lb, 256, 0, s>>>(sc.keys[0], n, sc.clusters);  // four passes end in keys[0]
+  const uint2* sorted = nullptr;
+  if (radixBits == 4) radix_passes<4>(sorted, sc, n, rb, scanTemp, s);
+  else if (radixBits == 6) radix_passes<6>(sorted, sc, n, rb, scanTemp, s);
+  else radix_passes<8>(sorted, sc, n, rb, scanTemp, s);
+  k_bvh_seed<<<lb, 256, 0, s>>>(sorted, n, sc.clusters);
   note_launches(1);
   for (const BvhLevel& v : L.levels) {
     k_bvh_treelets<<<v.blocks, 32, 0, s>>>(b, nodeOff, sc.clusters, v.inputOffset, v.outputOffset, v.inputCount, v.nodeBase);
     note_launches(1);
   }
   int rblocks = blocks_of(L.nodes, 256);
-  if (rblocks > 152 * 8) rblocks = 152 * 8;
+  if (rblocks > device_sms() * 8) rblocks = device_sms() * 8;
   k_bvh_ropes<<<rblocks, 256, 0, s>>>(b, nodeOff, L.nodes, L.root);
   note_launches(1);
 }

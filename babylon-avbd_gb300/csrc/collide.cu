@@ -385,7 +385,7 @@ void launch_pairs(const BodyPtrs& b, const WorldDev* worlds, Tick t, Grid g, NoC
   scan_exclusive(t.pairPrefix, t.nActive + 1, &ctr->activePairs, scanTemp, s);
   k_pair_write<<<grid_blocks(t.nBodies, 128), 128, 0, s>>>(c, worlds, g, t, pairCount, P.pair); note_launches(1);
   int blocks = grid_blocks(t.nBodies * 8LL, 256);
-  if (blocks > 152 * 16) blocks = 152 * 16;
+  if (blocks > device_sms() * 16) blocks = device_sms() * 16;
   k_pair_slots<<<blocks, 256, 0, s>>>(worlds, t, ctr); note_launches(1);
 }
 
@@ -698,8 +698,21 @@ __device__ __forceinline__ V3 box_support(const BoxGeo& g, V3 n) {
   return best;
 }
 
-// support of a sphere (both spine points coincide): first of the two, pushed out by r
-__device__ __forceinline__ V3 sphere_support(V3 c, float r, V3 n) { return madd(c, n, r); }
+// A round body's spine (cpuContacts3D.js:44-51): a capsule's segment along its local Y, of
+// half-length height / 2 - r; a sphere's is its centre (both ends at a zero offset).
+__device__ __forceinline__ void spine_of(float4 p, float4 q, float4 size, int shape, V3& s0, V3& s1) {
+  const float r = size.x / 2;
+  const float half = shape == SHAPE_CAPSULE ? fmaxf(0.f, size.y / 2 - r) : 0.f;
+  const V3 c = v3(p);
+  s0 = c + rotate(q, V3{0.f, -half, 0.f});
+  s1 = c + rotate(q, V3{0.f, half, 0.f});
+}
+
+// support of a round body: the first spine end of greatest dot(v, n), pushed out by r
+__device__ __forceinline__ V3 round_support(V3 s0, V3 s1, float r, V3 n) {
+  const V3 p = dot(s1, n) > dot(s0, n) ? s1 : s0;
+  return madd(p, n, r);
+}
 
 __device__ __forceinline__ void closest_seg(V3 p, V3 q, V3 r, V3 s, V3& oa, V3& ob) {
   V3 d1 = q - p, d2 = s - r, w = p - r;
@@ -762,24 +775,24 @@ __device__ __forceinline__ V3 closest_surface(const BoxGeo& g, V3 p) {
   return best;
 }
 
-// At least one body is a sphere (BOTH_ROUND: both are, and the box code compiles away). Returns
-// the contact count (0 or 1).
+// At least one body is round, a sphere or a capsule (BOTH_ROUND: both are, and the box code
+// compiles away). Returns the contact count (0 or 1).
 template <bool BOTH_ROUND>
 __device__ int collide(float4 pA, float4 qA, float4 sA, int shA, float4 pB, float4 qB, float4 sB, int shB, M33& basis,
                        V3& rA, V3& rB) {
-  const bool roundA = BOTH_ROUND || shA == SHAPE_SPHERE, roundB = BOTH_ROUND || shB == SHAPE_SPHERE;
+  const bool roundA = BOTH_ROUND || shA != SHAPE_BOX, roundB = BOTH_ROUND || shB != SHAPE_BOX;
   BoxGeo box;
   const V3 cA = v3(pA), cB = v3(pB);
-  // a sphere's spine is its centre (rotate of a zero offset adds +-0)
-  const V3 spA = cA + rotate(qA, V3{0.f, 0.f, 0.f});
-  const V3 spB = cB + rotate(qB, V3{0.f, 0.f, 0.f});
+  V3 spA0{0.f, 0.f, 0.f}, spA1{0.f, 0.f, 0.f}, spB0{0.f, 0.f, 0.f}, spB1{0.f, 0.f, 0.f};
+  if (roundA) spine_of(pA, qA, sA, shA, spA0, spA1);
+  if (roundB) spine_of(pB, qB, sB, shB, spB0, spB1);
   const float radA = sA.x / 2, radB = sB.x / 2;
   if (!roundA) box_geo(box, pA, qA, sA);
   else if (!roundB) box_geo(box, pB, qB, sB);
   float gap = -INFINITY;
   V3 n{0.f, 0.f, 1.f};
-  auto supA = [&](V3 d) { return roundA ? sphere_support(spA, radA, d) : box_support(box, d); };
-  auto supB = [&](V3 d) { return roundB ? sphere_support(spB, radB, d) : box_support(box, d); };
+  auto supA = [&](V3 d) { return roundA ? round_support(spA0, spA1, radA, d) : box_support(box, d); };
+  auto supB = [&](V3 d) { return roundB ? round_support(spB0, spB1, radB, d) : box_support(box, d); };
   auto consider = [&](V3 axis) {
     if (hyp(axis) < 1e-9f) return;
     V3 v = unitv(axis);
@@ -808,7 +821,7 @@ __device__ int collide(float4 pA, float4 qA, float4 sA, int shA, float4 pB, floa
     }
   if (roundA && roundB) {
     V3 pa, pb;
-    closest_seg(spA, spA, spB, spB, pa, pb);
+    closest_seg(spA0, spA1, spB0, spB1, pa, pb);
     consider(pa - pb);
     if (gap > 0) return 0;
   }
@@ -818,20 +831,19 @@ __device__ int collide(float4 pA, float4 qA, float4 sA, int shA, float4 pB, floa
     const bool isRound = roundIsA ? roundA : roundB;
     const bool polyIsBox = roundIsA ? !roundB : !roundA;
     if (!isRound || !polyIsBox) continue;
-    const V3 sp = roundIsA ? spA : spB;
-    for (int i = 0; i < 8; i++) {
-      // nearest(spine0, spine1, v) on a degenerate spine is spine0
-      V3 e = sp - sp;
-      V3 ap = box.v[i] - sp;
-      float ee = dot(e, e);
+    const V3 s0 = roundIsA ? spA0 : spB0, s1 = roundIsA ? spA1 : spB1;
+    const V3 e = s1 - s0;
+    const float ee = dot(e, e);
+    for (int i = 0; i < 8; i++) {  // vertex to its nearest spine point (cpuContacts3D.js nearest)
+      V3 ap = box.v[i] - s0;
       float t = dot(ap, e) / (ee != 0.f ? ee : 1.f);
       t = fmaxf(0.f, fminf(1.f, t));
-      consider(box.v[i] - madd(sp, e, t));
+      consider(box.v[i] - madd(s0, e, t));
       if (gap > 0) return 0;
     }
     for (int i = 0; i < 12; i++) {
       V3 pa, pb;
-      closest_seg(sp, sp, box.v[kEdges[i][0]], box.v[kEdges[i][1]], pa, pb);
+      closest_seg(s0, s1, box.v[kEdges[i][0]], box.v[kEdges[i][1]], pa, pb);
       consider(pa - pb);
       if (gap > 0) return 0;
     }
@@ -845,14 +857,14 @@ __device__ int collide(float4 pA, float4 qA, float4 sA, int shA, float4 pB, floa
   V3 xa, xb;
   if (roundA && roundB) {
     V3 pa, pb;
-    closest_seg(spA, spA, spB, spB, pa, pb);
+    closest_seg(spA0, spA1, spB0, spB1, pa, pb);
     xa = madd(pa, n, -radA);
     xb = madd(pb, n, radB);
   } else if (roundA) {
-    xa = sphere_support(spA, radA, n * -1.f);
+    xa = round_support(spA0, spA1, radA, n * -1.f);
     xb = closest_surface(box, xa);
   } else {
-    xb = sphere_support(spB, radB, n);
+    xb = round_support(spB0, spB1, radB, n);
     xa = closest_surface(box, xb);
   }
   rA = rotateInv(qA, xa - cA);
@@ -950,9 +962,9 @@ __global__ void __launch_bounds__(256) k_np_classify(BodyPtrs bd, const WorldDev
       const uint2 key = cur.pair[p];
       const int a = int(key.x), b = int(key.y);
       const int shA = bd.meta[a].y, shB = bd.meta[b].y;
-      if (shA == SHAPE_SPHERE || shB == SHAPE_SPHERE) {
+      if (shA != SHAPE_BOX || shB != SHAPE_BOX) {  // a sphere or a capsule: the generic path
         sphere = true;
-        bothRound = shA == SHAPE_SPHERE && shB == SHAPE_SPHERE;
+        bothRound = shA != SHAPE_BOX && shB != SHAPE_BOX;
       } else {
         const WorldDev& W = worlds[bd.meta[a].x];
         box::Sat best;
@@ -1011,7 +1023,9 @@ __global__ void __launch_bounds__(128, AVBD_NP_BOX_MINB) k_np_box(BodyPtrs bd, c
 // A sphere and a box clearly apart: the distance from the sphere's centre to the box exceeds its
 // radius by far more than any rounding of the separating-axis search (1e-3 plus 1e-5 of the
 // coordinates' size), so that search would end with a positive gap and no contact: skip it.
-__device__ __forceinline__ bool sphere_box_apart(float4 pA, float4 qA, float4 sA, int shA, float4 pB, float4 qB, float4 sB) {
+__device__ __forceinline__ bool sphere_box_apart(float4 pA, float4 qA, float4 sA, int shA, float4 pB, float4 qB, float4 sB,
+                                                 int shB) {
+  if (shA == SHAPE_CAPSULE || shB == SHAPE_CAPSULE) return false;  // capsules always run the search
   const bool sphereA = shA == SHAPE_SPHERE;
   const float4 pc = sphereA ? pA : pB, pbx = sphereA ? pB : pA, qbx = sphereA ? qB : qA, sbx = sphereA ? sB : sA;
   const float r = (sphereA ? sA : sB).x * 0.5f;
@@ -1042,7 +1056,7 @@ __global__ void __launch_bounds__(128, AVBD_NP_SPHERE_MINB) k_np_sphere(BodyPtrs
     M33 basis{V3{0, 0, 0}, V3{0, 0, 0}, V3{0, 0, 0}};
     uint32_t feat[1] = {1u};  // feature i + 1
     V3 rA[1], rB[1];
-    const int nc = (!BOTH_ROUND && sphere_box_apart(pA, qA, sA, shA, pB, qB, sB))
+    const int nc = (!BOTH_ROUND && sphere_box_apart(pA, qA, sA, shA, pB, qB, sB, shB))
                        ? 0
                        : gen::collide<BOTH_ROUND>(pA, qA, sA, shA, pB, qB, sB, shB, basis, rA[0], rB[0]);
     finish_pair(bd, W, t, bd.meta[a].x, cur, p, key, pA, qA, sA, pB, qB, sB, true, nc, basis, feat, rA, rB);
@@ -1054,11 +1068,11 @@ void launch_narrowphase(const BodyPtrs& b, const WorldDev* worlds, Tick t, PairP
   cudaMemsetAsync(ns.ctr, 0, 3 * sizeof(int), s);
   if (t.nActive == 0) return;
   int blocks = grid_blocks(pairBudget, 256);
-  if (blocks > 152 * 16) blocks = 152 * 16;
+  if (blocks > device_sms() * 16) blocks = device_sms() * 16;
   k_np_classify<<<blocks, 256, 0, s>>>(b, worlds, P, t, ctr, ns); note_launches(1);
-  k_np_box<<<152 * 16, 128, 0, s>>>(b, worlds, P, t, ns); note_launches(1);
-  k_np_sphere<false><<<152 * 16, 128, 0, s>>>(b, worlds, P, t, ns); note_launches(1);
-  k_np_sphere<true><<<152 * 16, 128, 0, s>>>(b, worlds, P, t, ns); note_launches(1);
+  k_np_box<<<device_sms() * 16, 128, 0, s>>>(b, worlds, P, t, ns); note_launches(1);
+  k_np_sphere<false><<<device_sms() * 16, 128, 0, s>>>(b, worlds, P, t, ns); note_launches(1);
+  k_np_sphere<true><<<device_sms() * 16, 128, 0, s>>>(b, worlds, P, t, ns); note_launches(1);
 }
 
 }  // namespace avbd

@@ -53,7 +53,8 @@ __global__ void k_read_selected(BodyPtrs bd, const WorldDev* __restrict__ worlds
     o[24] = py.x; o[25] = py.y; o[26] = py.z; o[27] = 0.f;
     o[28] = qy.x; o[29] = qy.y; o[30] = qy.z; o[31] = qy.w;
     o[32] = v.x; o[33] = v.y; o[34] = v.z; o[35] = (vp.x * W.up0 + vp.y * W.up1) + vp.z * W.up2;
-    o[36] = w.x; o[37] = w.y; o[38] = w.z; o[39] = float(meta.y);
+    // shape code of world.js:543-551: box 0, sphere 1, capsule -1
+    o[36] = w.x; o[37] = w.y; o[38] = w.z; o[39] = meta.y == SHAPE_CAPSULE ? -1.f : float(meta.y);
   }
 }
 
@@ -124,6 +125,7 @@ Arena* arenaFor(avbd_ctx* ctx, const avbd_scene_desc* scenes, const avbd_params*
 void readSelected(Arena& A, int w, const uint32_t* indices, int n, int posesOnly, float* out) {
   const WorldRec& R = A.resident(w);
   for (int k = 0; k < n; k++) REQUIRE(indices[k] < uint32_t(R.nBodies), "body index out of range");
+  A.flushEdits(w);  // queued commands apply before a read (src/native/solver3D.js:223-227,245,249)
   if (n == 0) return;
   const int stride = posesOnly ? 8 : 40;
   const size_t ib = Arena::align256(size_t(n) * 4);
@@ -137,23 +139,32 @@ void readSelected(Arena& A, int w, const uint32_t* indices, int n, int posesOnly
   A.flush();
 }
 
-void setVelocities(Arena& A, int off, int limit, const uint32_t* indices, int n, const float* velocity, const float* angular) {
+// setVelocities / setLinearVelocities / setAngularVelocities (src/native/runtime.js:354-380):
+// like the reference's velocity batches, the writes are queued in stream order with the steps:
+// body commands of kind 0 (linear) and 1 (angular) for the world's next step or read. `indices`
+// are global to the worlds listed in `starts` (first body index of each, ascending).
+void setVelocities(Arena& A, const std::vector<std::pair<long long, int>>& starts, long long limit, const uint32_t* indices, int n,
+                   const float* velocity, const float* angular) {
   REQUIRE(n == 0 || indices, "null argument");
   REQUIRE(n >= 0, "negative count");
-  for (int k = 0; k < n; k++) REQUIRE(indices[k] < uint32_t(limit), "body index out of range");
+  for (int k = 0; k < n; k++) REQUIRE((long long)indices[k] < limit, "body index out of range");
   for (int k = 0; velocity && k < 3 * n; k++) REQUIRE(std::isfinite(velocity[k]), "velocities must be finite");
   for (int k = 0; angular && k < 3 * n; k++) REQUIRE(std::isfinite(angular[k]), "velocities must be finite");
   if (n == 0 || (!velocity && !angular)) return;
-  const size_t ib = Arena::align256(size_t(n) * 4), vb = Arena::align256(size_t(n) * 12);
-  char* io = A.ioBuffer(ib + 2 * vb);
-  uint32_t* di = reinterpret_cast<uint32_t*>(io);
-  float* dv = velocity ? reinterpret_cast<float*>(io + ib) : nullptr;
-  float* da = angular ? reinterpret_cast<float*>(io + ib + vb) : nullptr;
-  A.put(di, indices, size_t(n) * 4);
-  if (dv) A.put(dv, velocity, size_t(n) * 12);
-  if (da) A.put(da, angular, size_t(n) * 12);
-  k_set_velocities<<<grid_blocks(n, 128), 128, 0, A.s>>>(A.B, di, n, off, dv, da); note_launches(1);
-  CK(cudaGetLastError());
+  std::map<int, std::vector<uint32_t>> per;  // world slot -> records
+  for (int k = 0; k < n; k++) {
+    const auto it = std::upper_bound(starts.begin(), starts.end(), std::make_pair((long long)indices[k], INT32_MAX)) - 1;
+    std::vector<uint32_t>& r = per[it->second];
+    const uint32_t local = uint32_t((long long)indices[k] - it->first);
+    for (int kind = 0; kind < 2; kind++) {
+      const float* v = kind == 0 ? velocity : angular;
+      if (!v) continue;
+      uint32_t rec[12] = {local, uint32_t(kind), 0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
+      std::memcpy(rec + 4, v + 3 * size_t(k), 12);
+      r.insert(r.end(), rec, rec + 12);
+    }
+  }
+  for (auto& kv : per) A.queueEdits(kv.first, kv.second.data(), int(kv.second.size() / 12));
 }
 
 }  // namespace
@@ -192,6 +203,7 @@ int avbd_ctx_synchronize(avbd_ctx* ctx) {
   API_BEGIN
   REQUIRE(ctx, "null context");
   bind(ctx);
+  for (void* p : ctx->owned) static_cast<Arena*>(p)->resolve();  // queued steps final (held ones re-run)
   CK(cudaStreamSynchronize(ctx->stream));
   API_END
 }
@@ -268,21 +280,16 @@ static __device__ __align__(256) float g_select_scratch[AVBD_NOALLOC_MAX_SELECTE
 
 namespace {
 
-std::mutex g_select_mutex;
-float* g_select_ptr[256] = {};
-
-// Device address of g_select_scratch on `device` (which must be current): looked up once per
-// device. In host code the symbol itself is only a host-side stand-in for the device array.
+// Device address of g_select_scratch on `device` (which must be current). In host code the
+// symbol itself is only a host-side stand-in for the device array. The address is looked up on
+// every call (a cheap query that allocates nothing), so a primary context that was reset in
+// between (cudaDeviceReset) never leaves a stale address behind.
 float* select_scratch(int device) {
-  std::lock_guard<std::mutex> lock(g_select_mutex);
-  if (device < 0 || device >= 256) throw Error(AVBD_E_INVALID, "device index out of range");
-  if (!g_select_ptr[device]) {
-    void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_select_scratch);
-    if (e != cudaSuccess) throw Error(AVBD_E_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-    g_select_ptr[device] = static_cast<float*>(p);
-  }
-  return g_select_ptr[device];
+  if (device < 0) throw Error(AVBD_E_INVALID, "device index out of range");
+  void* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_select_scratch);
+  if (e != cudaSuccess) throw Error(AVBD_E_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+  return static_cast<float*>(p);
 }
 
 }  // namespace
@@ -300,6 +307,16 @@ int avbd_world_read_selected_noalloc(avbd_world* w, const uint32_t* indices, int
   bind(A.ctx);
   const WorldRec& R = A.resident(w->w);
   for (int k = 0; k < n; k++) REQUIRE(indices[k] < uint32_t(R.nBodies), "body index out of range");
+  // A read sees the queued body commands applied (src/native/solver3D.js:223-227). Applying them
+  // can grow the command buffers, which allocates, so this entry point refuses instead.
+  if (!R.edits.empty() || R.wakePending)
+    throw Error(AVBD_E_STATE, "avbd_world_read_selected_noalloc: the world has queued body commands; apply them first "
+                              "(avbd_world_flush_edits or a step)");
+  // Steps still queued must be final; one that overflowed needs buffer growth (an allocation), so
+  // this entry point refuses then too.
+  if (!A.settle())
+    throw Error(AVBD_E_STATE, "avbd_world_read_selected_noalloc: a queued step needs more buffer room; make it final first "
+                              "(any other read, or avbd_ctx_synchronize)");
   if (n == 0) return AVBD_OK;
   float* scratch = select_scratch(A.ctx->device);
   uint32_t* dIdx = reinterpret_cast<uint32_t*>(scratch);
@@ -350,8 +367,7 @@ int avbd_world_set_velocities(avbd_world* w, const uint32_t* indices, int32_t n,
   Arena& A = *w->A;
   bind(A.ctx);
   const WorldRec& R = A.resident(w->w);
-  setVelocities(A, R.dev.bodyOff, R.nBodies, indices, n, velocity, angular);
-  if (n > 0) A.wakeWorld(w->w);
+  setVelocities(A, {{0LL, w->w}}, R.nBodies, indices, n, velocity, angular);
   API_END
 }
 
@@ -712,10 +728,11 @@ int avbd_batch_read_poses(avbd_batch* b, float* out) {
   Arena& A = *b->A;
   bind(A.ctx);
   const int n = int(b->bodies);  // the batch's worlds occupy bodies [0, n) in creation order
+  A.resolve();
   if (n == 0) return AVBD_OK;
   if (!A.poseStage) A.poseStage = dalloc<float4>(size_t(n) * 2);
   int blocks = grid_blocks(n, 256);
-  if (blocks > 152 * 8) blocks = 152 * 8;
+  if (blocks > device_sms() * 8) blocks = device_sms() * 8;
   k_read_poses<<<blocks, 256, 0, A.s>>>(A.B.pose, A.B.size, n, A.poseStage); note_launches(1);
   CK(cudaMemcpyAsync(out, A.poseStage, size_t(n) * 32, cudaMemcpyDeviceToHost, A.s));
   CK(cudaStreamSynchronize(A.s));
@@ -726,18 +743,11 @@ int avbd_batch_set_velocities(avbd_batch* b, const uint32_t* indices, int32_t n,
   API_BEGIN
   REQUIRE(b, "null batch");
   bind(b->A->ctx);
-  setVelocities(*b->A, 0, int(b->bodies), indices, n, velocity, angular);
-  // the worlds whose bodies got velocities wake
-  std::vector<std::pair<long long, int>> start;  // (first body, world slot) in body order
-  for (int w : b->worlds) start.emplace_back(b->A->W[w].dev.bodyOff, w);
-  std::sort(start.begin(), start.end());
-  std::vector<char> hit(start.size(), 0);
-  for (int k = 0; k < n; k++) {
-    const auto it = std::upper_bound(start.begin(), start.end(), std::make_pair((long long)indices[k], INT32_MAX));
-    hit[size_t(it - start.begin()) - 1] = 1;
-  }
-  for (size_t k = 0; k < hit.size(); k++)
-    if (hit[k]) b->A->wakeWorld(start[k].second);
+  // batch body index (the arena's body slot) -> (world, local index)
+  std::vector<std::pair<long long, int>> starts;
+  for (int w : b->worlds) starts.emplace_back((long long)b->A->W[w].dev.bodyOff, w);
+  std::sort(starts.begin(), starts.end());
+  setVelocities(*b->A, starts, b->bodies, indices, n, velocity, angular);
   API_END
 }
 

@@ -40,6 +40,7 @@ constexpr uint32_t STICK_BIT = 0x80000000u;
 constexpr uint32_t JOINT_BIT = 0x80000000u;  // constraint-list entry is a joint id
 constexpr int SHAPE_BOX = 0;
 constexpr int SHAPE_SPHERE = 1;
+constexpr int SHAPE_CAPSULE = 2;  // along local Y; size (2r, height, 2r) (src/gpu/capsuleShape.js)
 constexpr int KIND_JOINT = 0;
 constexpr int KIND_SPRING = 1;
 // Angular rows about a hinge axis (src/gpu/angularConstraints.js info types 3 and 4): a motor
@@ -114,6 +115,23 @@ struct PairPtrs {
   float4* ct;      // 4 per contact, 8 contacts per slot
 };
 
+// Control block of the tick protocol (one per arena, device memory). A tick never waits for
+// the host: its capacities are chosen before it is queued, and its gate (k_tick_gate, after the
+// constraint lists and colours, before anything that changes a world's state) checks them. A
+// tick whose pair regions or work items overflowed sets `held`; from then on every kernel that
+// would change state, in that tick and in every tick queued after it, returns at once, so the
+// worlds stay exactly as the last good tick left them. The host sees `held` later, grows the
+// capacities and queues the held ticks again (the reference's protectSolverStep, which turns the
+// solve of an overflowing step into no-ops, src/gpu/gpuSolverKernels.js:72-102, with adapt's
+// growth, src/vendor/three-avbd-lib/solver3D.ts:1515-1559; here the held steps are re-run so
+// capacities never change a result).
+struct TickCtl {
+  int held;       // 1: a tick overflowed; state-changing kernels do nothing until the host clears it
+  int ticksDone;  // ticks completed (not held), counted by k_tick_end
+  int itemsNeed;  // largest number of contact work items a tick needed
+  int waitFail;   // a bounded wait of the persistent solve gave up (an error, never expected)
+};
+
 // The active set of one tick.
 struct Tick {
   const int4* active;   // per active world, by body offset: (world, bodyPrefix, jointPrefix, -)
@@ -132,7 +150,11 @@ struct Tick {
   int maxWorlds;
   int slotStride;       // pair slots per buffer
   int bodyStride;       // colour entries per buffer
+  TickCtl* ctl;         // the arena's tick control block
 };
+
+// A held tick (TickCtl::held): the kernels that change world state return at once.
+__device__ __forceinline__ bool tick_held(const TickCtl* c) { return *(volatile const int*)&c->held != 0; }
 
 // Device counters (one block of ints, reset each tick where noted).
 struct Counters {
@@ -204,7 +226,8 @@ struct Topo {
   int* color;        // both colour buffers, 2 * bodyStride entries (see Tick::which)
   int* won;          // round scratch, per body
   unsigned char* pending;  // per body
-  int* colorBodies;  // active indices k, bucketed by colour
+  int* colorBodies;  // active indices k, bucketed by colour, ascending within a bucket
+  int* colorScan;    // colour scatter scratch: (colour, block of 256 positions) counts, scanned
   // manifold-contact work items of the dynamic bodies, bucket order (see launch_primal):
   int* itemStart;  // per bucket slot, nBodies + 1 (exclusive scan of item counts)
   int4* itemRef;   // item -> (pair slot, item code (item_code), body A, body B)
@@ -216,6 +239,11 @@ size_t scan_temp_bytes(int n);
 // exclusive scan of n ints in place; writes the total to *total (device) if non-null
 void scan_exclusive(int* data, int n, int* total, void* temp, cudaStream_t s);
 int grid_blocks(long long n, int threads);
+// Streaming multiprocessors of the current device (looked up once per device): grids of the
+// grid-stride kernels are capped at a multiple of it.
+int device_sms();
+// Looks up the per-device launch geometry (call before capturing launches into a graph).
+void prepare_launches();
 // Kernel launches issued by this library (host counter, for the benchmark's launch count).
 void note_launches(int n);
 long long launches_total();
@@ -248,8 +276,9 @@ void bvh_layout(int n, BvhLayout& L);
 size_t bvh_scratch_keys(int n);
 size_t bvh_scratch_hist(int n);
 size_t bvh_scratch_bounds(int n);
+// radixBits: digit width of the Morton-code sort (4, 6 or 8; same order for every width)
 void launch_bvh_build(const BodyPtrs& b, int bodyOff, int n, BvhPool pool, int nodeOff, const BvhLayout& L, BvhScratch sc,
-                      void* scanTemp, cudaStream_t s);
+                      void* scanTemp, int radixBits, cudaStream_t s);
 void launch_bvh_refit(const BodyPtrs& b, int bodyOff, int n, BvhPool pool, int nodeOff, const BvhLayout& L, cudaStream_t s);
 
 // solve.cu
@@ -262,12 +291,17 @@ void launch_body_warmstart(const BodyPtrs& b, const WorldDev* worlds, Tick t, cu
 void launch_adjacency(const BodyPtrs& b, JointPtrs j, PairPtrs P, Tick t, const Counters* ctr, Topo topo, int pairBudget,
                       void* scanTemp, cudaStream_t s);
 void launch_coloring(const BodyPtrs& b, const WorldDev* worlds, JointPtrs j, PairPtrs P, Tick t, Topo topo, int rounds,
-                     Counters* ctr, cudaStream_t s);
+                     Counters* ctr, void* scanTemp, cudaStream_t s);
+// scratch ints of the colour scatter for a tick of n bodies
+inline size_t color_scan_ints(size_t n) { return size_t(MAX_COLORS) * ((n + 255) / 256 + 1) + 1; }
 // Per tick, before the counter readback: per-body manifold-contact item counts, their scan and
 // the per-colour item totals. After the readback (with itemRef large enough): fill.
 void launch_items_count(PairPtrs P, Tick t, Topo topo, Counters* ctr, void* scanTemp, cudaStream_t s);
 void launch_items_fill(const BodyPtrs& b, const WorldDev* worlds, PairPtrs P, Tick t, Topo topo, const Counters* ctr,
                        cudaStream_t s);
+// The tick's gate (TickCtl): after the items count, holds the tick when a world's pair region
+// overflowed or the work items exceed itemCap.
+void launch_tick_gate(Tick t, const Counters* ctr, long long itemCap, cudaStream_t s);
 
 // Work-item code: contact index (3 bits), side (0: body A, 1: body B), whether this item runs the
 // contact's dual update (the item of the body solved last in an iteration: the other body is
@@ -280,19 +314,24 @@ __host__ __device__ __forceinline__ int item_contact(int code) { return code & 7
 __host__ __device__ __forceinline__ int item_side(int code) { return (code >> 3) & 1; }
 __host__ __device__ __forceinline__ bool item_dual_owner(int code) { return (code & 16) != 0; }
 __host__ __device__ __forceinline__ int item_iterations(int code) { return code >> 5; }
-// sleepy: some stepped world has sleeping on (rows of sleeping bodies are skipped: nobody reads them)
-void launch_primal(const BodyPtrs& b, const WorldDev* worlds, JointPtrs j, PairPtrs P, Tick t, Topo topo, const Counters* ctr,
-                   int color, int iteration, int nBodiesColor, int nItemsColor, bool sleepy, cudaStream_t s);
-// Ticks of at most this many bodies run their solve loop as one cooperative launch.
-#ifndef AVBD_COOP_SOLVE_MAX
-#define AVBD_COOP_SOLVE_MAX 131072
-#endif
-// The whole solve loop (all iterations, colours and joint duals) in one cooperative launch, for
-// ticks small enough that per-colour launches are latency-bound; same order, same bits.
-cudaError_t launch_solve_coop(const BodyPtrs& b, const WorldDev* worlds, JointPtrs j, PairPtrs P, Tick t, Topo topo, const Counters* ctr,
-                              int maxIter, int nBodies, bool sleepy, cudaStream_t s);
-// Joint duals of one iteration (contact duals run inside launch_primal, see k_primal).
-void launch_dual_joints(const BodyPtrs& b, const WorldDev* worlds, JointPtrs j, Tick t, int iteration, cudaStream_t s);
+// The solve loop of a tick (every iteration, colour and chunk, with the contact and joint duals
+// fused) in one persistent launch, chosen at run time (the autotuner's candidates):
+//   queue   tiles (iteration, colour, chunk) drained in order; a tile waits only for its own
+//           worlds' earlier stages (k_solve_queue);
+//   barrier colour by colour with a grid barrier between colours (k_solve_coop).
+// Both give the same bits. sleepy: some stepped world has sleeping on (rows of sleeping bodies
+// are skipped: nobody reads them).
+struct SolveConfig {
+  int queue = 1;                     // 1: tile queue, 0: barrier per colour
+  int blocks = 0;                    // persistent blocks (0: every resident block)
+  int waves = 2;                     // chunks per block and colour (chunk size = colour / (blocks * waves))
+  long long waitCycles = 4000000000LL;  // bound of one wait of the tile queue (SM cycles, ~2 s)
+  int probe = 0;                     // tests: every wait past the first stage runs out (see k_solve_queue)
+};
+// ints of the tile queue's scratch for a world table of maxWorlds entries
+size_t solve_queue_ints(int maxWorlds);
+cudaError_t launch_solve(const BodyPtrs& b, const WorldDev* worlds, JointPtrs j, PairPtrs P, Tick t, Topo topo, const Counters* ctr,
+                         int maxIter, int nBodies, bool sleepy, const SolveConfig& cfg, int* queueScratch, cudaStream_t s);
 void launch_velocities(const BodyPtrs& b, const WorldDev* worlds, Tick t, cudaStream_t s);
 // Contact events (FLAG_EVENTS worlds), per world: its event region, events written since the
 // last read (may pass the capacity), the capacity, and the steps it has taken.
@@ -361,11 +400,15 @@ struct SleepBufs {
 void launch_sleep(const BodyPtrs& b, const WorldDev* worlds, JointPtrs J, PairPtrs P, NoCollide nc, Tick t,
                   const Counters* ctr, int pairBudget, SleepBufs sb, int maxWorlds, cudaStream_t s);
 // wake every body of bodies [off, off + n): asleep cleared, quiet time 0
-void launch_sleep_wake(const BodyPtrs& b, int off, int n, cudaStream_t s);
+void launch_sleep_wake(const BodyPtrs& b, int off, int n, const TickCtl* ctl, cudaStream_t s);
 // Body command records of one world (sorted by body, ranges per body; see k_apply_edits), and
 // the warm-start drop of teleported bodies (sorted local indices) in its last pair region.
-void launch_apply_edits(const BodyPtrs& b, const uint32_t* rec, const int2* ranges, int nranges, int bodyOff, cudaStream_t s);
-void launch_drop_contacts(PairPtrs P, size_t base, int np, const uint32_t* tele, int ntele, int bodyOff, cudaStream_t s);
+// Both do nothing while a tick is held (ctl); the world's last pair count is read from the device
+// (*np, at most npMax).
+void launch_apply_edits(const BodyPtrs& b, const uint32_t* rec, const int2* ranges, int nranges, int bodyOff, const TickCtl* ctl,
+                        cudaStream_t s);
+void launch_drop_contacts(PairPtrs P, size_t base, const int* np, int npMax, const uint32_t* tele, int ntele, int bodyOff,
+                          const TickCtl* ctl, cudaStream_t s);
 void launch_tick_end(Tick t, cudaStream_t s);
 void launch_count_active(JointPtrs j, PairPtrs P, const int* slots, int nSlots, const int* joints, int nJoints, Counters* out,
                          cudaStream_t s);

@@ -34,6 +34,7 @@ __device__ __forceinline__ void emit(const EventBufs& ev, int w, uint32_t kind, 
 
 __global__ void k_events_begin(BodyPtrs bd, const WorldDev* __restrict__ worlds, PairPtrs P, Tick t,
                                const Counters* __restrict__ ctr, EventBufs ev) {
+  if (tick_held(t.ctl)) return;
   const int np = ctr->activePairs;
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < np; q += gridDim.x * blockDim.x) {
     const int p = t.pairs[q];
@@ -68,6 +69,7 @@ __global__ void k_events_begin(BodyPtrs bd, const WorldDev* __restrict__ worlds,
 }
 
 __global__ void k_events_end(BodyPtrs bd, const WorldDev* __restrict__ worlds, PairPtrs P, Tick t, EventBufs ev) {
+  if (tick_held(t.ctl)) return;
   for (int a0 = blockIdx.x; a0 < t.nActive; a0 += gridDim.x) {
     const int w = t.active[a0].x;
     const WorldDev& W = worlds[w];
@@ -92,6 +94,7 @@ __global__ void k_events_end(BodyPtrs bd, const WorldDev* __restrict__ worlds, P
 }
 
 __global__ void k_events_commit(BodyPtrs bd, const WorldDev* __restrict__ worlds, Tick t, EventBufs ev) {
+  if (tick_held(t.ctl)) return;
   const int stride = gridDim.x * blockDim.x;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < t.nBodies; k += stride) {
     const int i = t.bodies[k];
@@ -109,8 +112,9 @@ void launch_events(const BodyPtrs& b, const WorldDev* worlds, PairPtrs P, Tick t
                    EventBufs ev, cudaStream_t s) {
   if (t.nActive == 0) return;
   int pb = grid_blocks(pairBudget > 0 ? pairBudget : 1, 256);
-  if (pb > 152 * 8) pb = 152 * 8;
-  int wb = t.nActive < 152 * 8 ? t.nActive : 152 * 8;
+  const int cap = device_sms() * 8;
+  if (pb > cap) pb = cap;
+  int wb = t.nActive < cap ? t.nActive : cap;
   const int total = t.nBodies > t.nActive ? t.nBodies : t.nActive;
   k_events_begin<<<pb, 256, 0, s>>>(b, worlds, P, t, ctr, ev);
   k_events_end<<<wb, 256, 0, s>>>(b, worlds, P, t, ev);

@@ -161,9 +161,16 @@ __device__ Hit trace(const BodyPtrs& bd, int i, const CastQuery& q) {
   const V3 o = rotate(inv, v3(q.o) - v3(p4)), d = rotate(inv, v3(q.d));
   const float r = q.d.w;
   Hit hit;
-  if (bd.meta[i].y == SHAPE_SPHERE) {
+  const int shape = bd.meta[i].y;
+  if (shape == SHAPE_SPHERE) {
     const float radius = sz.x * 0.5f + r;
     hit = dot(o, o) <= radius * radius ? Hit{0.f, -d} : ray_sphere(o, d, V3{0.f, 0.f, 0.f}, radius);
+  } else if (shape == SHAPE_CAPSULE) {  // its segment along local Y, radius + r (shapeQueries.wgsl trace)
+    const float half = fmaxf(0.f, sz.y * 0.5f - sz.x * 0.5f);
+    const V3 a{0.f, -half, 0.f}, b{0.f, half, 0.f};
+    const float radius = sz.x * 0.5f + r;
+    const V3 delta = o - closest_on(a, b, o);
+    hit = dot(delta, delta) <= radius * radius ? Hit{0.f, -d} : ray_capsule(o, d, a, b, radius);
   } else {
     hit = ray_box(o, d, V3{sz.x * 0.5f, sz.y * 0.5f, sz.z * 0.5f}, r);
   }

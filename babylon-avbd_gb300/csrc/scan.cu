@@ -118,6 +118,17 @@ int grid_blocks(long long n, int threads) {
 #include <atomic>
 
 namespace avbd {
+static std::atomic<int> g_sms[64];
+int device_sms() {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) dev = 0;
+  int v = g_sms[dev].load(std::memory_order_relaxed);
+  if (v > 0) return v;
+  if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v < 1) v = 1;
+  g_sms[dev].store(v, std::memory_order_relaxed);
+  return v;
+}
 static std::atomic<long long> g_launches{0};
 void note_launches(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 long long launches_total() { return g_launches.load(std::memory_order_relaxed); }

@@ -91,7 +91,7 @@ struct avbd_server {
     unsigned long long bestUse = ~0ull;
     for (auto& kv : worlds) {
       const Served& w = kv.second;
-      if (w.queued > 0 || w.slot == keepSlot || !A->W[w.slot].resident) continue;
+      if (w.queued > 0 || w.slot == keepSlot || !A->W[w.slot].resident || A->W[w.slot].pinned) continue;
       if (w.lastUse < bestUse) {
         bestUse = w.lastUse;
         best = w.slot;
@@ -313,18 +313,22 @@ int avbd_server_read_poses(avbd_server* s, const int64_t* world_ids, int32_t n, 
     const Served& w = s->get(world_ids[k]);
     const WorldRec& R = A.W[w.slot];
     if (total + size_t(R.nBodies) > size_t(0x7fffffff)) throw Error(AVBD_E_CAPACITY, "too many bodies in one read");
-    if (R.resident) seg.push_back(make_int4(R.dev.bodyOff, R.nBodies, int(total), 0));
+    if (R.resident) {
+      A.flushEdits(w.slot);  // queued commands apply before a read
+      seg.push_back(make_int4(R.dev.bodyOff, R.nBodies, int(total), 0));
+    }
     else {
       seg.push_back(make_int4(0, 0, int(total), 0));
       hostRows.push_back({w.slot, total});
     }
     total += size_t(R.nBodies);
   }
+  A.resolve();
   if (total == 0) return AVBD_OK;
   s->ensurePoseBuffers(seg.size(), total);
   A.put(s->segDev, seg.data(), seg.size() * sizeof(int4));
   int blocks = grid_blocks((long long)total, 256);
-  if (blocks > 152 * 8) blocks = 152 * 8;
+  if (blocks > device_sms() * 8) blocks = device_sms() * 8;
   k_gather_poses<<<blocks, 256, 0, A.s>>>(A.B, s->segDev, int(seg.size()), int(total), s->poseDev); note_launches(1);
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(out, s->poseDev, total * 2 * sizeof(float4), cudaMemcpyDeviceToHost, A.s));

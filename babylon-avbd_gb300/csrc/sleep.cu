@@ -87,6 +87,7 @@ __device__ __forceinline__ bool sleep_edge(const BodyPtrs& bd, const WorldDev* w
 }
 
 __global__ void k_sleep_init(BodyPtrs bd, const WorldDev* __restrict__ worlds, Tick t, SleepBufs sb) {
+  if (tick_held(t.ctl)) return;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < t.nBodies; k += gridDim.x * blockDim.x) {
     const int i = t.bodies[k];
     if (!sleep_world(bd, worlds, i)) continue;
@@ -97,6 +98,7 @@ __global__ void k_sleep_init(BodyPtrs bd, const WorldDev* __restrict__ worlds, T
 
 __global__ void k_sleep_edges(BodyPtrs bd, const WorldDev* __restrict__ worlds, JointPtrs J, PairPtrs P, NoCollide nc, Tick t,
                               const Counters* __restrict__ ctr, SleepBufs sb, int mode) {
+  if (tick_held(t.ctl)) return;
   const int np = ctr->activePairs;
   const int total = t.nJoints + np + nc.n;
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += gridDim.x * blockDim.x) {
@@ -115,6 +117,7 @@ __global__ void k_sleep_edges(BodyPtrs bd, const WorldDev* __restrict__ worlds, 
 }
 
 __global__ void k_sleep_roots(BodyPtrs bd, const WorldDev* __restrict__ worlds, Tick t, SleepBufs sb) {
+  if (tick_held(t.ctl)) return;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < t.nBodies; k += gridDim.x * blockDim.x) {
     const int i = t.bodies[k];
     if (!sleep_world(bd, worlds, i)) continue;
@@ -127,6 +130,7 @@ __device__ __forceinline__ float sleep_speed(float4 v, float4 w) {
 }
 
 __global__ void k_sleep_reduce(BodyPtrs bd, const WorldDev* __restrict__ worlds, Tick t, SleepBufs sb) {
+  if (tick_held(t.ctl)) return;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < t.nBodies; k += gridDim.x * blockDim.x) {
     const int i = t.bodies[k];
     const WorldDev& W = worlds[bd.meta[i].x];
@@ -139,6 +143,7 @@ __global__ void k_sleep_reduce(BodyPtrs bd, const WorldDev* __restrict__ worlds,
 }
 
 __global__ void k_sleep_time(BodyPtrs bd, const WorldDev* __restrict__ worlds, Tick t, SleepBufs sb) {
+  if (tick_held(t.ctl)) return;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < t.nBodies; k += gridDim.x * blockDim.x) {
     const int i = t.bodies[k];
     const WorldDev& W = worlds[bd.meta[i].x];
@@ -157,6 +162,7 @@ __global__ void k_sleep_time(BodyPtrs bd, const WorldDev* __restrict__ worlds, T
 }
 
 __global__ void k_sleep_apply(BodyPtrs bd, const WorldDev* __restrict__ worlds, Tick t, SleepBufs sb) {
+  if (tick_held(t.ctl)) return;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < t.nBodies; k += gridDim.x * blockDim.x) {
     const int i = t.bodies[k];
     const int w = bd.meta[i].x;
@@ -166,7 +172,8 @@ __global__ void k_sleep_apply(BodyPtrs bd, const WorldDev* __restrict__ worlds, 
   }
 }
 
-__global__ void k_sleep_wake(BodyPtrs bd, int off, int n) {
+__global__ void k_sleep_wake(BodyPtrs bd, int off, int n, const TickCtl* ctl) {
+  if (tick_held(ctl)) return;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
     bd.sleep[off + k] &= ~SLEEP_ASLEEP;
     bd.sleepTime[off + k] = 0.f;
@@ -180,7 +187,7 @@ void launch_sleep(const BodyPtrs& b, const WorldDev* worlds, JointPtrs J, PairPt
   if (t.nBodies == 0) return;
   const int bblocks = grid_blocks(t.nBodies, 256);
   int eblocks = grid_blocks((long long)t.nJoints + pairBudget + nc.n, 256);
-  if (eblocks > 152 * 8) eblocks = 152 * 8;
+  if (eblocks > device_sms() * 8) eblocks = device_sms() * 8;
   if (eblocks < 1) eblocks = 1;
   cudaMemsetAsync(sb.wake, 0, sizeof(int) * size_t(maxWorlds), s);
   k_sleep_init<<<bblocks, 256, 0, s>>>(b, worlds, t, sb);
@@ -193,9 +200,9 @@ void launch_sleep(const BodyPtrs& b, const WorldDev* worlds, JointPtrs J, PairPt
   note_launches(7);
 }
 
-void launch_sleep_wake(const BodyPtrs& b, int off, int n, cudaStream_t s) {
+void launch_sleep_wake(const BodyPtrs& b, int off, int n, const TickCtl* ctl, cudaStream_t s) {
   if (n <= 0) return;
-  k_sleep_wake<<<grid_blocks(n, 256), 256, 0, s>>>(b, off, n);
+  k_sleep_wake<<<grid_blocks(n, 256), 256, 0, s>>>(b, off, n, ctl);
   note_launches(1);
 }
 

@@ -12,6 +12,7 @@
 import { createRequire } from "node:module";
 import { IgnoreCollision, Joint, Spring } from "../../../reference/three-avbd/src/avbd3d/ref/forces.ts";
 import { isSphere } from "../../../reference/three-avbd/src/avbd3d/shapes.ts";
+import { isCapsule } from "../../gpu/capsuleShape.js";
 import { angularConstraintOptions, initialAngularConstraint } from "../../gpu/angularConstraints.js";
 import { initialSpringMaterial, springMaterial } from "../../gpu/springMaterial.js";
 import { installNativeRuntime } from "../runtime.js";
@@ -82,7 +83,7 @@ export function packScene(scene, options = {}) {
     a.mass[s] = b.mass;
     a.friction[s] = b.friction;
     a.radius[s] = b.radius;
-    a.shape[s] = isSphere(b) ? 1 : 0;
+    a.shape[s] = isSphere(b) ? 1 : isCapsule(b) ? 2 : 0;  // AVBD_SHAPE_BOX / SPHERE / CAPSULE
     a.group[s] = b.group ?? 0xffffffff;
     a.collidesWith[s] = b.collidesWith ?? 0xffffffff;
     a.restitution[s] = b.restitution ?? 0;

@@ -60,6 +60,7 @@ def args_parse():
     p.add_argument("--cpu-sample", type=int, default=256, help="worlds timed on the CPU path")
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--full-steps", type=int, default=60, help="world_mix: steps of the configuration's whole run")
     p.add_argument("--no-plain", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--spatial-sort", choices=["on", "off", "auto"], default="auto",
@@ -375,6 +376,67 @@ def run_reference(args, dist):
     print(json.dumps(line), flush=True)
 
 
+def timed_batch(pipe, stream, worlds, warmup, steps, profile=False, sync_each=False, clocks=None):
+    """A fresh batch of `worlds`: `warmup` untimed steps, then `steps` steps queued back to back
+    (the engine's step never waits for the device) with a CUDA event on the engine's stream after
+    each; returns (per-tick ms, total ms, the batch's profile read, bodies). `profile` turns on
+    the engine's per-kernel-class events and algorithmic-byte counting (the instrumented run)."""
+    import torch
+    batch = pipe.createBatch(worlds)
+    for _ in range(warmup):
+        batch.step(1)
+    pipe.synchronize()
+    if profile:
+        batch.profile(True)
+    p0 = batch.profileRead()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+    pipe.synchronize()
+    torch.cuda.synchronize()
+    if clocks is not None:
+        clocks.__enter__()
+    ev[0].record(stream)
+    for k in range(steps):
+        batch.step(1)
+        ev[k + 1].record(stream)
+        if sync_each:
+            pipe.synchronize()
+    pipe.synchronize()
+    torch.cuda.synchronize()
+    if clocks is not None:
+        clocks.__exit__(None, None, None)
+    ticks = np.array([ev[k].elapsed_time(ev[k + 1]) for k in range(steps)])
+    total = float(ev[0].elapsed_time(ev[-1]))
+    p1 = batch.profileRead()
+    p1["launches_timed"] = p1["launches"] - p0["launches"]
+    p1["graph_replays_timed"] = p1["graph_replays"] - p0["graph_replays"]
+    p1["graph_captures_timed"] = p1["graph_captures"] - p0["graph_captures"]
+    nb = batch.bodyCount
+    batch.destroy()
+    return ticks, total, p1, nb
+
+
+def pct(x, q):
+    return round(float(np.percentile(x, q)), 3) if len(x) else None
+
+
+def parity_c0():
+    """One config-0 step from the engine's state after 75 steps against the oracle: float32 in the
+    engine's colour order (the parity bar), float64 in the same order and float64 in the
+    reference's sequential order (the reported errors)."""
+    import parity
+    from avbd_gb300 import createSolverPipeline, workloads
+    sc = workloads.box_pile_c0()
+    pipe = createSolverPipeline("gb300", device=0)
+    w = pipe.createSolver(sc)
+    rep = parity.compare_step(w, sc, 75)
+    pipe.destroy()
+    return {"workload": "box_pile_c0 step 76 from the engine's state after 75 steps", "tolerance": parity.TOL,
+            "pairs_equal": rep["pairs_equal"], "contact_counts_equal": rep["contact_counts_equal"],
+            "colors_equal": rep["colors_equal"], "fp32_same_order_err": rep["max_err_fp32"],
+            "fp64_same_order_err": rep["max_err_fp64"], "fp64_sequential_err": rep["max_err_fp64_sequential"],
+            "err": "max over positions, quaternions, velocities of |gpu - cpu| / (|cpu| + 1)"}
+
+
 def run_ours(args, dist):
     import torch
     from avbd_gb300 import createSolverPipeline
@@ -386,74 +448,63 @@ def run_ours(args, dist):
     log(f"{len(worlds)} worlds built; creating pipeline")
     pipe = createSolverPipeline("gb300", device=dev)
     stream = torch.cuda.ExternalStream(pipe.stream, device=dev)
-    batch = pipe.createBatch(worlds)
-    nb = batch.bodyCount
-    log(f"batch created ({nb} bodies); warm-up")
-    for _ in range(args.warmup):
-        batch.step(1)
-    pipe.synchronize()
-    # ---------------- timed region (device-resident; CUDA events on the engine's stream, plus the
-    # engine's per-kernel-class events for the stage split and the roofline: ~0.2 % of a step here)
+    # ---------------- timed region: the clean run (no instrumentation; ticks replay their CUDA
+    # graph), device-resident, CUDA events on the engine's stream, max over ranks
     log("timed region")
-    batch.profile(True)
-    launches0 = batch.profileRead()["launches"]
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
     dist.barrier()
-    pipe.synchronize()
-    torch.cuda.synchronize()
-    with Clocks(dev) as clk:
-        ev[0].record(stream)
-        for k in range(args.steps):
-            batch.step(1)
-            ev[k + 1].record(stream)
-        pipe.synchronize()
-        torch.cuda.synchronize()
-    ticks = np.array([ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)])
-    elapsed_ms = float(ev[0].elapsed_time(ev[-1]))
-    prof = batch.profileRead()
-    batch.profile(False)
-    launches = prof["launches"] - launches0
+    clk = Clocks(dev)
+    ticks, elapsed_ms, pclean, nb = timed_batch(pipe, stream, worlds, args.warmup, args.steps, clocks=clk)
     elapsed_ms = dist.max(elapsed_ms)
     total_bodies = dist.sum(float(nb))
     value = total_bodies * args.steps / (elapsed_ms / 1000.0)
-    # ---------------- roofline of the dominant kernel class
+    log(f"timed region done: {elapsed_ms:.1f} ms")
+    # ---------------- the same steps instrumented: per-kernel-class events and algorithmic bytes
+    iticks, iel, prof, _ = timed_batch(pipe, stream, worlds, args.warmup, args.steps, profile=True)
     peak, peak_kind = load_peaks()
-    # the solve class: the per-colour k_primal launches with the contact duals fused, plus the
-    # joint duals (k_dual_joints) of every iteration
     classes = {"solve": (prof["ms_primal"] + prof["ms_dual"], prof["bytes_primal"] + prof["bytes_dual"],
-                         "k_primal + k_dual_joints (primal and dual of every iteration)"),
+                         "k_solve_coop (every iteration's primal with the fused contact duals, and the joint duals)"),
                "collide": (prof["ms_collide"], prof["bytes_collide"], "collision kernels")}
     dom = max(classes, key=lambda k: classes[k][0])
     ms, byts, kname = classes[dom]
+    nst = max(prof["steps"], 1)
     achieved = byts / (ms / 1000.0) / 1e9 if ms > 0 else 0.0
     ratio = load_traffic().get(dom)
-    traffic = round(ratio * byts / max(prof["steps"], 1)) if ratio else None
+    traffic = round(ratio * byts / nst) if ratio else None
     roof = {"kernel": kname, "bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
             "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_kind,
-            "traffic": traffic, "algorithmic_bytes_per_step": byts / max(prof["steps"], 1),
+            "traffic": traffic, "algorithmic_bytes_per_step": byts / nst,
             "per": "step (the class's launches of one step: achieved and traffic both per step)",
-            "measured": "CUDA events around each launch on the engine's stream over the timed region",
-            "launches_per_step": (prof["primal_launches"] / max(prof["steps"], 1)) if dom == "solve" else None}
-    roof["classes"] = {k: {"ms_per_step": round(v[0] / max(prof["steps"], 1), 3),
-                           "algorithmic_gb_per_step": round(v[1] / max(prof["steps"], 1) / 1e9, 4),
+            "measured": "CUDA events around each launch on the engine's stream over the instrumented run",
+            "launches_per_step": (prof["primal_launches"] / nst) if dom == "solve" else None}
+    roof["classes"] = {k: {"ms_per_step": round(v[0] / nst, 3), "algorithmic_gb_per_step": round(v[1] / nst / 1e9, 4),
                            "achieved_gbs": round(v[1] / (v[0] / 1000.0) / 1e9, 1) if v[0] > 0 else None}
                        for k, v in classes.items()}
-    breakdown = {k: round(v[0] / max(prof["steps"], 1), 3) for k, v in classes.items()}
-    breakdown["topology"] = round(prof["ms_topology"] / max(prof["steps"], 1), 3)
-    breakdown["other"] = round(prof["ms_other"] / max(prof["steps"], 1), 3)
+    breakdown = {k: round(v[0] / nst, 3) for k, v in classes.items()}
+    breakdown["topology"] = round(prof["ms_topology"] / nst, 3)
+    breakdown["other"] = round(prof["ms_other"] / nst, 3)
+    instrumented = {"ms_per_step": round(iel / args.steps, 3), "stage_ms_per_step": breakdown,
+                    "note": "direct launches with an event pair around each kernel class and a byte-count "
+                            "kernel plus a host wait after every tick"}
+    # ---------------- the configuration's whole run (60 steps of the world mix), p50/p99 per tick
+    full = None
+    if args.workload == "world_mix" and args.full_steps > 0:
+        fticks, fel, _, _ = timed_batch(pipe, stream, worlds, 0, args.full_steps)
+        full = {"steps": args.full_steps, "value": nb * args.full_steps / (fel / 1000.0), "unit": UNIT,
+                "tick_ms": {"p50": pct(fticks, 50), "p95": pct(fticks, 95), "p99": pct(fticks, 99),
+                            "max": round(float(fticks.max()), 3)},
+                "note": "steps 1..N of fresh worlds, queued back to back, CUDA events per tick"}
+        log(f"full run done: {fel:.1f} ms")
     # ---------------- e2e through the public API with host buffers
     e2e = None
-    log(f"timed region done: {elapsed_ms:.1f} ms")
     if not args.no_e2e:
         # the same steps of the run as the device-timed region: a fresh batch of the same worlds,
         # the same warm-up (later steps of a pile carry more contacts and take longer)
-        batch.destroy()
         batch = pipe.createBatch(worlds)
         for _ in range(args.warmup):
             batch.step(1)
         pipe.synchronize()
         offs = np.cumsum([0] + batch.bodyCounts[:-1])
-        # one command per world: kick its last body (world offset + count - 1) upwards
+        # one command per world: set its last body's velocity (world offset + count - 1) upwards
         idx_host = torch.from_numpy((offs + np.array(batch.bodyCounts) - 1).astype(np.int64)).pin_memory()
         vel_host = torch.zeros((len(offs), 3), dtype=torch.float32).pin_memory()
         vel_host[:, 1] = 0.5
@@ -468,12 +519,13 @@ def run_ours(args, dist):
             batch.readPoses(poses_np)
         el = time.perf_counter() - t0
         el = dist.max(el)
+        batch.destroy()
         e2e = {"value": total_bodies * args.steps / el, "unit": UNIT,
                "h2d_bytes_per_step": int(idx_np.size * 4 + vel_np.nbytes),
                "d2h_bytes_per_step": int(poses_np.nbytes)}
-    # ---------------- plain path and CPU baseline (rank 0)
-    plain = cpu = None
     log("e2e done")
+    # ---------------- plain path (rank 0): each world in its own launch sequence
+    plain = None
     if dist.rank == 0 and not args.no_plain:
         sample = sample_worlds(worlds, args.plain_sample)
         plain_worlds = [pipe.createSolver(w) for w in sample]
@@ -490,13 +542,26 @@ def run_ours(args, dist):
         pb = sum(w.bodyCount for w in plain_worlds)
         plain = {"value": pb * psteps / el, "unit": UNIT,
                  "sample": f"{len(plain_worlds)} of {len(worlds)} worlds ({pb} bodies), each stepped in its own "
-                           f"launch sequence, {psteps} steps after {args.warmup} warm-up steps"}
+                           f"launch sequence (queued without waiting), {psteps} steps after {args.warmup} warm-up steps"}
         for w in plain_worlds:
             w.destroy()
+        # config 0 on the plain path: one 1,001-body world, 100 steps queued back to back
+        from avbd_gb300 import workloads
+        w0 = pipe.createSolver(workloads.box_pile_c0())
+        w0.step(args.warmup)
+        pipe.synchronize()
+        t0 = time.perf_counter()
+        w0.step(100)
+        pipe.synchronize()
+        plain["box_pile_c0_ms_per_step"] = round((time.perf_counter() - t0) * 10.0, 4)
+        plain["box_pile_c0_graph_replays"] = w0.profileRead()["graph_replays"]
+        w0.destroy()
         log("plain path done")
+    cpu = parity = None
     if dist.rank == 0 and not args.no_cpu:
         sample, warm = cpu_sample(args, worlds)
         cpu = cpu_baseline(sample, warm, args.steps, args.cpu_seconds)
+        parity = parity_c0()
     log("cpu baseline done")
     served = None
     if not args.no_serve and args.workload == "world_mix":
@@ -509,10 +574,12 @@ def run_ours(args, dist):
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": cfg,
-            "tick_ms": {"p50": round(float(np.percentile(ticks, 50)), 3), "p95": round(float(np.percentile(ticks, 95)), 3),
-                        "p99": round(float(np.percentile(ticks, 99)), 3)},
-            "plain_gpu": plain, "stage_ms_per_step": breakdown, "roofline": roof, "cpu_baseline": cpu,
-            "e2e": e2e, "gpu_launches": int(launches), "clocks": clk.summary(), "served": served}
+            "tick_ms": {"p50": pct(ticks, 50), "p95": pct(ticks, 95), "p99": pct(ticks, 99)},
+            "graphs": {"on": bool(pclean["graphs_on"]), "replays_timed": pclean["graph_replays_timed"],
+                       "captures_timed": pclean["graph_captures_timed"], "ticks_held": pclean["ticks_held"]},
+            "full_run": full, "instrumented": instrumented, "plain_gpu": plain, "stage_ms_per_step": breakdown,
+            "roofline": roof, "cpu_baseline": cpu, "parity": parity, "e2e": e2e,
+            "gpu_launches": int(pclean["launches_timed"]), "clocks": clk.summary(), "served": served}
     print(json.dumps(line), flush=True)
 
 

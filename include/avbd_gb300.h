@@ -33,6 +33,9 @@ typedef struct avbd_batch avbd_batch;
 /* Shapes and constraint kinds (src/native/scenes.js addBox/addSphere, addJoint/addSpring). */
 #define AVBD_SHAPE_BOX 0
 #define AVBD_SHAPE_SPHERE 1
+/* addCapsule (src/native/scenes.js:180-193, src/gpu/capsuleShape.js): along local Y, size =
+ * (2 radius, tip-to-tip height, 2 radius), bounding radius height / 2. */
+#define AVBD_SHAPE_CAPSULE 2
 #define AVBD_CONS_JOINT 0
 #define AVBD_CONS_SPRING 1
 #define AVBD_CONS_IGNORE 2
@@ -87,7 +90,7 @@ typedef struct avbd_scene_desc {
   const float* moment;           /* 3n principal moments */
   const float* friction;         /* n */
   const float* radius;           /* n bounding radius */
-  const int32_t* shape;          /* n AVBD_SHAPE_* */
+  const int32_t* shape;          /* n AVBD_SHAPE_* (sphere and capsule: the spine/radius shapes) */
   const uint32_t* group;         /* n [0xffffffff] */
   const uint32_t* collides_with; /* n [0xffffffff] */
   int32_t n_cons;
@@ -142,6 +145,20 @@ typedef struct avbd_profile {
   double bytes_primal; /* algorithmic bytes (see the engine's traffic accounting) */
   double bytes_dual;
   double bytes_collide;
+  int64_t graph_captures; /* ticks recorded into a CUDA graph (then launched) */
+  int64_t graph_replays;  /* ticks launched by replaying a recorded graph */
+  int32_t graphs_on;      /* 0 when graph capture failed on this device (ticks launch directly) */
+  int32_t ticks_held;     /* ticks held on the device for growth and run again */
+  /* The run-time autotuner's choice for the last tick's class (device, size, joints, iterations):
+   * tuned = 1 once every candidate was timed; the solve loop's schedule (1: tile queue, 0: colour
+   * barriers), chunks per block and colour, persistent blocks (0: all resident), and the digit
+   * width of the tree builds' Morton sort. */
+  int32_t tuned;
+  int32_t solve_queue;
+  int32_t solve_waves;
+  int32_t solve_blocks;
+  int32_t radix_bits;
+  int32_t pad2;
 } avbd_profile;
 
 /* ---------------------------------------------------------------- context */
@@ -183,11 +200,13 @@ int avbd_world_read_selected(avbd_world* w, const uint32_t* indices, int32_t n, 
  * stalls the frame), a serving process that has committed its device-memory budget to world state,
  * or a JavaScript binding that must not block its event loop. The staging for the indices and the
  * records lives in one fixed per-GPU device buffer of AVBD_NOALLOC_MAX_SELECTED records (about
- * 1.3 MB, held by every GPU that loads the library until the process exits). The first call on a
- * device looks that buffer up (make the first call before any stream capture). Requests with
- * n > AVBD_NOALLOC_MAX_SELECTED fail with AVBD_E_CAPACITY. Every call shares the buffer, which keeps
- * the last call's contents: calls whose work overlaps on the GPU (different threads or streams)
- * race; serialise them. Output is identical to avbd_world_read_selected. */
+ * 1.3 MB, held by every GPU that loads the library until the process exits). Every call looks that
+ * buffer's device address up (make the first call before any stream capture). Requests with
+ * n > AVBD_NOALLOC_MAX_SELECTED fail with AVBD_E_CAPACITY. A world with queued body commands
+ * (avbd_world_edit) fails with AVBD_E_STATE: applying them can allocate, so apply them first with
+ * avbd_world_flush_edits or a step. Every call shares the buffer, which keeps the last call's
+ * contents: calls whose work overlaps on the GPU (different threads or streams) race; serialise
+ * them. Output is identical to avbd_world_read_selected. */
 #define AVBD_NOALLOC_MAX_SELECTED 8192
 int avbd_world_read_selected_noalloc(avbd_world* w, const uint32_t* indices, int32_t n, int32_t poses_only, float* out);
 /* world.setPoses / setVelocities (src/native/runtime.js, scenes.d.ts:317-454); rotation or

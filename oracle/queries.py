@@ -164,6 +164,12 @@ def trace(pos, quat, size, shape, origin, direction, radius, max_distance):
     if shape == 1:
         rad = size[0] * 0.5 + radius
         hit = (0.0, _neg(d)) if _dot(o, o) <= rad * rad else ray_sphere(o, d, (0.0, 0.0, 0.0), rad)
+    elif shape == 2:  # capsule along local Y (shapeQueries.wgsl trace, shape -1)
+        half = max(0.0, size[1] * 0.5 - size[0] * 0.5)
+        a, b = (0.0, -half, 0.0), (0.0, half, 0.0)
+        rad = size[0] * 0.5 + radius
+        delta = _sub(o, _closest(a, b, o))
+        hit = (0.0, _neg(d)) if _dot(delta, delta) <= rad * rad else ray_capsule(o, d, a, b, rad)
     else:
         hit = ray_box(o, d, (size[0] * 0.5, size[1] * 0.5, size[2] * 0.5), radius)
     if hit[0] > max_distance or hit[0] < 0:

@@ -6,7 +6,7 @@ force count), shipped by the reference as
 ``reference/three-avbd/tests/fixtures/oracle3d/scene-*.json``. They are copied unchanged so
 the tests can run where the reference is not present.
 
-Usage: python tests/golden/make_fixtures.py [path-to-reference-checkout]
+Usage: python tests/golden/make_fixtures.py <path-to-reference-checkout>
 """
 import json
 import os
@@ -16,7 +16,7 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
-def main(ref_root="/root/reference"):
+def main(ref_root):
     src = os.path.join(ref_root, "reference", "three-avbd", "tests", "fixtures", "oracle3d")
     dst = os.path.join(HERE, "oracle3d")
     os.makedirs(dst, exist_ok=True)
@@ -28,4 +28,6 @@ def main(ref_root="/root/reference"):
 
 
 if __name__ == "__main__":
-    main(*sys.argv[1:])
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_fixtures.py <path-to-reference-checkout>")
+    main(sys.argv[1])

@@ -76,9 +76,13 @@ def test_edits_wait_for_the_step_and_agree_across_apis(pipe):
     w.step(10)
     before = w.readBodyState()
     w.editBodies(edits)
-    assert np.array_equal(w.readBodyState()["velocity"], before["velocity"])  # queued, not applied
-    w.flushEdits()
-    assert w.readBodyState()["position"][9][1] == 30.0
+    # a read applies the queued commands first (the reference's reads call flushEdits,
+    # src/native/solver3D.js:223-227, src/native/cpu/world.js:566-575)
+    after = w.readBodyState()
+    assert not np.array_equal(after["velocity"][5], before["velocity"][5])
+    assert after["position"][9][1] == 30.0
+    w.flushEdits()  # nothing left to apply
+    assert np.array_equal(w.readBodyState()["velocity"], after["velocity"])
     w.step(5)
     ref = w.readBodyState()
     w.destroy()
