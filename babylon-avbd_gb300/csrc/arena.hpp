@@ -429,6 +429,7 @@ class Arena {
     CK(cudaMemset(T.pending, 0, N));
     T.colorBodies = dalloc<int>(N);
     T.colorScan = dalloc<int>(color_scan_ints(N));
+    T.slotRef = dalloc<int2>(N);
     T.itemStart = dalloc<int>(N + 1);
     ctr = dalloc<Counters>(1);
     CK(cudaMemset(ctr, 0, sizeof(Counters)));
@@ -454,7 +455,7 @@ class Arena {
                     J.rB, J.stiff, J.penLin, J.penAng, J.lamLin, J.lamAng, J.C0Lin, J.C0Ang, J.restQ, J.broken, worlds,
                     which, pairN, wover, wactive, active, activeBodies, activeJoints, pairPrefix, pairCount, G.cellCount,
                     G.cellFill, G.cellBodies, G.cellKey, G.cellPos, G.pairTmp, G.bodyBucket, G.large, T.adjStart, T.adjFill, T.activeIndex, T.color, T.won,
-                    T.pending, T.colorBodies, T.colorScan, T.itemStart, T.itemRef, ctr, NC.keys, NC.jid, scanTemp, traffic,
+                    T.pending, T.colorBodies, T.colorScan, T.slotRef, T.itemStart, T.itemRef, ctr, NC.keys, NC.jid, scanTemp, traffic,
                     poseStage, P.pair, P.count, P.basis, P.ct, NS.sat, NS.boxList, NS.sphereList, NS.sphere2List, NS.ctr, activePairs,
                     T.adjList, G.bvh.node, G.bvh.parent, G.bvh.escape, G.bvh.minIdx, bsc.keys[0], bsc.keys[1], bsc.hist,
                     bsc.clusters, bsc.bounds, editRec, editRanges, editTele, io, ctl, queueScratch};
@@ -559,6 +560,7 @@ class Arena {
     CK(cudaMemset(T.pending, 0, N));
     for (int** p : {&T.activeIndex, &T.won, &T.colorBodies, &activeBodies, &G.cellBodies, &G.bodyBucket}) rescratch(*p, N);
     rescratch(T.colorScan, color_scan_ints(N));
+    rescratch(T.slotRef, N);
     rescratch(G.cellKey, N);
     rescratch(G.cellPos, N);
     rescratch(G.pairTmp, N * PAIR_TMP);
@@ -623,7 +625,7 @@ class Arena {
   size_t scratchBytes() const { return itemCap * sizeof(int4); }
   static size_t scratchReserve(long long nb) { return size_t(nb) * 512; }
   size_t footprint(long long nb, long long nj, long long slots, long long nw) const {
-    const size_t perBody = 12 * 16 + 2 * 4 + 1 + 16 * 4 + 32 + 4 * PAIR_TMP + 1;
+    const size_t perBody = 12 * 16 + 2 * 4 + 1 + 16 * 4 + 32 + 4 * PAIR_TMP + 1 + 8;
     const size_t perJoint = 8 + 10 * 16 + 4 + 4 + 8;
     const size_t perSlot = 2 * (8 + 4 + 3 * 16 + MAX_CONTACTS * 64) + 16 + 4 * 4 + 8;
     const size_t perWorld = sizeof(WorldDev) + 4 * 4 + 16 + 4 + MAX_LARGE * 4;
@@ -2207,23 +2209,28 @@ class Arena {
     cudaGraphExec_t exec = nullptr;
     long long launches = 0;
     unsigned long long use = 0;
+    char* table = nullptr;  // pinned: the tick's active table and world map, copied in by the graph itself
   };
+  std::map<std::vector<long long>, int> graphSightings;  // keys seen, for capture on the second sighting
   std::vector<GraphEntry> graphs;
   bool graphsOn = true;
   std::string graphsOff;  // why graphs were turned off
   long long graphGen = -1;
   unsigned long long graphClock = 0;
   long long graphReplays = 0, graphCaptures = 0, ticksHeld = 0;
-  long long actVersion = 0;
   std::vector<int> actUploaded;  // the active worlds whose table the device holds
 
   void clearGraphs() {
-    for (GraphEntry& g : graphs)
+    if (!graphs.empty()) cudaStreamSynchronize(s);  // replays in flight may still read the tables
+    for (GraphEntry& g : graphs) {
       if (g.exec) cudaGraphExecDestroy(g.exec);
+      if (g.table) cudaFreeHost(g.table);
+    }
     graphs.clear();
+    graphSightings.clear();
   }
-  std::vector<long long> planKey(const TickPlan& p) const {
-    std::vector<long long> k = {actVersion, p.na, p.nb, p.nj, p.maxIter, p.pairBudget, p.itemCap,
+  std::vector<long long> planKey(const TickPlan& p, const std::vector<int>& act) const {
+    std::vector<long long> k = {p.na, p.nb, p.nj, p.maxIter, p.pairBudget, p.itemCap,
                                 (p.bounce ? 1 : 0) | (p.sleeping ? 2 : 0) | (p.events ? 4 : 0) | (p.sleepy ? 8 : 0) |
                                     (p.t.triggerBits ? 16 : 0),
                                 rounds, slotCap, bodyCap, maxWorlds, solveCfg.queue, solveCfg.blocks, solveCfg.waves,
@@ -2232,7 +2239,33 @@ class Arena {
       k.push_back(tr.first);
       k.push_back(tr.second);
     }
+    k.insert(k.end(), act.begin(), act.end());
     return k;
+  }
+
+  // The tick's active table (per active world: world, first body and joint position) and the
+  // world -> active index map, as the device holds them.
+  void activeTables(const std::vector<int>& act, std::vector<int4>& table, std::vector<int>& wtab) const {
+    const int na = int(act.size());
+    table.assign(size_t(std::max(na, 1)), make_int4(0, 0, 0, 0));
+    wtab.assign(size_t(maxWorlds), -1);
+    int b0 = 0, j0 = 0;
+    for (int a = 0; a < na; a++) {
+      table[a] = make_int4(act[a], b0, j0, 0);
+      wtab[act[a]] = a;
+      b0 += W[act[a]].nBodies;
+      j0 += W[act[a]].nJoints;
+    }
+  }
+  void uploadActive(const std::vector<int>& act) {
+    if (act == actUploaded && uploadedWorlds == maxWorlds) return;
+    std::vector<int4> table;
+    std::vector<int> wtab;
+    activeTables(act, table, wtab);
+    if (!act.empty()) put(active, table.data(), sizeof(int4) * act.size());
+    put(wactive, wtab.data(), sizeof(int) * maxWorlds);
+    actUploaded = act;
+    uploadedWorlds = maxWorlds;
   }
 
   // The launch sequence of one tick (direct, or recorded into a graph by stream capture).
@@ -2290,8 +2323,11 @@ class Arena {
     CK(cudaMemcpyAsync(ctlHost, ctl, sizeof(TickCtl), cudaMemcpyDeviceToHost, s));
   }
 
-  void runTick(const TickPlan& p) {
+  // Direct launches for a launch sequence seen once; on its second sighting it is recorded into a
+  // graph (which copies its own active table in first) and replayed from then on.
+  void runTick(const TickPlan& p, const std::vector<int>& act) {
     if (prof || !graphsOn || p.tune[0] || p.tune[2]) {
+      uploadActive(act);
       launchTick(p);
       return;
     }
@@ -2299,20 +2335,37 @@ class Arena {
       clearGraphs();
       graphGen = alloc_generation();
     }
-    const std::vector<long long> key = planKey(p);
+    const std::vector<long long> key = planKey(p, act);
     GraphEntry* hit = nullptr;
     for (GraphEntry& g : graphs)
       if (g.key == key) hit = &g;
     if (!hit) {
+      if (graphSightings.size() > 256) graphSightings.clear();
+      if (++graphSightings[key] < 2) {
+        uploadActive(act);
+        launchTick(p);
+        return;
+      }
+      std::vector<int4> table;
+      std::vector<int> wtab;
+      activeTables(act, table, wtab);
+      const size_t tb = sizeof(int4) * table.size(), wb = sizeof(int) * wtab.size();
+      char* host = nullptr;
+      CK(cudaHostAlloc((void**)&host, tb + wb, cudaHostAllocDefault));
+      std::memcpy(host, table.data(), tb);
+      std::memcpy(host + tb, wtab.data(), wb);
       const long long before = launches_total();
       cudaGraph_t g = nullptr;
       CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
       try {
+        CK(cudaMemcpyAsync(active, host, tb, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(wactive, host + tb, wb, cudaMemcpyHostToDevice, s));
         launchTick(p);
       } catch (...) {
         cudaStreamEndCapture(s, &g);
         if (g) cudaGraphDestroy(g);
         cudaGetLastError();
+        cudaFreeHost(host);
         throw;
       }
       cudaError_t e = cudaStreamEndCapture(s, &g);
@@ -2323,18 +2376,22 @@ class Arena {
       note_launches(int(-n));  // recorded, not run
       if (e != cudaSuccess) {
         cudaGetLastError();
+        cudaFreeHost(host);
         graphsOn = false;
         graphsOff = std::string("graph capture failed: ") + cudaGetErrorString(e);
         std::fprintf(stderr, "avbd_gb300: %s; ticks are launched directly\n", graphsOff.c_str());
+        uploadActive(act);
         launchTick(p);
         return;
       }
-      if (graphs.size() >= 8) {
+      if (graphs.size() >= 32) {
         auto lru = std::min_element(graphs.begin(), graphs.end(), [](const GraphEntry& a, const GraphEntry& b) { return a.use < b.use; });
+        CK(cudaStreamSynchronize(s));  // a replay in flight may still read its table
         cudaGraphExecDestroy(lru->exec);
+        cudaFreeHost(lru->table);
         graphs.erase(lru);
       }
-      graphs.push_back(GraphEntry{key, x, n, 0});
+      graphs.push_back(GraphEntry{key, x, n, 0, host});
       hit = &graphs.back();
       graphCaptures++;
     } else {
@@ -2343,6 +2400,8 @@ class Arena {
     hit->use = ++graphClock;
     CK(cudaGraphLaunch(hit->exec, s));
     note_launches(int(hit->launches));
+    actUploaded = act;  // the graph copied its table in
+    uploadedWorlds = maxWorlds;
   }
 
   // Body commands and wakes queued for the tick's worlds (kernels that do nothing when held):
@@ -2416,22 +2475,6 @@ class Arena {
     }
     p.sleepy = p.sleeping;
     const int na = int(act.size());
-    if (act != actUploaded || uploadedWorlds != maxWorlds) {
-      std::vector<int4> table(size_t(std::max(na, 1)));
-      std::vector<int> wtab(size_t(maxWorlds), -1);
-      int b0 = 0, j0 = 0;
-      for (int a = 0; a < na; a++) {
-        table[a] = make_int4(act[a], b0, j0, 0);
-        wtab[act[a]] = a;
-        b0 += W[act[a]].nBodies;
-        j0 += W[act[a]].nJoints;
-      }
-      if (na) put(active, table.data(), sizeof(int4) * na);
-      put(wactive, wtab.data(), sizeof(int) * maxWorlds);
-      actUploaded = act;
-      uploadedWorlds = maxWorlds;
-      actVersion++;
-    }
     long long budget = 0;
     for (int w : act) budget += W[w].dev.pairCap;
     ensureItems(nb);
@@ -2455,7 +2498,12 @@ class Arena {
       while ((1LL << sizeLog2) < (long long)std::max(nb, 1)) sizeLog2++;
       const TuneKey key{ctx->device, sizeLog2, nj > 0 ? 1 : 0, maxIter};
       int sc = -1, rc = -1;
-      tuner.pick(key, rebuild, device_sms(), solveCfg, radixBits, sc, rc);
+      if (tuner.needsHarvest(key)) {  // every candidate issued: wait for their timings, settle
+        std::vector<cudaEvent_t> more;
+        tuner.harvest(true, more);
+        for (cudaEvent_t ev : more) pool.push_back(ev);
+      }
+      tuner.pick(key, rebuild, device_sms(), solveCfg, radixBits, sc, rc, !prof);
       p.radixBits = radixBits;
       if ((sc >= 0 || rc >= 0) && !prof) {
         if (sc >= 0) {
@@ -2490,7 +2538,7 @@ class Arena {
       W[w].which ^= 1;
       W[w].steps++;
     }
-    runTick(p);
+    runTick(p, act);
     e.done = tickEvent();
     CK(cudaEventRecord(e.done, s));
     if (prof) {  // the tick's algorithmic bytes (profiling runs only)

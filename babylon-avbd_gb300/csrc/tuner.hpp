@@ -88,11 +88,21 @@ class Tuner {
 
   // The configuration for a tick of this class; `timed` tells whether the tick should be timed
   // for the tuner (candidate index in *solveCand / *radixCand, -1 otherwise).
-  void pick(const TuneKey& key, bool rebuild, int sms, SolveConfig& solve, int& radix, int& solveCand, int& radixCand) {
+  void pick(const TuneKey& key, bool rebuild, int sms, SolveConfig& solve, int& radix, int& solveCand, int& radixCand,
+            bool measure = true) {
     solve = base;
     radix = baseRadix;
     solveCand = radixCand = -1;
     if (!enabled) return;
+    if (!measure) {  // no timing possible: the class's choices if known, else the defaults
+      TuneCache& C = TuneCache::get();
+      std::lock_guard<std::mutex> lock(C.m);
+      auto it = C.solve.find(key);
+      if (it != C.solve.end() && !solvePinned) solve = it->second;
+      auto jt = C.radix.find(key);
+      if (jt != C.radix.end() && !radixPinned) radix = jt->second;
+      return;
+    }
     TuneCache& C = TuneCache::get();
     std::lock_guard<std::mutex> lock(C.m);
     if (!solvePinned) {
@@ -167,6 +177,22 @@ class Tuner {
       settle(p.key, st);
     }
     pending.resize(keep);
+  }
+
+  // True when every candidate of the class has been issued its samples but the class is not
+  // settled yet: the caller waits for the timings (ticks run ahead of the host) before the next.
+  bool needsHarvest(const TuneKey& key) {
+    if (!enabled || pending.empty()) return false;
+    TuneCache& C = TuneCache::get();
+    std::lock_guard<std::mutex> lock(C.m);
+    auto it = states.find(key);
+    if (it == states.end()) return false;
+    const State& st = it->second;
+    const bool solveDue = !solvePinned && !C.solve.count(key) && !st.solveCands.empty() &&
+                          st.solveTurn >= (unsigned long long)(SAMPLES * st.solveCands.size());
+    const bool radixDue = !radixPinned && !C.radix.count(key) && !st.radixCands.empty() &&
+                          st.radixTurn >= (unsigned long long)st.radixCands.size();
+    return solveDue || radixDue;
   }
 
   // True once the class has its choices (nothing left to time for it).

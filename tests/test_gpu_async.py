@@ -39,7 +39,8 @@ def _dense_cluster(seed=7, n=300):
     return b.arrays()
 
 
-def test_step_returns_before_the_device_finishes(pipe):
+def test_step_returns_before_the_device_finishes(pipe, monkeypatch):
+    monkeypatch.setenv("AVBD_TUNE", "0")  # the autotuner's timed ticks launch directly
     worlds, _, _ = workloads.world_mix(256, target=130_000)
     b = pipe.createBatch(worlds)
     b.step(3)
@@ -52,7 +53,7 @@ def test_step_returns_before_the_device_finishes(pipe):
     print(f"queued in {queued * 1e3:.2f} ms, done after {total * 1e3:.2f} ms")
     assert queued < 0.5 * total
     prof = b.profileRead()
-    assert prof["graphs_on"] == 1 and prof["graph_replays"] >= 10, prof
+    assert prof["graphs_on"] == 1 and prof["graph_replays"] >= 9, prof  # recorded at its second sighting
     b.destroy()
 
 
