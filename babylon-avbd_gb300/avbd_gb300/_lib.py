@@ -78,6 +78,10 @@ SIGNATURES = [
     ("avbd_ctx_destroy", C.c_int, [C.c_void_p]),
     ("avbd_ctx_stream", C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
     ("avbd_ctx_synchronize", C.c_int, [C.c_void_p]),
+    ("avbd_ctx_fence", C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
+    ("avbd_fence_wait", C.c_int, [C.c_void_p]),
+    ("avbd_fence_query", C.c_int, [C.c_void_p, _ip]),
+    ("avbd_fence_destroy", C.c_int, [C.c_void_p]),
     ("avbd_world_create", C.c_int, [C.c_void_p, C.POINTER(SceneDesc), C.POINTER(Params), C.POINTER(C.c_void_p)]),
     ("avbd_world_destroy", C.c_int, [C.c_void_p]),
     ("avbd_world_step", C.c_int, [C.c_void_p, C.c_int32]),
@@ -109,6 +113,9 @@ SIGNATURES = [
     ("avbd_server_admit", C.c_int, [C.c_void_p, C.POINTER(SceneDesc), C.POINTER(Params), _i64p]),
     ("avbd_server_advance", C.c_int, [C.c_void_p, C.c_int64, C.c_int32, _i64p]),
     ("avbd_server_tick", C.c_int, [C.c_void_p, _ip]),
+    ("avbd_server_tick_steps", C.c_int, [C.c_void_p, C.c_int32, C.c_int32, _ip]),
+    ("avbd_server_ready", C.c_int, [C.c_void_p, _i64p, C.c_int32, C.c_int32, _ip]),
+    ("avbd_server_take_reply", C.c_int, [C.c_void_p, C.c_int64, _fp, C.c_int64, _ip]),
     ("avbd_server_completed", C.c_int, [C.c_void_p, _i64p, C.c_int32, _ip]),
     ("avbd_server_read_poses", C.c_int, [C.c_void_p, _i64p, C.c_int32, _fp]),
     ("avbd_server_read_state", C.c_int, [C.c_void_p, C.c_int64, _fp, _fp, _fp, _fp, _fp]),

@@ -238,6 +238,34 @@ def _arrays(scene) -> SceneArrays:
     raise ValueError("expected an AvbdScene3D or SceneArrays")
 
 
+class Fence:
+    """onSubmittedWorkDone as a value: ``wait()`` blocks until the device passes it (thread-safe,
+    so a worker thread may wait while the caller keeps queuing steps); ``done`` polls."""
+
+    def __init__(self, h):
+        self._h = h
+
+    def wait(self):
+        L.check(L.lib().avbd_fence_wait(self._h))
+
+    @property
+    def done(self) -> bool:
+        d = C.c_int32()
+        L.check(L.lib().avbd_fence_query(self._h, C.byref(d)))
+        return bool(d.value)
+
+    def destroy(self):
+        if self._h is not None:
+            L.check(L.lib().avbd_fence_destroy(self._h))
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+
 class SolverPipeline:
     """A device context owning worlds and batches; ``destroy()`` releases all of them."""
 
@@ -264,6 +292,13 @@ class SolverPipeline:
     def synchronize(self):
         self._live()
         L.check(L.lib().avbd_ctx_synchronize(self._h))
+
+    def fence(self) -> "Fence":
+        """A fence after the work queued so far; ``wait()`` may run on another thread."""
+        self._live()
+        h = C.c_void_p()
+        L.check(L.lib().avbd_ctx_fence(self._h, C.byref(h)))
+        return Fence(h)
 
     def createSolver(self, scene, options=None) -> "World":
         """``pipeline.createSolver(scene, options)``; options ``broadphase`` ("auto", "grid",
@@ -1253,12 +1288,38 @@ class Server:
         L.check(L.lib().avbd_server_advance(self._h, int(world), int(steps), C.byref(t)))
         return t.value
 
-    def tick(self) -> int:
-        """One step of every world with queued steps; returns how many worlds were stepped."""
+    def tick(self, maxSteps: int = 1, replies: bool = False) -> int:
+        """Up to ``maxSteps`` steps of every world with queued steps, queued on the device without
+        waiting (the same bits as that many single ticks); returns the world-steps taken. With
+        ``replies`` the poses of each world whose request a step completes are captured right
+        after that step: those tickets come from ``ready()`` and their poses from ``takeReply``."""
+        self._live()
+        if int(maxSteps) != maxSteps or maxSteps < 1:
+            raise ValueError("maxSteps must be a positive integer")
+        n = C.c_int32()
+        L.check(L.lib().avbd_server_tick_steps(self._h, int(maxSteps), int(bool(replies)), C.byref(n)))
+        return n.value
+
+    def ready(self, wait: bool = False, cap: int = 65536) -> list:
+        """Tickets whose captured replies have arrived (wait: until every queued step has run)."""
+        self._live()
+        out = np.zeros(max(int(cap), 1), dtype=np.int64)
+        n = C.c_int32()
+        done = []
+        while True:
+            L.check(L.lib().avbd_server_ready(self._h, out.ctypes.data_as(L._i64p), out.size, int(bool(wait)), C.byref(n)))
+            done.extend(int(x) for x in out[:n.value])
+            if n.value < out.size:
+                return done
+
+    def takeReply(self, ticket: int) -> np.ndarray:
+        """The captured poses of a ready ticket's world, (bodies, 8) float32; handed out once."""
         self._live()
         n = C.c_int32()
-        L.check(L.lib().avbd_server_tick(self._h, C.byref(n)))
-        return n.value
+        L.check(L.lib().avbd_server_take_reply(self._h, int(ticket), None, 0, C.byref(n)))
+        out = np.zeros((n.value, 8), dtype=np.float32)
+        L.check(L.lib().avbd_server_take_reply(self._h, int(ticket), L.fptr(out), n.value, C.byref(n)))
+        return out
 
     def completed(self, cap: int = 65536) -> list:
         self._live()

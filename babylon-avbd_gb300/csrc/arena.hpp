@@ -458,7 +458,7 @@ class Arena {
                     T.pending, T.colorBodies, T.colorScan, T.slotRef, T.itemStart, T.itemRef, ctr, NC.keys, NC.jid, scanTemp, traffic,
                     poseStage, P.pair, P.count, P.basis, P.ct, NS.sat, NS.boxList, NS.sphereList, NS.sphere2List, NS.ctr, activePairs,
                     T.adjList, G.bvh.node, G.bvh.parent, G.bvh.escape, G.bvh.minIdx, bsc.keys[0], bsc.keys[1], bsc.hist,
-                    bsc.clusters, bsc.bounds, editRec, editRanges, editTele, io, ctl, queueScratch};
+                    bsc.clusters, bsc.bounds, editRec, editRanges, editTele, io, ctl, queueScratch, replySeg};
     for (void* p : ptrs) dfree(p);
     for (WorldRec& R : W) dfree(R.evDev);
     if (ctrHost) cudaFreeHost(ctrHost);
@@ -945,6 +945,7 @@ class Arena {
     }
     std::sort(all.begin(), all.end());
     if (int(all.size()) > ncCap) {
+      CK(cudaStreamSynchronize(s));  // queued ticks still read the old arrays
       dfree(NC.keys);
       dfree(NC.jid);
       NC.keys = nullptr;
@@ -964,8 +965,9 @@ class Arena {
   }
 
   // Add a world (with rebuild = false, call rebuildNoCollide after a batch of additions).
+  // Queued ticks need not finish first: the new world's uploads go to unused ranges in stream order
+  // behind them, and growth waits for the stream before it moves any array.
   int addWorld(const avbd_scene_desc& d, const avbd_params& p, bool rebuild = true) {
-    resolve();
     validate(d, p);
     ensureRoom(d.n_bodies, jointsOf(d), initialPairCap(d.n_bodies));  // may move W: before any reference into it
     const int w = takeSlot();
@@ -1084,7 +1086,6 @@ class Arena {
     uploadWorldDev(w);
     launch_joint_prepare(B, J, R.dev.jointOff, R.dev.jointOff + R.nJoints, s);
     if (rebuild) rebuildNoCollide();
-    flush();
     return w;
   }
 
@@ -2034,11 +2035,26 @@ class Arena {
     bool built = false, wake = false;
     std::vector<uint32_t> edits;
   };
+  // Poses of some stepped worlds right after a tick, gathered on the device and copied to pinned
+  // host memory in stream order (an owner's replies to requests that the tick completes); the
+  // tags are reported (confirmedTags) once the tick is confirmed, and a held tick's gather is
+  // queued again with it.
+  struct TickReply {
+    std::vector<int4> seg;  // (first body, bodies, first row, 0), ascending rows
+    int rows = 0;
+    float4* dev = nullptr;   // 2 per row
+    float4* host = nullptr;  // pinned, 2 per row
+    std::vector<long long> tags;
+  };
   struct TickLog {
     std::vector<int> act;
     std::vector<TickPre> pre;
+    TickReply reply;
     cudaEvent_t done = nullptr;
   };
+  std::vector<long long> confirmedTags;  // tags of confirmed ticks' replies, in order
+  int4* replySeg = nullptr;
+  size_t replySegCap = 0;
   std::deque<TickLog> tickLog;  // queued ticks not yet confirmed, in queue order
   long long logBase = 0;        // TickCtl::ticksDone before the first entry of tickLog
   static constexpr size_t MAX_IN_FLIGHT = 24;
@@ -2061,7 +2077,9 @@ class Arena {
     CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     return e;
   }
-  void dropLogFront() {
+  void dropLogFront() {  // the front tick is confirmed (or the log is abandoned after an error)
+    const TickLog& f = tickLog.front();
+    confirmedTags.insert(confirmedTags.end(), f.reply.tags.begin(), f.reply.tags.end());
     if (tickLog.front().done) tickEvents.push_back(tickLog.front().done);
     tickLog.pop_front();
     logBase++;
@@ -2430,7 +2448,7 @@ class Arena {
   }
 
   // One step of the given resident worlds, queued on the arena's stream without waiting.
-  void stepWorlds(std::vector<int> act) {
+  void stepWorlds(std::vector<int> act, TickReply* reply = nullptr) {
     std::sort(act.begin(), act.end(), [&](int a, int b) { return W[a].dev.bodyOff < W[b].dev.bodyOff; });
     act.erase(std::unique(act.begin(), act.end()), act.end());
     for (int w : act)
@@ -2453,6 +2471,7 @@ class Arena {
       R.wakePending = false;
       e.pre.push_back(std::move(pr));
     }
+    if (reply) e.reply = std::move(*reply);
     tickLog.push_back(std::move(e));
     queueTick(tickLog.back());
   }
@@ -2539,6 +2558,15 @@ class Arena {
       W[w].steps++;
     }
     runTick(p, act);
+    if (e.reply.rows > 0) {  // the tick's replies: gather, then copy to the owner's pinned block
+      if (e.reply.seg.size() > replySegCap) {
+        replySegCap = e.reply.seg.size() + e.reply.seg.size() / 2 + 64;
+        rescratch(replySeg, replySegCap);
+      }
+      put(replySeg, e.reply.seg.data(), e.reply.seg.size() * sizeof(int4));
+      launch_gather_poses(B, replySeg, int(e.reply.seg.size()), e.reply.rows, e.reply.dev, ctl, s);
+      CK(cudaMemcpyAsync(e.reply.host, e.reply.dev, size_t(e.reply.rows) * 2 * sizeof(float4), cudaMemcpyDeviceToHost, s));
+    }
     e.done = tickEvent();
     CK(cudaEventRecord(e.done, s));
     if (prof) {  // the tick's algorithmic bytes (profiling runs only)

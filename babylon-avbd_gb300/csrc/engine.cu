@@ -208,6 +208,54 @@ int avbd_ctx_synchronize(avbd_ctx* ctx) {
   API_END
 }
 
+struct avbd_fence {
+  int device = 0;
+  cudaEvent_t ev = nullptr;
+};
+
+int avbd_ctx_fence(avbd_ctx* ctx, avbd_fence** out) {
+  API_BEGIN
+  REQUIRE(ctx && out, "null argument");
+  bind(ctx);
+  auto* f = new avbd_fence;
+  f->device = ctx->device;
+  if (cudaEventCreateWithFlags(&f->ev, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventRecord(f->ev, ctx->stream) != cudaSuccess) {
+    if (f->ev) cudaEventDestroy(f->ev);
+    delete f;
+    throw avbd::Error(AVBD_E_CUDA, "cannot record a fence");
+  }
+  *out = f;
+  API_END
+}
+
+int avbd_fence_wait(avbd_fence* f) {
+  API_BEGIN
+  REQUIRE(f, "null fence");
+  CK(cudaSetDevice(f->device));
+  CK(cudaEventSynchronize(f->ev));
+  API_END
+}
+
+int avbd_fence_query(avbd_fence* f, int32_t* done) {
+  API_BEGIN
+  REQUIRE(f && done, "null argument");
+  CK(cudaSetDevice(f->device));
+  const cudaError_t e = cudaEventQuery(f->ev);
+  if (e != cudaSuccess && e != cudaErrorNotReady) CK(e);
+  *done = e == cudaSuccess;
+  API_END
+}
+
+int avbd_fence_destroy(avbd_fence* f) {
+  API_BEGIN
+  if (!f) return AVBD_OK;
+  CK(cudaSetDevice(f->device));
+  cudaEventDestroy(f->ev);
+  delete f;
+  API_END
+}
+
 int avbd_ctx_destroy(avbd_ctx* ctx) {
   API_BEGIN
   if (!ctx) return AVBD_OK;

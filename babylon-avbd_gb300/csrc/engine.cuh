@@ -411,6 +411,9 @@ void launch_apply_edits(const BodyPtrs& b, const uint32_t* rec, const int2* rang
 void launch_drop_contacts(PairPtrs P, size_t base, const int* np, int npMax, const uint32_t* tele, int ntele, int bodyOff,
                           const TickCtl* ctl, cudaStream_t s);
 void launch_tick_end(Tick t, cudaStream_t s);
+// Poses of listed worlds into rows of `out` (2 float4 per body); seg = (first body, bodies, first
+// row, -) ascending by row. With ctl, nothing is written while a tick is held.
+void launch_gather_poses(const BodyPtrs& b, const int4* seg, int nseg, int total, float4* out, const TickCtl* ctl, cudaStream_t s);
 void launch_count_active(JointPtrs j, PairPtrs P, const int* slots, int nSlots, const int* joints, int nJoints, Counters* out,
                          cudaStream_t s);
 

@@ -32,26 +32,6 @@ struct Served {
   std::deque<Ticket> tickets;
 };
 
-// Poses of listed resident worlds: seg = (first body, bodies, first output body, -), ascending
-// in the output position.
-__global__ void k_gather_poses(BodyPtrs bd, const int4* __restrict__ seg, int nseg, int total, float4* __restrict__ out) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
-    int a = 0, b = nseg;
-    while (b - a > 1) {
-      const int m = (a + b) >> 1;
-      if (seg[m].z <= i) a = m;
-      else b = m;
-    }
-    const int4 e = seg[a];
-    const int k = i - e.z;
-    if (k >= e.y) continue;  // output rows of evicted worlds (filled on the host)
-    const int body = e.x + k;
-    const float4 p = bd.pos(body);
-    out[2 * size_t(i)] = make_float4(p.x, p.y, p.z, bd.size[body].w);
-    out[2 * size_t(i) + 1] = bd.rot(body);
-  }
-}
-
 }  // namespace
 
 struct avbd_server {
@@ -69,12 +49,42 @@ struct avbd_server {
   size_t segCap = 0;
   float4* poseDev = nullptr;
   size_t poseCap = 0;
+  // Replies captured with the ticks (tick_steps with replies): rows (2 float4 per body) of one
+  // device and one pinned buffer, a row range per ticket until the reply is taken.
+  float4* replyDev = nullptr;
+  float4* replyHost = nullptr;
+  int replyCap = 0;
+  RangeAlloc replyRows;
+  std::unordered_map<int64_t, std::pair<int, int>> replyOf;  // ticket -> (first row, rows)
+  std::deque<int64_t> ready;                                // tickets whose reply has arrived
+
+  // Rows for a reply: grows both buffers (waiting for every queued tick first, whose replies
+  // point into the old ones) when the free ranges cannot place it.
+  int replyAlloc(int rows) {
+    int at = replyRows.alloc(rows);
+    if (at >= 0) return at;
+    A->resolve();
+    const int cap = std::max(replyCap + rows + 4096, replyCap * 2);
+    float4* d = dalloc<float4>(2 * size_t(cap));
+    float4* h = nullptr;
+    CK(cudaHostAlloc((void**)&h, 2 * size_t(cap) * sizeof(float4), cudaHostAllocDefault));
+    if (replyHost) std::memcpy(h, replyHost, 2 * size_t(replyCap) * sizeof(float4));
+    if (replyHost) cudaFreeHost(replyHost);
+    dfree(replyDev);
+    replyDev = d;
+    replyHost = h;
+    if (replyCap == 0) replyRows.init(cap);
+    else replyRows.grow(cap);
+    replyCap = cap;
+    notePeak();
+    return replyRows.alloc(rows);
+  }
 
   // Bytes held against the budget: the arena's arrays, its work-item scratch (at least the
   // reserve for its body capacity) and the pose-read buffers.
   size_t accounted(long long nb, long long nj, long long slots, long long nw) const {
     return A->footprint(nb, nj, slots, nw) + std::max(A->scratchBytes(), Arena::scratchReserve(nb)) + segCap * sizeof(int4) +
-           poseCap * 2 * sizeof(float4);
+           poseCap * 2 * sizeof(float4) + size_t(replyCap) * 2 * sizeof(float4);
   }
   size_t deviceBytes() const { return accounted(A->bodyCap, A->jointCap, A->slotCap, A->maxWorlds); }
   void notePeak() { peak = std::max(peak, deviceBytes()); }
@@ -192,6 +202,8 @@ int avbd_server_destroy(avbd_server* s) {
   delete s->A;
   dfree(s->segDev);
   dfree(s->poseDev);
+  dfree(s->replyDev);
+  if (s->replyHost) cudaFreeHost(s->replyHost);
   delete s;
   API_END
 }
@@ -239,9 +251,10 @@ int avbd_server_advance(avbd_server* s, int64_t world_id, int32_t steps, int64_t
   API_END
 }
 
-int avbd_server_tick(avbd_server* s, int32_t* n_stepped) {
+int avbd_server_tick_steps(avbd_server* s, int32_t max_steps, int32_t replies, int32_t* n_stepped) {
   API_BEGIN
   REQUIRE(s, "null server");
+  REQUIRE(max_steps >= 1, "max_steps must be positive");
   bind(s->ctx);
   Arena& A = *s->A;
   s->clock++;
@@ -258,32 +271,103 @@ int avbd_server_tick(avbd_server* s, int32_t* n_stepped) {
     if (!s->makeRoom(R.nBodies, R.nJoints, A.restoreSlots(w.slot), w.slot, false)) break;
     A.restore(w.slot);
   }
-  std::vector<int> act;
-  std::vector<int64_t> ids;
-  for (int64_t id : s->busy) {
-    const Served& w = s->worlds.at(id);
-    if (A.W[w.slot].resident) {
-      act.push_back(w.slot);
-      ids.push_back(id);
+  int32_t stepped = 0;
+  for (int step = 0; step < max_steps; step++) {
+    std::vector<int> act;
+    std::vector<int64_t> ids;
+    for (int64_t id : s->busy) {
+      const Served& w = s->worlds.at(id);
+      if (A.W[w.slot].resident) {
+        act.push_back(w.slot);
+        ids.push_back(id);
+      }
     }
-  }
-  if (!act.empty()) A.stepWorlds(act);
-  for (int64_t id : ids) {
-    Served& w = s->worlds.at(id);
-    w.queued--;
-    w.done++;
-    w.lastUse = s->clock;
-    s->bodySteps += w.nBodies;
-    while (!w.tickets.empty() && w.tickets.front().target <= w.done) {
-      s->completed.push_back(w.tickets.front().id);
-      s->completedCount++;
-      w.tickets.pop_front();
+    if (act.empty()) break;
+    // the tickets this step completes, and (with replies) their worlds' poses after it
+    Arena::TickReply reply;
+    std::vector<std::pair<int64_t, int64_t>> finishing;  // (world id, ticket)
+    for (int64_t id : ids) {
+      const Served& w = s->worlds.at(id);
+      for (const Ticket& t : w.tickets) {
+        if (t.target > w.done + 1) break;
+        finishing.push_back({id, t.id});
+      }
     }
-    if (w.queued == 0) s->busy.erase(id);
+    if (replies && !finishing.empty()) {
+      int rows = 0;
+      for (auto& f : finishing) rows += s->worlds.at(f.first).nBodies;
+      const int at = s->replyAlloc(rows);
+      reply.rows = rows;
+      reply.dev = s->replyDev + 2 * size_t(at);
+      reply.host = s->replyHost + 2 * size_t(at);
+      int row = 0;
+      for (auto& f : finishing) {
+        const Served& w = s->worlds.at(f.first);
+        reply.seg.push_back(make_int4(A.W[w.slot].dev.bodyOff, w.nBodies, row, 0));
+        reply.tags.push_back(f.second);
+        s->replyOf[f.second] = {at + row, w.nBodies};
+        row += w.nBodies;
+      }
+    }
+    A.stepWorlds(act, reply.rows > 0 ? &reply : nullptr);
+    for (int64_t id : ids) {
+      Served& w = s->worlds.at(id);
+      w.queued--;
+      w.done++;
+      w.lastUse = s->clock;
+      s->bodySteps += w.nBodies;
+      while (!w.tickets.empty() && w.tickets.front().target <= w.done) {
+        if (!replies) {  // with replies a ticket completes once its tick is confirmed (avbd_server_ready)
+          s->completed.push_back(w.tickets.front().id);
+          s->completedCount++;
+        }
+        w.tickets.pop_front();
+      }
+      if (w.queued == 0) s->busy.erase(id);
+    }
+    stepped += int32_t(act.size());
+    s->ticks++;
   }
-  s->ticks++;
   s->notePeak();
-  if (n_stepped) *n_stepped = int32_t(act.size());
+  if (n_stepped) *n_stepped = stepped;
+  API_END
+}
+
+int avbd_server_tick(avbd_server* s, int32_t* n_stepped) { return avbd_server_tick_steps(s, 1, 0, n_stepped); }
+
+int avbd_server_ready(avbd_server* s, int64_t* tickets, int32_t cap, int32_t wait, int32_t* n) {
+  API_BEGIN
+  REQUIRE(s && n && (cap == 0 || tickets), "null argument");
+  REQUIRE(cap >= 0, "negative capacity");
+  bind(s->ctx);
+  Arena& A = *s->A;
+  if (wait) A.resolve();
+  else A.trimLog();
+  for (long long t : A.confirmedTags) {
+    s->ready.push_back(t);
+    s->completedCount++;
+  }
+  A.confirmedTags.clear();
+  int k = 0;
+  while (k < cap && !s->ready.empty()) {
+    tickets[k++] = s->ready.front();
+    s->ready.pop_front();
+  }
+  *n = k;
+  API_END
+}
+
+int avbd_server_take_reply(avbd_server* s, int64_t ticket, float* out, int64_t cap_bodies, int32_t* n_bodies) {
+  API_BEGIN
+  REQUIRE(s && n_bodies, "null argument");
+  auto it = s->replyOf.find(ticket);
+  REQUIRE(it != s->replyOf.end(), "no reply for this ticket (not captured, or already taken)");
+  const int first = it->second.first, rows = it->second.second;
+  *n_bodies = rows;
+  if (!out || cap_bodies < rows) return AVBD_OK;  // size query
+  std::memcpy(out, s->replyHost + 2 * size_t(first), size_t(rows) * 2 * sizeof(float4));
+  s->replyRows.release(first, rows);
+  s->replyOf.erase(it);
   API_END
 }
 
@@ -329,7 +413,7 @@ int avbd_server_read_poses(avbd_server* s, const int64_t* world_ids, int32_t n, 
   A.put(s->segDev, seg.data(), seg.size() * sizeof(int4));
   int blocks = grid_blocks((long long)total, 256);
   if (blocks > device_sms() * 8) blocks = device_sms() * 8;
-  k_gather_poses<<<blocks, 256, 0, A.s>>>(A.B, s->segDev, int(seg.size()), int(total), s->poseDev); note_launches(1);
+  launch_gather_poses(A.B, s->segDev, int(seg.size()), int(total), s->poseDev, nullptr, A.s);
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(out, s->poseDev, total * 2 * sizeof(float4), cudaMemcpyDeviceToHost, A.s));
   A.flush();

@@ -10,6 +10,7 @@
 
 #include <cstdint>
 #include <cstring>
+#include <string>
 #include <vector>
 
 #include "avbd_gb300.h"
@@ -583,12 +584,159 @@ napi_value ServerStats(napi_env env, napi_callback_info info) {
   Set(env, obj, "peakDeviceBytes", Num(env, double(st.peak_device_bytes)));
   Set(env, obj, "liveWorlds", Num(env, double(st.live_worlds)));
   Set(env, obj, "evictedWorlds", Num(env, double(st.evicted_worlds)));
+  Set(env, obj, "pendingWorlds", Num(env, double(st.pending_worlds)));
   Set(env, obj, "admitted", Num(env, double(st.admitted)));
   Set(env, obj, "rejected", Num(env, double(st.rejected)));
   Set(env, obj, "evictions", Num(env, double(st.evictions)));
   Set(env, obj, "restores", Num(env, double(st.restores)));
   Set(env, obj, "bodySteps", Num(env, double(st.body_steps)));
   return obj;
+}
+
+napi_value TickSteps(napi_env env, napi_callback_info info) {  // (s, maxSteps, replies) -> steps taken
+  SERVER_ARG(3);
+  bool replies = false;
+  napi_get_value_bool(env, argv[2], &replies);
+  int32_t n = 0;
+  CALL(avbd_server_tick_steps(s, Int(env, argv[1]), replies ? 1 : 0, &n));
+  return Num(env, n);
+}
+
+// Every reply that has arrived, taken out of the server: [{ticket, poses: Float32Array}, ...].
+// Main thread only. Returns nullptr with *status set when a call fails.
+napi_value TakeReplies(napi_env env, avbd_server* s, int* status) {
+  std::vector<int64_t> tickets;
+  int64_t t[1024];
+  for (int32_t n = 1024; n == 1024;) {
+    if ((*status = avbd_server_ready(s, t, 1024, 0, &n)) != AVBD_OK) return nullptr;
+    tickets.insert(tickets.end(), t, t + n);
+  }
+  napi_value arr;
+  napi_create_array_with_length(env, tickets.size(), &arr);
+  for (size_t k = 0; k < tickets.size(); k++) {
+    int32_t rows = 0;
+    if ((*status = avbd_server_take_reply(s, tickets[k], nullptr, 0, &rows)) != AVBD_OK) return nullptr;
+    float* out;
+    napi_value poses = Float32(env, size_t(rows) * 8, &out);
+    if ((*status = avbd_server_take_reply(s, tickets[k], out, rows, &rows)) != AVBD_OK) return nullptr;
+    napi_value item;
+    napi_create_object(env, &item);
+    Set(env, item, "ticket", Num(env, double(tickets[k])));
+    Set(env, item, "poses", poses);
+    napi_set_element(env, arr, uint32_t(k), item);
+  }
+  return arr;
+}
+napi_value Ready(napi_env env, napi_callback_info info) {  // (s) -> [{ticket, poses}] without waiting
+  SERVER_ARG(1);
+  int status = AVBD_OK;
+  napi_value arr = TakeReplies(env, s, &status);
+  if (status != AVBD_OK) return ThrowLast(env);
+  return arr;
+}
+
+// ---------------------------------------------------------------- asynchronous serving
+// The Node event loop must not block on the device. A worker thread of libuv waits on a fence
+// (avbd_fence_wait touches nothing but the fence, the one thread-safe entry point); the completion
+// then runs on the main thread, where every other library call is made, and finds the work done.
+struct FenceWork {
+  avbd_server* server = nullptr;
+  avbd_fence* fence = nullptr;
+  napi_deferred deferred = nullptr;
+  napi_async_work work = nullptr;
+  int status = AVBD_OK;
+  std::string error;
+  int32_t stepped = 0;         // tickAsync: steps queued by the tick
+  bool read = false;           // readPosesAsync: the worlds to read and their total bodies
+  std::vector<int64_t> ids;
+  size_t bodies = 0;
+};
+
+void FenceExecute(napi_env, void* data) {  // worker thread
+  auto* f = static_cast<FenceWork*>(data);
+  if ((f->status = avbd_fence_wait(f->fence)) != AVBD_OK) f->error = avbd_last_error();
+}
+
+void FenceComplete(napi_env env, napi_status, void* data) {  // main thread
+  auto* f = static_cast<FenceWork*>(data);
+  avbd_fence_destroy(f->fence);
+  napi_value result = nullptr;
+  if (f->status == AVBD_OK) {
+    if (f->read) {
+      float* out;
+      result = Float32(env, f->bodies * 8, &out);
+      f->status = avbd_server_read_poses(f->server, f->ids.data(), int32_t(f->ids.size()), out);
+    } else {
+      napi_value replies = TakeReplies(env, f->server, &f->status);
+      napi_create_object(env, &result);
+      Set(env, result, "stepped", Num(env, f->stepped));
+      if (replies) Set(env, result, "replies", replies);
+    }
+    if (f->status != AVBD_OK) f->error = avbd_last_error();
+  }
+  if (f->status == AVBD_OK) {
+    napi_resolve_deferred(env, f->deferred, result);
+  } else {
+    napi_value msg, err;
+    napi_create_string_utf8(env, f->error.c_str(), NAPI_AUTO_LENGTH, &msg);
+    napi_create_error(env, nullptr, msg, &err);
+    napi_reject_deferred(env, f->deferred, err);
+  }
+  napi_delete_async_work(env, f->work);
+  delete f;
+}
+
+// Queue the fence wait of f on a libuv worker; returns the promise.
+napi_value QueueFence(napi_env env, avbd_ctx* ctx, FenceWork* f) {
+  napi_value promise, name;
+  if (avbd_ctx_fence(ctx, &f->fence) != AVBD_OK) {
+    delete f;
+    return ThrowLast(env);
+  }
+  napi_create_promise(env, &f->deferred, &promise);
+  napi_create_string_utf8(env, "avbd_gb300.fence", NAPI_AUTO_LENGTH, &name);
+  napi_create_async_work(env, nullptr, name, FenceExecute, FenceComplete, f, &f->work);
+  napi_queue_async_work(env, f->work);
+  return promise;
+}
+
+// (ctx, s, maxSteps) -> Promise<{stepped, replies: [{ticket, poses}]}>: one multi-step tick with
+// captured replies, queued without waiting; the promise settles once the device has run it (and
+// carries every reply that arrived by then). The caller may queue further ticks, admissions and
+// edits meanwhile: tick after tick stays in flight, as in avbd_server_tick_steps.
+napi_value TickAsync(napi_env env, napi_callback_info info) {
+  napi_value argv[3];
+  if (!Args(env, info, argv, 3)) return nullptr;
+  auto* ctx = External<avbd_ctx>(env, argv[0]);
+  auto* s = External<avbd_server>(env, argv[1]);
+  if (!ctx || !s) return nullptr;
+  auto* f = new FenceWork;
+  f->server = s;
+  if (avbd_server_tick_steps(s, Int(env, argv[2]), 1, &f->stepped) != AVBD_OK) {
+    delete f;
+    return ThrowLast(env);
+  }
+  return QueueFence(env, ctx, f);
+}
+
+// (ctx, s, Float64Array ids, bodies) -> Promise<Float32Array>: the listed worlds' poses, read once
+// the device has run every tick queued before the call (steps queued after it may be included).
+napi_value ReadPosesAsync(napi_env env, napi_callback_info info) {
+  napi_value argv[4];
+  if (!Args(env, info, argv, 4)) return nullptr;
+  auto* ctx = External<avbd_ctx>(env, argv[0]);
+  auto* s = External<avbd_server>(env, argv[1]);
+  if (!ctx || !s) return nullptr;
+  const double* ids;
+  size_t n;
+  if (!Typed(env, argv[2], &ids, &n)) return nullptr;
+  auto* f = new FenceWork;
+  f->server = s;
+  f->read = true;
+  f->ids.assign(n, 0);
+  for (size_t k = 0; k < n; k++) f->ids[k] = int64_t(ids[k]);
+  f->bodies = size_t(Int(env, argv[3]));
+  return QueueFence(env, ctx, f);
 }
 
 napi_value Init(napi_env env, napi_value exports) {
@@ -609,7 +757,8 @@ napi_value Init(napi_env env, napi_value exports) {
              {"createServer", CreateServer},   {"destroyServer", DestroyServer},   {"admit", Admit},
              {"advance", Advance},             {"tick", Tick},                     {"completed", Completed},
              {"serverReadPoses", ServerReadPoses}, {"serverEdit", ServerEdit},     {"evict", Evict},
-             {"release", Release},             {"serverStats", ServerStats}};
+             {"release", Release},             {"serverStats", ServerStats},       {"tickSteps", TickSteps},
+             {"ready", Ready},                 {"tickAsync", TickAsync},           {"readPosesAsync", ReadPosesAsync}};
   for (const auto& f : fns) {
     napi_value v;
     napi_create_function(env, f.name, NAPI_AUTO_LENGTH, f.fn, nullptr, &v);

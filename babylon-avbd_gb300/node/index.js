@@ -386,10 +386,130 @@ class Gb300World {
   }
 }
 
+/** A request loop over the engine's world server (no counterpart in the reference, which creates
+ * one solver per world). advance(id, steps) returns a promise of the world's poses after those
+ * steps, 8 floats per body (position, friction, quaternion) in the scene's creation order.
+ * Ticks are queued back to back, at most `depth` in flight on the device; each steps every world
+ * with queued steps by up to `maxStepsPerTick` steps and captures the reply of every request it
+ * completes. Admissions, edits and new requests made while ticks run join the next tick; nothing
+ * here waits for the device on the event loop (the addon waits on a libuv worker). */
+export class Gb300Server {
+  constructor(ctx, { budgetBytes, initialBodies, initialWorlds, maxStepsPerTick = 16, depth = 2 } = {}) {
+    this.ctx = ctx;
+    this.handle = addon.createServer(ctx, budgetBytes, initialBodies, initialWorlds);
+    this.maxSteps = maxStepsPerTick;
+    this.depth = depth;
+    this.orders = new Map();   // world id -> slot of each creation index
+    this.waiting = new Map();  // ticket -> {id, resolve, reject}
+    this.inFlight = 0;
+    this.scheduled = false;
+    this.destroyed = false;
+  }
+  assertLive() {
+    if (this.destroyed) throw Error("The server has been destroyed");
+  }
+  /** Admit a scene (createSolver under the server's device-memory budget); returns the world id.
+   * Throws when the world cannot fit even after evicting every idle world. */
+  admit(scene, solverOptions = {}) {
+    this.assertLive();
+    const packed = packScene(scene, solverOptions);
+    const id = addon.admit(this.handle, packed.arrays, packed.params);
+    const slots = new Int32Array(packed.order.length);
+    packed.order.forEach((i, s) => (slots[i] = s));
+    this.orders.set(id, slots);
+    scene.created = true;
+    return id;
+  }
+  /** Queue `steps` steps of a world; resolves with its poses after them. */
+  advance(id, steps) {
+    this.assertLive();
+    const ticket = addon.advance(this.handle, id, steps);
+    if (steps === 0) return this.readPoses([id]);
+    return new Promise((resolve, reject) => {
+      this.waiting.set(ticket, { id, resolve, reject });
+      this.schedule();
+    });
+  }
+  /** Poses of the listed worlds once the ticks queued so far have run, world after world. */
+  async readPoses(ids) {
+    this.assertLive();
+    const bodies = ids.reduce((n, id) => n + this.orders.get(id).length, 0);
+    const poses = await addon.readPosesAsync(this.ctx, this.handle, Float64Array.from(ids), bodies);
+    let at = 0;
+    const out = new Float32Array(poses.length);
+    for (const id of ids) {
+      const slots = this.orders.get(id);
+      out.set(this.creationOrder(poses.subarray(8 * at, 8 * (at + slots.length)), slots), 8 * at);
+      at += slots.length;
+    }
+    return out;
+  }
+  creationOrder(poses, slots) {
+    const out = new Float32Array(poses.length);
+    for (let i = 0; i < slots.length; i++) out.set(poses.subarray(8 * slots[i], 8 * slots[i] + 8), 8 * i);
+    return out;
+  }
+  edit(id, records) {
+    this.assertLive();
+    addon.serverEdit(this.handle, id, records);
+  }
+  evict(id) {
+    this.assertLive();
+    addon.evict(this.handle, id);
+  }
+  release(id) {
+    this.assertLive();
+    addon.release(this.handle, id);
+    this.orders.delete(id);
+  }
+  stats() {
+    return addon.serverStats(this.handle);
+  }
+  schedule() {
+    if (this.scheduled || this.destroyed) return;
+    this.scheduled = true;
+    setImmediate(() => {
+      this.scheduled = false;
+      this.pump();
+    });
+  }
+  pump() {
+    while (!this.destroyed && this.inFlight < this.depth && addon.serverStats(this.handle).pendingWorlds > 0) {
+      this.inFlight++;
+      addon.tickAsync(this.ctx, this.handle, this.maxSteps).then(
+        ({ replies }) => {
+          this.inFlight--;
+          for (const { ticket, poses } of replies ?? []) {
+            const req = this.waiting.get(ticket);
+            if (!req) continue;
+            this.waiting.delete(ticket);
+            req.resolve(this.creationOrder(poses, this.orders.get(req.id)));
+          }
+          this.schedule();
+        },
+        (err) => {
+          this.inFlight--;
+          for (const req of this.waiting.values()) req.reject(err);
+          this.waiting.clear();
+        },
+      );
+    }
+  }
+  destroy() {
+    if (this.destroyed) return;
+    this.destroyed = true;
+    for (const req of this.waiting.values()) req.reject(Error("The server has been destroyed"));
+    this.waiting.clear();
+    addon.synchronize(this.ctx);
+    addon.destroyServer(this.handle);
+  }
+}
+
 /** createSolverPipeline({backend: "gb300", deviceIndex}) */
 export function createGb300Pipeline(options = {}) {
   const ctx = addon.createContext(options.deviceIndex ?? 0);
   const worlds = new Set();
+  const servers = new Set();
   return {
     backend: "gb300",
     createSolver(scene, solverOptions = {}) {
@@ -398,9 +518,16 @@ export function createGb300Pipeline(options = {}) {
       worlds.add(w);
       return w;
     },
+    createServer(serverOptions = {}) {
+      const server = new Gb300Server(ctx, serverOptions);
+      servers.add(server);
+      return server;
+    },
     destroy() {
       for (const w of worlds) w.destroy();
       worlds.clear();
+      for (const s of servers) s.destroy();
+      servers.clear();
       addon.destroyContext(ctx);
     },
   };

@@ -177,6 +177,18 @@ int avbd_ctx_stream(avbd_ctx* ctx, void** stream);
 /* Wait until all queued work of the context has finished (the reference's
  * device.queue.onSubmittedWorkDone). */
 int avbd_ctx_synchronize(avbd_ctx* ctx);
+/* A fence after the work queued so far on the context's stream: onSubmittedWorkDone as a value
+ * that another thread can wait on. avbd_fence_wait and avbd_fence_query touch only the fence, so
+ * a host binding's worker thread may wait on it while the calling thread keeps queuing work (the
+ * Node addon's asynchronous reads: wait on a worker, then read on the main thread, which finds the
+ * work done). Every other entry point stays single-threaded per context. */
+typedef struct avbd_fence avbd_fence;
+int avbd_ctx_fence(avbd_ctx* ctx, avbd_fence** out);
+/* Block the calling thread until the device has passed the fence. Thread-safe. */
+int avbd_fence_wait(avbd_fence* fence);
+/* *done = 1 when the device has passed the fence, else 0. Thread-safe. */
+int avbd_fence_query(avbd_fence* fence, int32_t* done);
+int avbd_fence_destroy(avbd_fence* fence);
 
 /* ---------------------------------------------------------------- plain worlds */
 
@@ -420,6 +432,21 @@ int avbd_server_advance(avbd_server* s, int64_t world_id, int32_t steps, int64_t
 /* One step of every world with queued steps (evicted ones are restored first, room
  * permitting). *n_stepped = worlds stepped (may be 0). */
 int avbd_server_tick(avbd_server* s, int32_t* n_stepped);
+/* Up to max_steps steps of every world with queued steps, queued back to back on the device
+ * without waiting (each step is a tick over the worlds that still have steps: the same bits as
+ * max_steps calls of avbd_server_tick), so a request for K steps completes in one call. With
+ * replies, the poses of every world whose request a step completes are gathered right after that
+ * step and copied to pinned host memory in stream order; those tickets are then reported by
+ * avbd_server_ready (once their step has run on the device), not by avbd_server_completed, and
+ * avbd_server_take_reply hands out the poses. No counterpart in the reference (which has no
+ * server). */
+int avbd_server_tick_steps(avbd_server* s, int32_t max_steps, int32_t replies, int32_t* n_stepped);
+/* Tickets whose replies have arrived (wait = 0: without waiting for the device). */
+int avbd_server_ready(avbd_server* s, int64_t* tickets, int32_t cap, int32_t wait, int32_t* n);
+/* The reply of a ready ticket: its world's poses after the completing step, 8 floats per body
+ * (pos, friction, quat), n_bodies rows; with out NULL or cap_bodies < n_bodies only the size is
+ * returned. A reply is handed out once. */
+int avbd_server_take_reply(avbd_server* s, int64_t ticket, float* out, int64_t cap_bodies, int32_t* n_bodies);
 /* Drain up to `cap` completed tickets (oldest first); *n = number written. */
 int avbd_server_completed(avbd_server* s, int64_t* tickets, int32_t cap, int32_t* n);
 /* Poses of every body of each listed world, 8 floats each (pos.xyz, friction, quat), world

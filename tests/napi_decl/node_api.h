@@ -12,6 +12,10 @@ typedef enum { napi_undefined, napi_null, napi_boolean, napi_number, napi_string
 typedef enum { napi_int8_array, napi_uint8_array, napi_uint8_clamped_array, napi_int16_array, napi_uint16_array, napi_int32_array, napi_uint32_array, napi_float32_array, napi_float64_array, napi_bigint64_array, napi_biguint64_array } napi_typedarray_type;
 typedef napi_value (*napi_callback)(napi_env env, napi_callback_info info);
 typedef void (*napi_finalize)(napi_env env, void* data, void* hint);
+typedef struct napi_deferred__* napi_deferred;
+typedef struct napi_async_work__* napi_async_work;
+typedef void (*napi_async_execute_callback)(napi_env env, void* data);
+typedef void (*napi_async_complete_callback)(napi_env env, napi_status status, void* data);
 #define NAPI_AUTO_LENGTH SIZE_MAX
 extern "C" {
 napi_status napi_throw_error(napi_env, const char*, const char*);
@@ -34,5 +38,15 @@ napi_status napi_create_object(napi_env, napi_value*);
 napi_status napi_get_boolean(napi_env, bool, napi_value*);
 napi_status napi_create_function(napi_env, const char*, size_t, napi_callback, void*, napi_value*);
 napi_status napi_create_string_utf8(napi_env, const char*, size_t, napi_value*);
+napi_status napi_create_array_with_length(napi_env, size_t, napi_value*);
+napi_status napi_set_element(napi_env, napi_value, uint32_t, napi_value);
+napi_status napi_create_error(napi_env, napi_value, napi_value, napi_value*);
+napi_status napi_create_promise(napi_env, napi_deferred*, napi_value*);
+napi_status napi_resolve_deferred(napi_env, napi_deferred, napi_value);
+napi_status napi_reject_deferred(napi_env, napi_deferred, napi_value);
+napi_status napi_create_async_work(napi_env, napi_value, napi_value, napi_async_execute_callback,
+                                   napi_async_complete_callback, void*, napi_async_work*);
+napi_status napi_queue_async_work(napi_env, napi_async_work);
+napi_status napi_delete_async_work(napi_env, napi_async_work);
 }
 #define NAPI_MODULE(name, init) napi_value napi_register_module_v1(napi_env env, napi_value exports) { return init(env, exports); }

@@ -171,3 +171,89 @@ def test_admission_fails_cleanly_when_nothing_can_be_evicted(pipe):
     server.release(a)
     assert server.stats()["live_worlds"] == 0
     server.destroy()
+
+
+def _poses(state):
+    """8 floats per body (pos, friction slot, quat) as a reply carries them, from a state read."""
+    return state["position"], state["rotation"]
+
+
+def test_multi_step_ticks_with_replies_equal_worlds_alone(pipe):
+    """Requests of K = 1, 4 and 16 steps run in one multi-step tick each (the steps queued back to
+    back on the device) give the same bits as the worlds stepped alone, and each reply carries its
+    world's poses right after the step that completed the request."""
+    scenes = _scenes()[:5]
+    server = pipe.createServer(budgetBytes=8 << 30)
+    ids = [server.admit(sc) for sc in scenes]
+    ks = [1, 4, 16, 7, 16]
+    tickets = {server.advance(w, k): (i, k) for i, (w, k) in enumerate(zip(ids, ks))}
+    taken = server.tick(maxSteps=16, replies=True)
+    assert taken == sum(ks)
+    assert server.completed() == []  # captured replies are reported by ready(), not completed()
+    got = set()
+    for _ in range(2000):
+        got.update(server.ready())
+        if len(got) == len(tickets):
+            break
+    else:
+        got.update(server.ready(wait=True))
+    assert got == set(tickets)
+    for t, (i, k) in tickets.items():
+        rep = server.takeReply(t)
+        ref = _alone(pipe, scenes[i], k)
+        assert rep.shape == (scenes[i].n_bodies, 8)
+        assert np.array_equal(rep[:, :3], ref["position"]) and np.array_equal(rep[:, 4:], ref["rotation"]), (i, k)
+        _assert_same(server.readBodyState(ids[i]), ref, f"world {i}")
+    with pytest.raises(L.AvbdError):
+        server.takeReply(next(iter(tickets)))  # handed out once
+    server.destroy()
+
+
+def test_world_admitted_while_ticks_are_in_flight(pipe):
+    """Admission does not wait for the queued ticks: a world admitted while another world's steps
+    are still running on the device evolves bit for bit as it does alone, and so does the other."""
+    a_scene, b_scene = _scenes()[1], _scenes()[2]
+    server = pipe.createServer(budgetBytes=8 << 30, initialBodies=4096, initialWorlds=16)
+    a = server.admit(a_scene)
+    server.advance(a, 24)
+    server.tick(maxSteps=12)          # 12 steps queued, not waited for
+    b = server.admit(b_scene)         # admitted while they run
+    server.advance(b, 10)
+    server.tick(maxSteps=16)          # a's last 12 steps with b's 10
+    _assert_same(server.readBodyState(a), _alone(pipe, a_scene, 24), "a")
+    _assert_same(server.readBodyState(b), _alone(pipe, b_scene, 10), "b")
+    server.destroy()
+
+
+def test_fence_wait_on_a_worker_thread_then_replies_without_waiting(pipe):
+    """The Node addon's request loop: a multi-step tick with replies is queued, a worker thread
+    waits on a fence after it (the one thread-safe entry point) while the caller queues the next
+    tick, and then every reply of the first tick is ready without waiting for the device."""
+    import threading
+    scenes = _scenes()[:3]
+    server = pipe.createServer(budgetBytes=8 << 30)
+    ids = [server.admit(sc) for sc in scenes]
+    first = {server.advance(w, 8): i for i, w in enumerate(ids)}
+    server.tick(maxSteps=8, replies=True)
+    fence = pipe.fence()
+    waited = threading.Event()
+    worker = threading.Thread(target=lambda: (fence.wait(), waited.set()))
+    worker.start()
+    second = {server.advance(w, 4): i for i, w in enumerate(ids)}
+    server.tick(maxSteps=4, replies=True)  # queued while the worker waits
+    worker.join(timeout=60)
+    assert waited.is_set() and fence.done
+    fence.destroy()
+    got = set(server.ready())
+    assert set(first) <= got
+    for t, i in first.items():
+        rep = server.takeReply(t)
+        ref = _alone(pipe, scenes[i], 8)
+        assert np.array_equal(rep[:, :3], ref["position"]) and np.array_equal(rep[:, 4:], ref["rotation"]), i
+    got |= set(server.ready(wait=True))
+    assert set(second) <= got
+    for t, i in second.items():
+        rep = server.takeReply(t)
+        ref = _alone(pipe, scenes[i], 12)
+        assert np.array_equal(rep[:, :3], ref["position"]), i
+    server.destroy()
