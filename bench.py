@@ -56,6 +56,8 @@ def args_parse():
     p.add_argument("--serve-rate", type=float, default=10_000.0, help="rate of the served stream in the default line")
     p.add_argument("--budget-gb", type=float, default=120.0, help="served: device-memory budget")
     p.add_argument("--serve-depth", type=int, default=2, help="served: ticks in flight on the device at most")
+    p.add_argument("--serve-steps", type=int, default=4, help="served: steps per world and tick at most")
+    p.add_argument("--serve-steps-sweep", default="1,4,16", help="served workload: steps-per-tick values run at --serve-rate")
     p.add_argument("--no-serve", action="store_true")
     p.add_argument("--worlds", type=int, default=4096)
     p.add_argument("--plain-sample", type=int, default=128, help="worlds timed on the plain path")
@@ -259,12 +261,12 @@ def load_traffic():
         return {}
 
 
-def served_stream(pipe, args, rate, seed):
+def served_stream(pipe, args, rate, seed, max_steps=None):
     """One Poisson request stream through the world server (the serving configuration: 20,000
     requests, creates of log-normal size and advances by K in {1, 4, 16}, continuous batching,
     budgeted admission with LRU eviction). The loop never waits for the device: each pass admits
     the requests that have arrived and, while fewer than `serve_depth` ticks are on the device,
-    queues one multi-step tick (every world with queued steps advances by up to 16 steps, the
+    queues one multi-step tick (every world with queued steps advances by up to `serve_steps` steps, the
     steps back to back on the device, the poses of each world whose request a step completes
     captured right after it); replies are collected as they arrive.
     Latency of a request = arrival to its reply: a create replies once the world is admitted; an
@@ -272,6 +274,7 @@ def served_stream(pipe, args, rate, seed):
     import torch
     from avbd_gb300 import _lib as L
     from avbd_gb300 import workloads
+    max_steps = max_steps or args.serve_steps
     r = workloads.request_stream(args.requests, rate, seed)
     creates = np.nonzero(r["create"])[0]
     packed = {int(i): L.PackedScene(workloads.lattice_pile(int(r["count"][i]), int(r["world_seed"][i]))) for i in creates}
@@ -316,7 +319,7 @@ def served_stream(pipe, args, rate, seed):
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            if server.tick(maxSteps=16, replies=True):
+            if server.tick(maxSteps=max_steps, replies=True):
                 e1.record(stream)
                 tick_events.append((e0, e1))
                 inflight.append(pipe.fence())
@@ -326,7 +329,7 @@ def served_stream(pipe, args, rate, seed):
             d2h += server.takeReply(t).nbytes
             lat_adv.append(now_s - ticket_info.pop(t))
         if not done and i < n and arrival[i] > time.perf_counter() - t0:
-            time.sleep(min(arrival[i] - (time.perf_counter() - t0), 0.0005))
+            time.sleep(max(0.0, min(arrival[i] - (time.perf_counter() - t0), 0.0005)))
     pipe.synchronize()
     wall = time.perf_counter() - t0
     for f in inflight:
@@ -342,7 +345,8 @@ def served_stream(pipe, args, rate, seed):
             "latency_ms": {"p50": pct_(lat, 50), "p95": pct_(lat, 95), "p99": pct_(lat, 99)},
             "advance_latency_ms": {"p50": pct_(la, 50), "p95": pct_(la, 95), "p99": pct_(la, 99)},
             "tick_ms": {"p50": pct_(tick_ms, 50), "p95": pct_(tick_ms, 95), "p99": pct_(tick_ms, 99), "ticks": len(tick_ms),
-                        "what": "device time of one serving tick (up to 16 steps of every world with queued steps)"},
+                        "what": f"device time of one serving tick (up to {max_steps} steps of every world with queued steps)"},
+            "max_steps_per_tick": max_steps, "ticks_in_flight": args.serve_depth,
             "admitted_worlds": st["admitted"], "rejected_worlds": rejected, "evictions": st["evictions"],
             "restores": st["restores"], "peak_device_gb": round(st["peak_device_bytes"] / 1e9, 2),
             "budget_gb": args.budget_gb, "h2d_bytes": int(h2d), "d2h_bytes": int(d2h),
@@ -362,6 +366,11 @@ def run_served(args, dist):
             log(f"served stream at {rate:.0f} req/s")
             lines.append(served_stream(pipe, args, rate, workloads.SEED_BASE + 4 + 1000 * dist.rank))
             log(json.dumps(lines[-1]))
+        steps_sweep = []
+        for m in (int(x) for x in args.serve_steps_sweep.split(",") if x):
+            log(f"served stream at {args.serve_rate:.0f} req/s, up to {m} steps per tick")
+            steps_sweep.append(served_stream(pipe, args, args.serve_rate, workloads.SEED_BASE + 4 + 1000 * dist.rank, m))
+            log(json.dumps(steps_sweep[-1]))
     pipe.destroy()
     if dist.rank != 0:
         return
@@ -371,7 +380,7 @@ def run_served(args, dist):
             "dtype": "f32", "data": "synthetic",
             "config": {"workload": "served_poisson", "requests": args.requests, "budget_gb": args.budget_gb,
                        "rates": args.rates},
-            "served": lines, "clocks": clk.summary()}
+            "served": lines, "steps_per_tick_sweep": steps_sweep, "clocks": clk.summary()}
     print(json.dumps(line), flush=True)
 
 
