@@ -9,7 +9,8 @@
 //
 // Tuned parameters:
 //   solve    schedule (tile queue / colour barriers), chunks per block and colour (the width of a
-//            colour-bucket chunk, i.e. bodies per block), persistent grid size (blocks per SM);
+//            colour-bucket chunk, i.e. bodies per block), persistent grid size (blocks per SM, or
+//            a quarter of the SMs for small ticks);
 //   radix    digit width of the tree build's Morton-code sort (4, 6 or 8 bits), on rebuild ticks.
 // A workload class is (device, log2 of the tick's bodies, whether it has joints, iterations).
 // Environment overrides (AVBD_SOLVE*, AVBD_RADIX_BITS) pin a parameter; AVBD_TUNE=0 keeps the
@@ -82,6 +83,7 @@ class Tuner {
     add(1, 2, 3 * sms);
     add(0, 1, 0);
     add(0, 2, 0);
+    add(0, 1, sms / 4 > 8 ? sms / 4 : 8);  // small ticks: fewer blocks make each colour barrier cheaper
     return c;
   }
   static std::vector<int> radixCandidates() { return {8, 6, 4}; }

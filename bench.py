@@ -56,7 +56,7 @@ def args_parse():
     p.add_argument("--serve-rate", type=float, default=10_000.0, help="rate of the served stream in the default line")
     p.add_argument("--budget-gb", type=float, default=120.0, help="served: device-memory budget")
     p.add_argument("--serve-depth", type=int, default=2, help="served: ticks in flight on the device at most")
-    p.add_argument("--serve-steps", type=int, default=4, help="served: steps per world and tick at most")
+    p.add_argument("--serve-steps", type=int, default=1, help="served: steps per world and tick at most (1: lowest latency; measured 1, 4, 16)")
     p.add_argument("--serve-steps-sweep", default="1,4,16", help="served workload: steps-per-tick values run at --serve-rate")
     p.add_argument("--no-serve", action="store_true")
     p.add_argument("--worlds", type=int, default=4096)
