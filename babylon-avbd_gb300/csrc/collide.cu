@@ -958,8 +958,35 @@ __device__ __forceinline__ void append(int* list, int* n, int p, bool take) {
   list[base + __popc(m & ((1u << lane) - 1))] = p;
 }
 
+// A sphere and a box clearly apart: the distance from the sphere's centre to the box exceeds its
+// radius by far more than any rounding of the separating-axis search (1e-3 plus 1e-5 of the
+// coordinates' size), so that search would end with a positive gap and no contact: skip it.
+__device__ __forceinline__ bool sphere_box_apart(float4 pA, float4 qA, float4 sA, int shA, float4 pB, float4 qB, float4 sB,
+                                                 int shB) {
+  if (shA == SHAPE_CAPSULE || shB == SHAPE_CAPSULE) return false;  // capsules always run the search
+  const bool sphereA = shA == SHAPE_SPHERE;
+  const float4 pc = sphereA ? pA : pB, pbx = sphereA ? pB : pA, qbx = sphereA ? qB : qA, sbx = sphereA ? sB : sA;
+  const float r = (sphereA ? sA : sB).x * 0.5f;
+  const V3 l = rotateInv(qbx, v3(pc) - v3(pbx));
+  const V3 h{sbx.x * 0.5f, sbx.y * 0.5f, sbx.z * 0.5f};
+  const V3 o{fmaxf(fabsf(l.x) - h.x, 0.f), fmaxf(fabsf(l.y) - h.y, 0.f), fmaxf(fabsf(l.z) - h.z, 0.f)};
+  const float margin = 1e-3f + 1e-5f * (fabsf(pc.x) + fabsf(pc.y) + fabsf(pc.z) + fabsf(pbx.x) + fabsf(pbx.y) + fabsf(pbx.z));
+  const float reach = r + margin;
+  return dot(o, o) > reach * reach;
+}
+
+// What finish_pair stores for a pair without contacts.
+__device__ __forceinline__ void finish_empty(const WorldDev& W, PairPtrs& cur, int p, float4 sA, float4 sB) {
+  cur.count[p] = 0;
+  cur.basis[3 * p + 0] = make_float4(0.f, 0.f, 0.f, sqrtf(sA.w * sB.w));
+  cur.basis[3 * p + 1] = make_float4(0.f, 0.f, 0.f, W.alpha);
+  cur.basis[3 * p + 2] = make_float4(0.f, 0.f, 0.f, W.betaLin);
+}
+
 // Pass 1: box-box pairs run SAT; separated ones are finished here (no contacts), the others are
-// queued with their chosen axis. Pairs with a sphere are queued for the generic path.
+// queued with their chosen axis. Pairs with a sphere or a capsule are queued for the generic path,
+// except sphere-box pairs clearly apart (sphere_box_apart), finished here too: the generic kernel
+// then gets only pairs that run the full search, so its warps do not idle on finished lanes.
 __global__ void __launch_bounds__(256) k_np_classify(BodyPtrs bd, const WorldDev* __restrict__ worlds, PairPtrs cur, Tick t,
                                                      const Counters* __restrict__ ctr, NarrowScratch ns) {
   const int np = ctr->activePairs;
@@ -974,6 +1001,13 @@ __global__ void __launch_bounds__(256) k_np_classify(BodyPtrs bd, const WorldDev
       if (shA != SHAPE_BOX || shB != SHAPE_BOX) {  // a sphere or a capsule: the generic path
         sphere = true;
         bothRound = shA != SHAPE_BOX && shB != SHAPE_BOX;
+        if (!bothRound) {
+          const float4 sA = bd.size[a], sB = bd.size[b];
+          if (sphere_box_apart(bd.pos(a), bd.rot(a), sA, shA, bd.pos(b), bd.rot(b), sB, shB)) {
+            finish_empty(worlds[bd.meta[a].x], cur, p, sA, sB);
+            sphere = false;
+          }
+        }
       } else {
         const WorldDev& W = worlds[bd.meta[a].x];
         box::Sat best;
@@ -993,7 +1027,7 @@ __global__ void __launch_bounds__(256) k_np_classify(BodyPtrs bd, const WorldDev
 
 // Pass 2a: contacts of box-box pairs that SAT found overlapping.
 #ifndef AVBD_NP_BOX_MINB
-#define AVBD_NP_BOX_MINB 5
+#define AVBD_NP_BOX_MINB 4  // blocks per SM the register allocation must allow (128 registers)
 #endif
 __global__ void __launch_bounds__(128, AVBD_NP_BOX_MINB) k_np_box(BodyPtrs bd, const WorldDev* __restrict__ worlds, PairPtrs cur, Tick t,
                                                 NarrowScratch ns) {
@@ -1029,23 +1063,6 @@ __global__ void __launch_bounds__(128, AVBD_NP_BOX_MINB) k_np_box(BodyPtrs bd, c
 
 // Pass 2b: pairs with a sphere (generic support-function SAT, one contact): sphere-box pairs,
 // then sphere-sphere pairs in a lighter instance of the same code.
-// A sphere and a box clearly apart: the distance from the sphere's centre to the box exceeds its
-// radius by far more than any rounding of the separating-axis search (1e-3 plus 1e-5 of the
-// coordinates' size), so that search would end with a positive gap and no contact: skip it.
-__device__ __forceinline__ bool sphere_box_apart(float4 pA, float4 qA, float4 sA, int shA, float4 pB, float4 qB, float4 sB,
-                                                 int shB) {
-  if (shA == SHAPE_CAPSULE || shB == SHAPE_CAPSULE) return false;  // capsules always run the search
-  const bool sphereA = shA == SHAPE_SPHERE;
-  const float4 pc = sphereA ? pA : pB, pbx = sphereA ? pB : pA, qbx = sphereA ? qB : qA, sbx = sphereA ? sB : sA;
-  const float r = (sphereA ? sA : sB).x * 0.5f;
-  const V3 l = rotateInv(qbx, v3(pc) - v3(pbx));
-  const V3 h{sbx.x * 0.5f, sbx.y * 0.5f, sbx.z * 0.5f};
-  const V3 o{fmaxf(fabsf(l.x) - h.x, 0.f), fmaxf(fabsf(l.y) - h.y, 0.f), fmaxf(fabsf(l.z) - h.z, 0.f)};
-  const float margin = 1e-3f + 1e-5f * (fabsf(pc.x) + fabsf(pc.y) + fabsf(pc.z) + fabsf(pbx.x) + fabsf(pbx.y) + fabsf(pbx.z));
-  const float reach = r + margin;
-  return dot(o, o) > reach * reach;
-}
-
 #ifndef AVBD_NP_SPHERE_MINB
 #define AVBD_NP_SPHERE_MINB 5  // blocks per SM the register allocation must allow
 #endif
@@ -1065,9 +1082,7 @@ __global__ void __launch_bounds__(128, AVBD_NP_SPHERE_MINB) k_np_sphere(BodyPtrs
     M33 basis{V3{0, 0, 0}, V3{0, 0, 0}, V3{0, 0, 0}};
     uint32_t feat[1] = {1u};  // feature i + 1
     V3 rA[1], rB[1];
-    const int nc = (!BOTH_ROUND && sphere_box_apart(pA, qA, sA, shA, pB, qB, sB, shB))
-                       ? 0
-                       : gen::collide<BOTH_ROUND>(pA, qA, sA, shA, pB, qB, sB, shB, basis, rA[0], rB[0]);
+    const int nc = gen::collide<BOTH_ROUND>(pA, qA, sA, shA, pB, qB, sB, shB, basis, rA[0], rB[0]);
     finish_pair(bd, W, t, bd.meta[a].x, cur, p, key, pA, qA, sA, pB, qB, sB, true, nc, basis, feat, rA, rB);
   }
 }
