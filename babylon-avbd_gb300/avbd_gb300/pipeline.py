@@ -1032,12 +1032,38 @@ class Batch:
         self._jointCounts = [p.n_joints for p in self._packed]
         self._kinds = [np.asarray(a.kind, dtype=np.int32).copy() for a in arrays_list]
         self.bodyCount = int(sum(self.bodyCounts))
+        self._pinned = []  # page-locked blocks of pinnedPoses(), freed with the batch
 
     def step(self, steps: int = 1):
         if self._h is None:
             raise RuntimeError("The batch has been destroyed")
         L.check(L.lib().avbd_batch_step(self._h, int(steps)))
         return self
+
+    def pinnedPoses(self) -> np.ndarray:
+        """A page-locked (bodyCount, 8) float32 array for stepRead, freed with the batch."""
+        ptr = C.c_void_p()
+        L.check(L.lib().avbd_pinned_alloc(max(self.bodyCount, 1) * 32, C.byref(ptr)))
+        self._pinned.append(ptr)
+        buf = (C.c_float * (max(self.bodyCount, 1) * 8)).from_address(ptr.value)
+        return np.ctypeslib.as_array(buf)[: self.bodyCount * 8].reshape(self.bodyCount, 8)
+
+    def stepRead(self, steps: int, out: np.ndarray) -> int:
+        """Queue ``steps`` steps and, after the last, a copy of every pose into ``out`` (page-locked:
+        ``pinnedPoses()``); returns at once with a tag for ``readDone``."""
+        if self._h is None:
+            raise RuntimeError("The batch has been destroyed")
+        if out.dtype != np.float32 or out.size != self.bodyCount * 8 or not out.flags["C_CONTIGUOUS"]:
+            raise ValueError("out must be a contiguous float32 array of bodyCount x 8")
+        tag = C.c_int64()
+        L.check(L.lib().avbd_batch_step_read(self._h, int(steps), out.ctypes.data_as(C.c_void_p), C.byref(tag)))
+        return int(tag.value)
+
+    def readDone(self, tag: int, wait: bool = False) -> bool:
+        """Whether the read of ``tag`` has landed (wait: block until it has, not for later steps)."""
+        done = C.c_int32()
+        L.check(L.lib().avbd_batch_read_done(self._h, int(tag), int(bool(wait)), C.byref(done)))
+        return bool(done.value)
 
     def readBodyState(self, world: int) -> dict:
         if not 0 <= world < self.worldCount:
@@ -1233,6 +1259,9 @@ class Batch:
             return
         L.check(L.lib().avbd_batch_destroy(self._h))
         self._h = None
+        for ptr in self._pinned:
+            L.lib().avbd_pinned_free(ptr)
+        self._pinned = []
         if self in self._pipe._children:
             self._pipe._children.remove(self)
 

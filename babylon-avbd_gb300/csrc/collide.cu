@@ -224,13 +224,23 @@ __device__ __forceinline__ void for_each_partner(const PairCtx& c, const WorldDe
   const bool small = !(pA.w > W.largeR);
   if (small) {
     const int cx = cell_coord(pA.x, W.cell), cy = cell_coord(pA.y, W.cell), cz = cell_coord(pA.z, W.cell);
-    for (int dz = -1; dz <= 1; dz++) {
-      // the nine bucket ranges of this plane are loaded together (eighteen independent loads in
-      // flight instead of two), then scanned in the same order as before
+    // Only the neighbour cells within the body's reach: a partner is closer than rA + rB <= rA +
+    // cell / 2 on every axis (cell >= 2 x the largest small radius); the reach is padded far
+    // beyond the rounding of the coordinates, so no cell that can hold a partner is skipped.
+    const float reach = pA.w + 0.501f * W.cell + 1e-5f * (fabsf(pA.x) + fabsf(pA.y) + fabsf(pA.z));
+    const int x0 = cell_coord(pA.x - reach, W.cell) < cx ? -1 : 0, x1 = cell_coord(pA.x + reach, W.cell) > cx ? 1 : 0;
+    const int y0 = cell_coord(pA.y - reach, W.cell) < cy ? -1 : 0, y1 = cell_coord(pA.y + reach, W.cell) > cy ? 1 : 0;
+    const int z0 = cell_coord(pA.z - reach, W.cell) < cz ? -1 : 0, z1 = cell_coord(pA.z + reach, W.cell) > cz ? 1 : 0;
+    for (int dz = z0; dz <= z1; dz++) {
+      // the bucket ranges of this plane are loaded together (up to eighteen independent loads in
+      // flight instead of two), then scanned
       int r0[9], r1[9];
 #pragma unroll
       for (int q = 0; q < 9; q++) {
-        const uint32_t b = cell_hash(w, cx + (q % 3) - 1, cy + (q / 3) - 1, cz + dz) & g.tableMask;
+        const int dx = (q % 3) - 1, dy = (q / 3) - 1;
+        r0[q] = r1[q] = 0;
+        if (dx < x0 || dx > x1 || dy < y0 || dy > y1) continue;
+        const uint32_t b = cell_hash(w, cx + dx, cy + dy, cz + dz) & g.tableMask;
         r0[q] = g.cellCount[b];
         r1[q] = g.cellCount[b + 1];
       }

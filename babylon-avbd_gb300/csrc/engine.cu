@@ -21,6 +21,9 @@ struct avbd_batch {
   Arena* A;
   std::vector<int> worlds;
   int64_t bodies;
+  std::vector<std::pair<long long, int>> starts;  // (first body, world slot), ascending
+  long long nextTag = 1;                          // tags of avbd_batch_step_read, in queue order
+  long long doneUpTo = 0;                         // every tag up to this one is confirmed
 };
 
 // ---------------------------------------------------------------- device helpers for the ABI
@@ -151,20 +154,30 @@ void setVelocities(Arena& A, const std::vector<std::pair<long long, int>>& start
   for (int k = 0; velocity && k < 3 * n; k++) REQUIRE(std::isfinite(velocity[k]), "velocities must be finite");
   for (int k = 0; angular && k < 3 * n; k++) REQUIRE(std::isfinite(angular[k]), "velocities must be finite");
   if (n == 0 || (!velocity && !angular)) return;
-  std::map<int, std::vector<uint32_t>> per;  // world slot -> records
+  // (start index, k) in index order: each world's records stay in call order (stable sort)
+  std::vector<std::pair<int, int>> order(n);
   for (int k = 0; k < n; k++) {
     const auto it = std::upper_bound(starts.begin(), starts.end(), std::make_pair((long long)indices[k], INT32_MAX)) - 1;
-    std::vector<uint32_t>& r = per[it->second];
-    const uint32_t local = uint32_t((long long)indices[k] - it->first);
-    for (int kind = 0; kind < 2; kind++) {
-      const float* v = kind == 0 ? velocity : angular;
-      if (!v) continue;
-      uint32_t rec[12] = {local, uint32_t(kind), 0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
-      std::memcpy(rec + 4, v + 3 * size_t(k), 12);
-      r.insert(r.end(), rec, rec + 12);
-    }
+    order[k] = {int(it - starts.begin()), k};
   }
-  for (auto& kv : per) A.queueEdits(kv.first, kv.second.data(), int(kv.second.size() / 12));
+  std::stable_sort(order.begin(), order.end(), [](const std::pair<int, int>& x, const std::pair<int, int>& y) { return x.first < y.first; });
+  std::vector<uint32_t> r;
+  for (size_t a = 0; a < order.size();) {
+    const int si = order[a].first;
+    r.clear();
+    for (; a < order.size() && order[a].first == si; a++) {
+      const int k = order[a].second;
+      const uint32_t local = uint32_t((long long)indices[k] - starts[size_t(si)].first);
+      for (int kind = 0; kind < 2; kind++) {
+        const float* v = kind == 0 ? velocity : angular;
+        if (!v) continue;
+        uint32_t rec[12] = {local, uint32_t(kind), 0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
+        std::memcpy(rec + 4, v + 3 * size_t(k), 12);
+        r.insert(r.end(), rec, rec + 12);
+      }
+    }
+    A.queueEdits(starts[size_t(si)].second, r.data(), int(r.size() / 12));
+  }
 }
 
 }  // namespace
@@ -728,7 +741,10 @@ int avbd_batch_create(avbd_ctx* ctx, const avbd_scene_desc* scenes, const avbd_p
   Arena* A = arenaFor(ctx, scenes, params, n_worlds, slots);
   int64_t nb = 0;
   for (int i = 0; i < n_worlds; i++) nb += scenes[i].n_bodies;
-  *out = new avbd_batch{A, slots, nb};
+  auto* b = new avbd_batch{A, slots, nb, {}, 1, 0};
+  for (int w : b->worlds) b->starts.emplace_back((long long)A->W[w].dev.bodyOff, w);
+  std::sort(b->starts.begin(), b->starts.end());
+  *out = b;
   API_END
 }
 
@@ -776,14 +792,99 @@ int avbd_batch_read_poses(avbd_batch* b, float* out) {
   Arena& A = *b->A;
   bind(A.ctx);
   const int n = int(b->bodies);  // the batch's worlds occupy bodies [0, n) in creation order
-  A.resolve();
-  if (n == 0) return AVBD_OK;
-  if (!A.poseStage) A.poseStage = dalloc<float4>(size_t(n) * 2);
+  if (n == 0) {
+    A.resolve();
+    return AVBD_OK;
+  }
+  if (!A.poseStage) {
+    A.resolve();  // the allocation waits for the device anyway
+    A.poseStage = dalloc<float4>(size_t(n) * 2);
+  }
   int blocks = grid_blocks(n, 256);
   if (blocks > device_sms() * 8) blocks = device_sms() * 8;
-  k_read_poses<<<blocks, 256, 0, A.s>>>(A.B.pose, A.B.size, n, A.poseStage); note_launches(1);
-  CK(cudaMemcpyAsync(out, A.poseStage, size_t(n) * 32, cudaMemcpyDeviceToHost, A.s));
-  CK(cudaStreamSynchronize(A.s));
+  // the read is queued behind the steps in flight and waited for with them (one wait); if one of
+  // those steps held itself, resolve() re-ran it after the read, which is then made again
+  const long long held = A.ticksHeld;
+  for (int pass = 0; pass < 2; pass++) {
+    k_read_poses<<<blocks, 256, 0, A.s>>>(A.B.pose, A.B.size, n, A.poseStage); note_launches(1);
+    CK(cudaMemcpyAsync(out, A.poseStage, size_t(n) * 32, cudaMemcpyDeviceToHost, A.s));
+    A.resolve();
+    CK(cudaStreamSynchronize(A.s));
+    if (A.ticksHeld == held) break;
+  }
+  API_END
+}
+
+int avbd_batch_step_read(avbd_batch* b, int32_t steps, float* out, int64_t* tag) {
+  API_BEGIN
+  REQUIRE(b && out && tag, "null argument");
+  REQUIRE(steps >= 1, "steps must be positive");
+  Arena& A = *b->A;
+  bind(A.ctx);
+  cudaPointerAttributes at{};
+  REQUIRE(cudaPointerGetAttributes(&at, out) == cudaSuccess && at.type == cudaMemoryTypeHost,
+          "out must be page-locked host memory (avbd_pinned_alloc, cudaHostAlloc or cudaHostRegister)");
+  const int n = int(b->bodies);
+  if (!A.poseStage && n > 0) {
+    A.resolve();
+    A.poseStage = dalloc<float4>(size_t(n) * 2);
+  }
+  for (int i = 0; i + 1 < steps; i++) A.stepWorlds(b->worlds);
+  Arena::TickReply reply;
+  const long long t = b->nextTag++;
+  if (n > 0) {
+    reply.rows = n;
+    reply.dev = A.poseStage;
+    reply.host = reinterpret_cast<float4*>(out);
+    reply.seg.push_back(make_int4(0, n, 0, 0));  // the batch's bodies are [0, n) of its arena
+  }
+  reply.tags.push_back(t);
+  A.stepWorlds(b->worlds, &reply);
+  *tag = t;
+  API_END
+}
+
+int avbd_batch_read_done(avbd_batch* b, int64_t tag, int32_t wait, int32_t* done) {
+  API_BEGIN
+  REQUIRE(b && done, "null argument");
+  REQUIRE(tag > 0 && tag < b->nextTag, "no such read");
+  Arena& A = *b->A;
+  bind(A.ctx);
+  // ticks are confirmed in queue order and tags grow with it
+  auto collect = [&] {
+    for (long long c : A.confirmedTags) b->doneUpTo = std::max(b->doneUpTo, c);
+    A.confirmedTags.clear();
+  };
+  A.trimLog();
+  collect();
+  if (tag > b->doneUpTo && wait) {
+    for (const auto& e : A.tickLog)  // wait for that tick only, not for the ticks queued after it
+      if (std::find(e.reply.tags.begin(), e.reply.tags.end(), (long long)tag) != e.reply.tags.end()) {
+        CK(cudaEventSynchronize(e.done));
+        break;
+      }
+    A.trimLog();
+    collect();
+    if (tag > b->doneUpTo) {  // held and queued again: make every queued tick final
+      A.resolve();
+      collect();
+    }
+  }
+  *done = tag <= b->doneUpTo ? 1 : 0;
+  API_END
+}
+
+int avbd_pinned_alloc(int64_t bytes, void** out) {
+  API_BEGIN
+  REQUIRE(out && bytes > 0, "bad argument");
+  *out = nullptr;
+  CK(cudaHostAlloc(out, size_t(bytes), cudaHostAllocDefault));
+  API_END
+}
+
+int avbd_pinned_free(void* p) {
+  API_BEGIN
+  if (p) CK(cudaFreeHost(p));
   API_END
 }
 
@@ -792,10 +893,7 @@ int avbd_batch_set_velocities(avbd_batch* b, const uint32_t* indices, int32_t n,
   REQUIRE(b, "null batch");
   bind(b->A->ctx);
   // batch body index (the arena's body slot) -> (world, local index)
-  std::vector<std::pair<long long, int>> starts;
-  for (int w : b->worlds) starts.emplace_back((long long)b->A->W[w].dev.bodyOff, w);
-  std::sort(starts.begin(), starts.end());
-  setVelocities(*b->A, starts, b->bodies, indices, n, velocity, angular);
+  setVelocities(*b->A, b->starts, b->bodies, indices, n, velocity, angular);
   API_END
 }
 

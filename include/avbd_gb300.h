@@ -358,6 +358,20 @@ int avbd_batch_counters(avbd_batch* b, avbd_counters* out);
 /* Poses of every body of every world, 8 floats each (pos.xyz, friction, quat), world by world
  * in creation order (readSelectedBodies(.., {posesOnly: true}) over the whole batch). */
 int avbd_batch_read_poses(avbd_batch* b, float* out);
+/* Pipelined reads (the WebGPU backend's reads are asynchronous too: mapAsync): queue `steps`
+ * steps of every world and, right after the last one, a copy of every body's pose (the layout of
+ * avbd_batch_read_poses) into `out`, then return at once with a tag. `out` must be page-locked host
+ * memory (avbd_pinned_alloc, cudaHostAlloc or cudaHostRegister) and stay valid until the read is
+ * done; the copy runs in stream order behind the steps and is made again if one of them had to be
+ * re-run. avbd_batch_read_done: *done = 1 once the read has landed (wait = 1: block until then,
+ * without waiting for steps queued after it). Typical loop: step_read into one of two buffers,
+ * then read_done on the other, so the host never stalls the device. No counterpart in the
+ * reference's CPU path. */
+int avbd_batch_step_read(avbd_batch* b, int32_t steps, float* out, int64_t* tag);
+int avbd_batch_read_done(avbd_batch* b, int64_t tag, int32_t wait, int32_t* done);
+/* Page-locked host memory for avbd_batch_step_read (cudaHostAlloc / cudaFreeHost). */
+int avbd_pinned_alloc(int64_t bytes, void** out);
+int avbd_pinned_free(void* p);
 /* setVelocities for bodies given by batch-global index (world offset + body index). */
 int avbd_batch_set_velocities(avbd_batch* b, const uint32_t* indices, int32_t n, const float* velocity, const float* angular);
 /* Body commands (as avbd_world_edit) for world `world` of the batch (world-local body indices). */

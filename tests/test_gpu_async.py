@@ -118,3 +118,29 @@ def test_queue_wait_limit_reports_an_error(pipe, monkeypatch):
     v.step(3)
     assert np.isfinite(v.readBodyState()["position"]).all()
     v.destroy()
+
+
+def test_pipelined_reads_equal_synchronous_reads(pipe):
+    """Batch reads queued behind their steps (stepRead into two page-locked buffers, readDone on
+    the previous one) give the poses a synchronous read gives after the same steps, also when the
+    first steps overflow the initial pair regions and are held and re-run (with their reads)."""
+    scenes = [_dense_cluster(seed=s) for s in (7, 8, 9)]
+    a = pipe.createBatch(scenes)
+    bufs = [a.pinnedPoses(), a.pinnedPoses()]
+    got, tags = [], []
+    for k in range(8):
+        tags.append(a.stepRead(1, bufs[k % 2]))
+        if k >= 1:
+            assert a.readDone(tags[k - 1], wait=True)
+            got.append(bufs[(k - 1) % 2].copy())
+    assert a.readDone(tags[-1], wait=True)
+    got.append(bufs[7 % 2].copy())
+    assert a.profileRead()["ticks_held"] >= 1
+    b = pipe.createBatch(scenes)
+    for k in range(8):
+        b.step(1)
+        assert np.array_equal(got[k], b.readPoses()), k
+    with pytest.raises(L.AvbdError):
+        a.stepRead(1, np.zeros((a.bodyCount, 8), dtype=np.float32))  # not page-locked
+    a.destroy()
+    b.destroy()
