@@ -647,6 +647,7 @@ struct FenceWork {
   int status = AVBD_OK;
   std::string error;
   int32_t stepped = 0;         // tickAsync: steps queued by the tick
+  bool only = false;           // fence: nothing to do after the wait
   bool read = false;           // readPosesAsync: the worlds to read and their total bodies
   std::vector<int64_t> ids;
   size_t bodies = 0;
@@ -661,7 +662,9 @@ void FenceComplete(napi_env env, napi_status, void* data) {  // main thread
   auto* f = static_cast<FenceWork*>(data);
   avbd_fence_destroy(f->fence);
   napi_value result = nullptr;
-  if (f->status == AVBD_OK) {
+  if (f->status == AVBD_OK && f->only) {
+    napi_get_undefined(env, &result);
+  } else if (f->status == AVBD_OK) {
     if (f->read) {
       float* out;
       result = Float32(env, f->bodies * 8, &out);
@@ -698,6 +701,19 @@ napi_value QueueFence(napi_env env, avbd_ctx* ctx, FenceWork* f) {
   napi_create_async_work(env, nullptr, name, FenceExecute, FenceComplete, f, &f->work);
   napi_queue_async_work(env, f->work);
   return promise;
+}
+
+// (ctx) -> Promise<undefined>, settled once the device has run everything queued before the call
+// (the reference's device.queue.onSubmittedWorkDone()). A read made after it finds the steps done,
+// so the event loop never waits on the device: the world's async reads await it first.
+napi_value Fence(napi_env env, napi_callback_info info) {
+  napi_value argv[1];
+  if (!Args(env, info, argv, 1)) return nullptr;
+  auto* ctx = External<avbd_ctx>(env, argv[0]);
+  if (!ctx) return nullptr;
+  auto* f = new FenceWork;
+  f->only = true;
+  return QueueFence(env, ctx, f);
 }
 
 // (ctx, s, maxSteps) -> Promise<{stepped, replies: [{ticket, poses}]}>: one multi-step tick with
@@ -758,7 +774,8 @@ napi_value Init(napi_env env, napi_value exports) {
              {"advance", Advance},             {"tick", Tick},                     {"completed", Completed},
              {"serverReadPoses", ServerReadPoses}, {"serverEdit", ServerEdit},     {"evict", Evict},
              {"release", Release},             {"serverStats", ServerStats},       {"tickSteps", TickSteps},
-             {"ready", Ready},                 {"tickAsync", TickAsync},           {"readPosesAsync", ReadPosesAsync}};
+             {"ready", Ready},                 {"tickAsync", TickAsync},           {"readPosesAsync", ReadPosesAsync},
+             {"fence", Fence}};
   for (const auto& f : fns) {
     napi_value v;
     napi_create_function(env, f.name, NAPI_AUTO_LENGTH, f.fn, nullptr, &v);

@@ -147,6 +147,7 @@ export function packScene(scene, options = {}) {
 class Gb300World {
   constructor(ctx, scene, options) {
     const packed = packScene(scene, options);
+    this.ctx = ctx;
     this.handle = addon.createWorld(ctx, packed.arrays, packed.params);
     this.mass = packed.arrays.mass;  // per slot, for readBodyState(index)
     this.dimension = 3;
@@ -222,8 +223,14 @@ class Gb300World {
       values.angular !== undefined ? Float32Array.from(values.angular) : null);
     return this;
   }
+  /** Resolves once the steps queued so far have run (a libuv worker waits, not the event loop);
+   * the reads below await it, so the read itself finds the device idle. */
+  deviceIdle() {
+    return addon.fence(this.ctx);
+  }
   async readSelectedBodies(indices, { posesOnly = false } = {}) {
     this.assertLive();
+    await this.deviceIdle();
     return addon.readSelected(this.handle, Uint32Array.from(indices), posesOnly);
   }
   async readBodies() {
@@ -233,6 +240,7 @@ class Gb300World {
    * record (word 19 is its effective mass, 0 while it sleeps); without an index, every body. */
   async readBodyState(index) {
     this.assertLive();
+    await this.deviceIdle();
     if (index === undefined) return addon.readState(this.handle, this.bodyCount);
     this.liveIndex(index);
     const r = addon.readSelected(this.handle, Uint32Array.of(index), false);
@@ -245,10 +253,12 @@ class Gb300World {
   }
   async readJoints() {
     this.assertLive();
+    await this.deviceIdle();
     return addon.readJoints(this.handle, this.jointCount);
   }
   async readCounters() {
     this.assertLive();
+    await this.deviceIdle();
     return addon.readCounters(this.handle);
   }
   setFilters(indices, groups, collidesWith) {

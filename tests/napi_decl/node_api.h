@@ -36,6 +36,7 @@ napi_status napi_create_typedarray(napi_env, napi_typedarray_type, size_t, napi_
 napi_status napi_create_external(napi_env, void*, napi_finalize, void*, napi_value*);
 napi_status napi_create_object(napi_env, napi_value*);
 napi_status napi_get_boolean(napi_env, bool, napi_value*);
+napi_status napi_get_undefined(napi_env, napi_value*);
 napi_status napi_create_function(napi_env, const char*, size_t, napi_callback, void*, napi_value*);
 napi_status napi_create_string_utf8(napi_env, const char*, size_t, napi_value*);
 napi_status napi_create_array_with_length(napi_env, size_t, napi_value*);
