@@ -474,7 +474,10 @@ def run_ours(args, dist):
     # one candidate schedule (tile queue or colour barriers, chunk width, grid size; the same bits
     # for all) and the fastest is kept for the process
     tb = pipe.createBatch(worlds)
-    tb.step(16)
+    # the radix width is timed on tree rebuild ticks only (one in bvh_rebuild): tree workloads
+    # need that many more ticks for its three candidates' two samples each
+    trees = [int(getattr(w.params, "bvh_rebuild", 16) or 16) for w in worlds if getattr(w.params, "broadphase", "auto") != "grid"]
+    tb.step(16 + (7 * max(trees) if trees and args.workload in ("mixed_1m", "cloth_wall") else 0))
     pipe.synchronize()
     tp = tb.profileRead()
     tuner = {"tuned": bool(tp["tuned"]), "solve": "tile queue" if tp["solve_queue"] else "colour barriers",
