@@ -68,7 +68,7 @@ class Tuner {
     }
   }
 
-  static std::vector<SolveConfig> solveCandidates(const SolveConfig& b, int sms) {
+  static std::vector<SolveConfig> solveCandidates(const SolveConfig& b, int sms, int sizeLog2) {
     std::vector<SolveConfig> c;
     auto add = [&](int queue, int waves, int blocks) {
       SolveConfig x = b;
@@ -83,7 +83,7 @@ class Tuner {
     add(1, 2, 3 * sms);
     add(0, 1, 0);
     add(0, 2, 0);
-    add(0, 1, sms / 4 > 8 ? sms / 4 : 8);  // small ticks: fewer blocks make each colour barrier cheaper
+    if (sizeLog2 <= 16) add(0, 1, sms / 4 > 8 ? sms / 4 : 8);  // small ticks: fewer blocks make each colour barrier cheaper
     return c;
   }
   static std::vector<int> radixCandidates() { return {8, 6, 4}; }
@@ -114,7 +114,7 @@ class Tuner {
       } else {
         auto& st = state(key);
         if (st.solveCands.empty()) {
-          st.solveCands = solveCandidates(base, sms);
+          st.solveCands = solveCandidates(base, sms, key.sizeLog2);
           st.solveBest.assign(st.solveCands.size(), 1e30f);
           st.solveSeen.assign(st.solveCands.size(), 0);
         }
