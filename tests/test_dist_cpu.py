@@ -54,3 +54,23 @@ def test_two_gloo_ranks_reduce_and_shard_worlds():
     # each rank draws its own worlds (weak scaling: same per-rank size, different seed)
     assert res[0][3] != res[1][3]
     assert not np.array_equal(res[0][5], res[1][5])
+
+
+def test_reference_arm_prints_the_contract_line():
+    """`bench.py --impl reference` (the CPU path the GPU arm is compared with) prints one JSON line
+    with the arm's keys, its copies declared as zero, on a small sample."""
+    import json
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, os.path.join(root, "bench.py"), "--impl", "reference", "--steps", "2",
+                        "--warmup", "1", "--worlds", "8", "--cpu-sample", "2", "--cpu-seconds", "0.5"],
+                       capture_output=True, text=True, timeout=600, cwd=root)
+    assert r.returncode == 0, r.stderr[-2000:]
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "higher_is_better", "scaling", "dtype",
+              "config", "cpu_baseline", "e2e"):
+        assert k in line, k
+    assert line["impl"] == "reference" and line["value"] > 0
+    assert line["cpu_baseline"]["kind"] in ("port", "reference") and line["cpu_baseline"]["cores"] >= 1
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
