@@ -249,12 +249,14 @@ __device__ __forceinline__ void for_each_partner(const PairCtx& c, const WorldDe
           const int nx = cx + (q % 3) - 1, ny = cy + (q / 3) - 1, nz = cz + dz;
           const int s0 = r0[q], s1 = r1[q];
           for (int s = s0; s < s1; s++) {
-            const int j = g.cellBodies[s];
-            if (j >= i) continue;
+            // the distance test first: one load per entry, and the few entries that pass it read
+            // their body index (the conditions are independent, so the pair set is the same)
             const float4 pB = g.cellPos[s];
             const float r = pA.w + pB.w;
             const V3 d = v3(pA) - v3(pB);
             if (!(dot(d, d) <= r * r)) continue;
+            const int j = g.cellBodies[s];
+            if (j >= i) continue;
             // only the entries of this very cell: a bucket shared by several neighbour cells (or
             // worlds) is scanned once per cell, and each body counts in its own cell only
             const int4 key = g.cellKey[s];
