@@ -1039,7 +1039,7 @@ __global__ void __launch_bounds__(256) k_np_classify(BodyPtrs bd, const WorldDev
 
 // Pass 2a: contacts of box-box pairs that SAT found overlapping.
 #ifndef AVBD_NP_BOX_MINB
-#define AVBD_NP_BOX_MINB 4  // blocks per SM the register allocation must allow (128 registers)
+#define AVBD_NP_BOX_MINB 3  // blocks per SM the register allocation must allow
 #endif
 __global__ void __launch_bounds__(128, AVBD_NP_BOX_MINB) k_np_box(BodyPtrs bd, const WorldDev* __restrict__ worlds, PairPtrs cur, Tick t,
                                                 NarrowScratch ns) {
