@@ -144,3 +144,35 @@ def test_pipelined_reads_equal_synchronous_reads(pipe):
         a.stepRead(1, np.zeros((a.bodyCount, 8), dtype=np.float32))  # not page-locked
     a.destroy()
     b.destroy()
+
+
+def test_pipelined_reads_with_velocity_commands_and_held_steps(pipe):
+    """Velocity commands queued between pipelined steps, with the first steps held (initial pair
+    regions too small) and re-run: the poses read equal those of the same commands and steps made
+    one at a time with synchronous reads."""
+    scenes = [_dense_cluster(seed=s, n=260) for s in (21, 22)]
+    rng = np.random.default_rng(3)
+    cmds = []
+    for k in range(6):
+        dynamic = [o + i for o, sc in zip((0, scenes[0].n_bodies), scenes) for i in range(1, sc.n_bodies)]
+        idx = rng.choice(dynamic, size=5, replace=False).astype(np.int64)
+        vel = rng.uniform(-2, 2, size=(5, 3)).astype(np.float32)
+        cmds.append((idx, vel))
+    a = pipe.createBatch(scenes)
+    bufs = [a.pinnedPoses(), a.pinnedPoses()]
+    got, tags = [], []
+    for k, (idx, vel) in enumerate(cmds):
+        a.setVelocities(idx, linear=vel)
+        tags.append(a.stepRead(1, bufs[k % 2]))
+        if k >= 1:
+            assert a.readDone(tags[k - 1], wait=True)
+            got.append(bufs[(k - 1) % 2].copy())
+    assert a.readDone(tags[-1], wait=True)
+    got.append(bufs[(len(cmds) - 1) % 2].copy())
+    b = pipe.createBatch(scenes)
+    for k, (idx, vel) in enumerate(cmds):
+        b.setVelocities(idx, linear=vel)
+        b.step(1)
+        assert np.array_equal(got[k], b.readPoses()), k
+    a.destroy()
+    b.destroy()
