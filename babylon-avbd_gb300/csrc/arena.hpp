@@ -429,7 +429,7 @@ class Arena {
     CK(cudaMemset(T.pending, 0, N));
     T.colorBodies = dalloc<int>(N);
     T.colorScan = dalloc<int>(color_scan_ints(N));
-    T.slotRef = dalloc<int2>(N);
+    T.slotRef = dalloc<int4>(N);
     T.itemStart = dalloc<int>(N + 1);
     ctr = dalloc<Counters>(1);
     CK(cudaMemset(ctr, 0, sizeof(Counters)));
