@@ -457,7 +457,7 @@ class Arena {
                     G.cellFill, G.cellBodies, G.cellKey, G.cellPos, G.pairTmp, G.bodyBucket, G.large, T.adjStart, T.adjFill, T.activeIndex, T.color, T.won,
                     T.pending, T.colorBodies, T.colorScan, T.slotRef, T.itemStart, T.itemRef, ctr, NC.keys, NC.jid, scanTemp, traffic,
                     poseStage, P.pair, P.count, P.basis, P.ct, NS.sat, NS.boxList, NS.sphereList, NS.sphere2List, NS.ctr, activePairs,
-                    T.adjList, G.bvh.node, G.bvh.parent, G.bvh.escape, G.bvh.minIdx, bsc.keys[0], bsc.keys[1], bsc.hist,
+                    T.adjList, T.adjOther, G.bvh.node, G.bvh.parent, G.bvh.escape, G.bvh.minIdx, bsc.keys[0], bsc.keys[1], bsc.hist,
                     bsc.clusters, bsc.bounds, editRec, editRanges, editTele, io, ctl, queueScratch, replySeg};
     for (void* p : ptrs) dfree(p);
     for (WorldRec& R : W) dfree(R.evDev);
@@ -484,7 +484,8 @@ class Arena {
       CK(cudaStreamSynchronize(s));
     }
     for (void* p : {(void*)P.pair, (void*)P.count, (void*)P.basis, (void*)P.ct, (void*)NS.sat, (void*)NS.boxList,
-                    (void*)NS.sphereList, (void*)NS.sphere2List, (void*)NS.ctr, (void*)activePairs, (void*)T.adjList})
+                    (void*)NS.sphereList, (void*)NS.sphere2List, (void*)NS.ctr, (void*)activePairs, (void*)T.adjList,
+                    (void*)T.adjOther})
       dfree(p);
     P = np;
     NS.sat = dalloc<float4>(cap);
@@ -494,6 +495,7 @@ class Arena {
     NS.ctr = dalloc<int>(3);
     activePairs = dalloc<int>(cap);
     T.adjList = dalloc<uint32_t>(2 * (size_t(jointCap) + size_t(cap)) + 1);
+    T.adjOther = dalloc<int>(2 * (size_t(jointCap) + size_t(cap)) + 1);
     if (slotCap == 0) slotA.init(cap);
     else slotA.grow(cap);
     slotCap = cap;
@@ -587,6 +589,7 @@ class Arena {
     regrow(J.broken, o, N);
     rescratch(activeJoints, N);
     rescratch(T.adjList, 2 * (N + size_t(slotCap)) + 1);
+    rescratch(T.adjOther, 2 * (N + size_t(slotCap)) + 1);
     jointA.grow(nj);
     jointCap = nj;
   }

@@ -222,6 +222,7 @@ struct Topo {
   int* adjStart;   // nBodies + 1
   int* adjFill;    // nBodies
   uint32_t* adjList;
+  int* adjOther;     // per constraint-list entry: the other body if it is dynamic, else -1
   int* activeIndex;  // body -> k (valid for active bodies)
   int* color;        // both colour buffers, 2 * bodyStride entries (see Tick::which)
   int* won;          // round scratch, per body
