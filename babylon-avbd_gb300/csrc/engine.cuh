@@ -230,7 +230,7 @@ struct Topo {
   int* colorBodies;  // active indices k, bucketed by colour, ascending within a bucket
   int* colorScan;    // colour scatter scratch: (colour, block of 256 positions) counts, scanned
   int4* slotRef;     // per bucket slot: (body, list position k, world, iterations | asleep << 30), written with the work items
-  // manifold-contact work items of the dynamic bodies, bucket order (see launch_primal):
+  // manifold-contact work items of the dynamic bodies, bucket order (see primal_chunk):
   int* itemStart;  // per bucket slot, nBodies + 1 (exclusive scan of item counts)
   int4* itemRef;   // item -> (pair slot, item code (item_code), body A, body B)
 };
