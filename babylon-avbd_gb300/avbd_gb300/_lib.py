@@ -56,7 +56,7 @@ class Profile(C.Structure):
                 ("graph_captures", C.c_int64), ("graph_replays", C.c_int64), ("graphs_on", C.c_int32),
                 ("ticks_held", C.c_int32), ("tuned", C.c_int32), ("solve_queue", C.c_int32),
                 ("solve_waves", C.c_int32), ("solve_blocks", C.c_int32), ("radix_bits", C.c_int32),
-                ("pad2", C.c_int32)]
+                ("solve_tile", C.c_int32)]
 
 
 class ServerDesc(C.Structure):

@@ -199,6 +199,7 @@ inline SolveConfig solve_config_from_env(SolveConfig c) {
   if (const char* v = std::getenv("AVBD_SOLVE")) c.queue = std::strcmp(v, "barrier") != 0;
   if (const char* v = std::getenv("AVBD_SOLVE_WAVES")) c.waves = std::max(1, std::atoi(v));
   if (const char* v = std::getenv("AVBD_SOLVE_BLOCKS")) c.blocks = std::max(0, std::atoi(v));
+  if (const char* v = std::getenv("AVBD_SOLVE_TILE")) c.tile = std::atoi(v) == 256 ? 256 : 128;
   if (const char* v = std::getenv("AVBD_SOLVE_WAIT_CYCLES")) c.waitCycles = std::max(0LL, std::atoll(v));
   if (const char* v = std::getenv("AVBD_SOLVE_WAIT_PROBE")) c.probe = std::atoi(v) != 0;
   return c;
@@ -1457,6 +1458,7 @@ class Arena {
     o->solve_waves = solveCfg.waves;
     o->solve_blocks = solveCfg.blocks;
     o->radix_bits = radixBits;
+    o->solve_tile = solveCfg.tile;
   }
 
   // ------------------------------------------------------------------ ticks
@@ -2255,7 +2257,7 @@ class Arena {
                                 (p.bounce ? 1 : 0) | (p.sleeping ? 2 : 0) | (p.events ? 4 : 0) | (p.sleepy ? 8 : 0) |
                                     (p.t.triggerBits ? 16 : 0),
                                 rounds, slotCap, bodyCap, maxWorlds, solveCfg.queue, solveCfg.blocks, solveCfg.waves,
-                                solveCfg.waitCycles, solveCfg.probe, p.radixBits};
+                                solveCfg.tile, solveCfg.waitCycles, solveCfg.probe, p.radixBits};
     for (auto& tr : p.trees) {
       k.push_back(tr.first);
       k.push_back(tr.second);

@@ -327,6 +327,7 @@ struct SolveConfig {
   int queue = 1;                     // 1: tile queue, 0: barrier per colour
   int blocks = 0;                    // persistent blocks (0: every resident block)
   int waves = 2;                     // chunks per block and colour (chunk size = colour / (blocks * waves))
+  int tile = 128;                    // work items per shared-memory tile: 128 (one per thread) or 256
   long long waitCycles = 4000000000LL;  // bound of one wait of the tile queue (SM cycles, ~2 s)
   int probe = 0;                     // tests: every wait past the first stage runs out (see k_solve_queue)
 };

@@ -9,8 +9,9 @@
 //
 // Tuned parameters:
 //   solve    schedule (tile queue / colour barriers), chunks per block and colour (the width of a
-//            colour-bucket chunk, i.e. bodies per block), persistent grid size (blocks per SM, or
-//            a quarter of the SMs for small ticks);
+//            colour-bucket chunk, i.e. bodies per block), work items per shared-memory tile (128 or
+//            256), persistent grid size (all resident blocks, or a quarter of the SMs for small
+//            ticks);
 //   radix    digit width of the tree build's Morton-code sort (4, 6 or 8 bits), on rebuild ticks.
 // A workload class is (device, log2 of the tick's bodies, whether it has joints, iterations).
 // Environment overrides (AVBD_SOLVE*, AVBD_RADIX_BITS) pin a parameter; AVBD_TUNE=0 keeps the
@@ -60,7 +61,7 @@ class Tuner {
     const char* t = std::getenv("AVBD_TUNE");
     enabled = !(t && std::atoi(t) == 0);
     solvePinned = std::getenv("AVBD_SOLVE") || std::getenv("AVBD_SOLVE_WAVES") || std::getenv("AVBD_SOLVE_BLOCKS") ||
-                  std::getenv("AVBD_SOLVE_WAIT_PROBE");
+                  std::getenv("AVBD_SOLVE_TILE") || std::getenv("AVBD_SOLVE_WAIT_PROBE");
     if (const char* r = std::getenv("AVBD_RADIX_BITS")) {
       const int v = std::atoi(r);
       baseRadix = (v == 4 || v == 6) ? v : 8;
@@ -70,20 +71,22 @@ class Tuner {
 
   static std::vector<SolveConfig> solveCandidates(const SolveConfig& b, int sms, int sizeLog2) {
     std::vector<SolveConfig> c;
-    auto add = [&](int queue, int waves, int blocks) {
+    auto add = [&](int queue, int waves, int blocks, int tile) {
       SolveConfig x = b;
       x.queue = queue;
       x.waves = waves;
       x.blocks = blocks;
+      x.tile = tile;
       c.push_back(x);
     };
-    add(1, 1, 0);
-    add(1, 2, 0);
-    add(1, 4, 0);
-    add(1, 2, 3 * sms);
-    add(0, 1, 0);
-    add(0, 2, 0);
-    if (sizeLog2 <= 16) add(0, 1, sms / 4 > 8 ? sms / 4 : 8);  // small ticks: fewer blocks make each colour barrier cheaper
+    for (int tile : {128, 256}) {
+      add(1, 1, 0, tile);
+      add(1, 2, 0, tile);
+      add(0, 1, 0, tile);
+      add(0, 2, 0, tile);
+    }
+    add(1, 4, 0, 128);
+    if (sizeLog2 <= 16) add(0, 1, sms / 4 > 8 ? sms / 4 : 8, 128);  // small ticks: fewer blocks make each colour barrier cheaper
     return c;
   }
   static std::vector<int> radixCandidates() { return {8, 6, 4}; }

@@ -477,12 +477,12 @@ def run_ours(args, dist):
     # the radix width is timed on tree rebuild ticks only (one in bvh_rebuild): tree workloads
     # need that many more ticks for its three candidates' two samples each
     trees = [int(getattr(w.params, "bvh_rebuild", 16) or 16) for w in worlds if getattr(w.params, "broadphase", "auto") != "grid"]
-    tb.step(16 + (7 * max(trees) if trees and args.workload in ("mixed_1m", "cloth_wall") else 0))
+    tb.step(24 + (7 * max(trees) if trees and args.workload in ("mixed_1m", "cloth_wall") else 0))
     pipe.synchronize()
     tp = tb.profileRead()
     tuner = {"tuned": bool(tp["tuned"]), "solve": "tile queue" if tp["solve_queue"] else "colour barriers",
              "chunks_per_block_and_colour": tp["solve_waves"], "persistent_blocks": tp["solve_blocks"] or "all resident",
-             "radix_bits": tp["radix_bits"]}
+             "items_per_tile": tp["solve_tile"], "radix_bits": tp["radix_bits"]}
     tb.destroy()
     log(f"tuned: {tuner}")
     # ---------------- timed region: the clean run (no instrumentation; ticks replay their CUDA
@@ -538,7 +538,7 @@ def run_ours(args, dist):
     if args.workload == "world_mix" and args.full_steps > 0 and len(worlds) >= 2:
         sub = worlds[: len(worlds) // 2]
         tb = pipe.createBatch(sub)  # the autotuner's ticks for this size class, untimed
-        tb.step(16)
+        tb.step(24)
         pipe.synchronize()
         tb.destroy()
         hticks, hel, _, hnb = timed_batch(pipe, stream, sub, 0, args.full_steps)

@@ -158,7 +158,7 @@ typedef struct avbd_profile {
   int32_t solve_waves;
   int32_t solve_blocks;
   int32_t radix_bits;
-  int32_t pad2;
+  int32_t solve_tile;  /* work items per shared-memory tile of the solve (128 or 256) */
 } avbd_profile;
 
 /* ---------------------------------------------------------------- context */

@@ -77,8 +77,9 @@ def test_held_ticks_rerun_exactly(pipe):
     b.destroy()
 
 
-SCHEDULES = [("queue", 1, 0), ("queue", 2, 0), ("queue", 4, 0), ("queue", 2, 24), ("queue", 8, 3),
-             ("barrier", 1, 0), ("barrier", 2, 0), ("barrier", 1, 5)]
+SCHEDULES = [("queue", 1, 0, 128), ("queue", 2, 0, 128), ("queue", 4, 0, 128), ("queue", 2, 24, 128), ("queue", 8, 3, 128),
+             ("queue", 1, 0, 256), ("queue", 2, 24, 256), ("barrier", 1, 0, 128), ("barrier", 2, 0, 128), ("barrier", 1, 5, 128),
+             ("barrier", 1, 0, 256), ("barrier", 2, 0, 256)]
 
 
 def test_solve_schedules_give_the_same_bits(pipe, monkeypatch):
@@ -86,10 +87,11 @@ def test_solve_schedules_give_the_same_bits(pipe, monkeypatch):
     scenes.append(workloads.cloth_wall(grid=8, wall=(3, 2, 2)))
     scenes.append(workloads.box_pile_c0(nx=4, ny=3, nz=4))
     states = []
-    for mode, waves, blocks in SCHEDULES:
+    for mode, waves, blocks, tile in SCHEDULES:
         monkeypatch.setenv("AVBD_SOLVE", mode)
         monkeypatch.setenv("AVBD_SOLVE_WAVES", str(waves))
         monkeypatch.setenv("AVBD_SOLVE_BLOCKS", str(blocks))
+        monkeypatch.setenv("AVBD_SOLVE_TILE", str(tile))
         batch = pipe.createBatch(scenes)
         batch.step(20)
         states.append([batch.readBodyState(k) for k in range(len(scenes))])
