@@ -48,10 +48,12 @@ AVBD_HD float4 qnormalize(float4 q) {
   return make_float4(q.x / l, q.y / l, q.z / l, q.w / l);
 }
 // rotation vector taking b to a (math.ts qsub)
-AVBD_HD V3 qsub(float4 a, float4 b) {
-  float4 t = qmul(a, qinverse(b));
+// qsub(a, b) from b's inverse (qinverse(b)), for a b whose inverse is kept: the same bits
+AVBD_HD V3 qsub_inv(float4 a, float4 bInv) {
+  float4 t = qmul(a, bInv);
   return V3{t.x * 2, t.y * 2, t.z * 2};
 }
+AVBD_HD V3 qsub(float4 a, float4 b) { return qsub_inv(a, qinverse(b)); }
 // integrate a rotation vector (math.ts qaddv)
 AVBD_HD float4 qaddv(float4 a, V3 b) {
   float4 s = qmul(make_float4(b.x, b.y, b.z, 0.f), a);
