@@ -107,6 +107,7 @@ SIGNATURES = [
     ("avbd_batch_read_done", C.c_int, [C.c_void_p, C.c_int64, C.c_int32, _ip]),
     ("avbd_pinned_alloc", C.c_int, [C.c_int64, C.POINTER(C.c_void_p)]),
     ("avbd_pinned_free", C.c_int, [C.c_void_p]),
+    ("avbd_check_division", C.c_int, [C.c_int32, C.c_int64, C.c_uint32, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     ("avbd_batch_set_velocities", C.c_int, [C.c_void_p, _up, C.c_int32, _fp, _fp]),
     ("avbd_world_profile", C.c_int, [C.c_void_p, C.c_int32]),
     ("avbd_world_profile_read", C.c_int, [C.c_void_p, C.POINTER(Profile)]),

@@ -888,6 +888,26 @@ int avbd_pinned_free(void* p) {
   API_END
 }
 
+int avbd_check_division(int32_t device, int64_t n, uint32_t seed, int64_t* reciprocal_mismatches,
+                        int64_t* quotient_mismatches) {
+  API_BEGIN
+  REQUIRE(reciprocal_mismatches && quotient_mismatches && n >= 0, "bad argument");
+  int count = 0;
+  CK(cudaGetDeviceCount(&count));
+  REQUIRE(device >= 0 && device < count, "no such CUDA device");
+  CK(cudaSetDevice(device));
+  unsigned long long* bad = dalloc<unsigned long long>(2);
+  cudaError_t e = cudaMemset(bad, 0, 2 * sizeof(unsigned long long));
+  if (e == cudaSuccess) e = launch_check_division(n, seed, bad);
+  unsigned long long h[2] = {0, 0};
+  if (e == cudaSuccess) e = cudaMemcpy(h, bad, sizeof(h), cudaMemcpyDeviceToHost);
+  cudaFree(bad);
+  CK(e);
+  *reciprocal_mismatches = int64_t(h[0]);
+  *quotient_mismatches = int64_t(h[1]);
+  API_END
+}
+
 int avbd_batch_set_velocities(avbd_batch* b, const uint32_t* indices, int32_t n, const float* velocity, const float* angular) {
   API_BEGIN
   REQUIRE(b, "null batch");

@@ -422,6 +422,10 @@ void launch_gather_poses(const BodyPtrs& b, const int4* seg, int nseg, int total
 void launch_count_active(JointPtrs j, PairPtrs P, const int* slots, int nSlots, const int* joints, int nJoints, Counters* out,
                          cudaStream_t s);
 
+// The LDL^T solve's shared-reciprocal division against the IEEE division: bad[0] += reciprocals that
+// differ (every float of the range), bad[1] += quotients that differ (n seeded operand pairs).
+cudaError_t launch_check_division(long long n, uint32_t seed, unsigned long long* bad);
+
 // Algorithmic bytes of one tick's kernels from its live counts (the bytes each kernel must
 // move at minimum; see launch_traffic): out3 = {primal per iteration, dual per iteration, collision}.
 void launch_traffic(const BodyPtrs& b, JointPtrs j, PairPtrs P, Tick t, Topo topo, const Counters* ctr, int pairBudget,

@@ -491,6 +491,15 @@ int avbd_server_evict(avbd_server* s, int64_t world_id);
 int avbd_server_release(avbd_server* s, int64_t world_id);
 int avbd_server_read_stats(avbd_server* s, avbd_server_stats* out);
 
+/* ---- diagnostics (no reference counterpart) */
+/* The solve's LDL^T factorisation divides by each pivot through its reciprocal (one Newton step on
+ * rcp.approx) and Markstein's fused-multiply-add correction, which must give the bits of the IEEE
+ * division wherever it is used. This checks the reciprocal against 1/d for every float of its
+ * range (both signs) and the quotients on n seeded operand pairs, on `device`, and counts the
+ * results that differ in any bit. */
+int avbd_check_division(int32_t device, int64_t n, uint32_t seed, int64_t* reciprocal_mismatches,
+                        int64_t* quotient_mismatches);
+
 #ifdef __cplusplus
 }
 #endif
