@@ -2161,10 +2161,11 @@ class Arena {
       }
       if (round >= 8) throw Error(AVBD_E_CAPACITY, "pair regions or work items did not converge");
       // timings of held ticks (whose solve did nothing) must not reach the autotuner
-      for (auto& pt : tuner.pending)
-        for (cudaEvent_t ev : {pt.a, pt.b, pt.c, pt.d})
-          if (ev) pool.push_back(ev);
-      tuner.pending.clear();
+      {
+        std::vector<cudaEvent_t> freed;
+        tuner.discard(freed);
+        for (cudaEvent_t ev : freed) pool.push_back(ev);
+      }
       const long long good = c.ticksDone - logBase;
       ticksHeld += (long long)tickLog.size() - good;
       if (good < 0 || good >= (long long)tickLog.size()) throw Error(AVBD_E_STATE, "tick protocol out of step");
@@ -2230,6 +2231,7 @@ class Arena {
     bool bounce = false, sleeping = false, events = false, sleepy = false;
     int radixBits = 8;
     cudaEvent_t tune[4] = {nullptr, nullptr, nullptr, nullptr};  // autotuner timing: solve (0, 1), tree builds (2, 3)
+    int* tuneItems = nullptr;  // autotuner: page-locked slot for the solve's work-item count
     std::vector<std::pair<int, int>> trees;  // (world, rebuild)
   };
   struct GraphEntry {
@@ -2333,6 +2335,7 @@ class Arena {
     launch_body_warmstart(B, worlds, t, s);
     if (prof) span(P_OTHER, o0, mark());
     cudaEvent_t a = prof ? mark() : nullptr;
+    if (p.tuneItems) CK(cudaMemcpyAsync(p.tuneItems, &ctr->itemsTotal, sizeof(int), cudaMemcpyDeviceToHost, s));
     if (p.tune[0]) CK(cudaEventRecord(p.tune[0], s));
     CK(launch_solve(B, worlds, J, P, t, T, ctr, p.maxIter, p.nb, p.sleepy, solveCfg, queueScratch, s));
     if (p.tune[1]) CK(cudaEventRecord(p.tune[1], s));
@@ -2535,15 +2538,17 @@ class Arena {
       tuner.pick(key, rebuild, device_sms(), solveCfg, radixBits, sc, rc, !prof);
       p.radixBits = radixBits;
       if ((sc >= 0 || rc >= 0) && !prof) {
+        int slot = -1;
         if (sc >= 0) {
           p.tune[0] = event();
           p.tune[1] = event();
+          p.tuneItems = tuner.itemSlot(slot);
         }
         if (rc >= 0) {
           p.tune[2] = event();
           p.tune[3] = event();
         }
-        tuner.pending.push_back(Tuner::Pending{key, sc, rc, p.tune[0], p.tune[1], p.tune[2], p.tune[3]});
+        tuner.pending.push_back(Tuner::Pending{key, sc, rc, p.tune[0], p.tune[1], p.tune[2], p.tune[3], slot, nb});
       }
       lastTuned = tuner.settled(key, !p.trees.empty());
     }

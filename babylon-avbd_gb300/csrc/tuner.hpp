@@ -6,6 +6,8 @@
 // the workload itself: the first ticks of a workload class on a device each run one candidate
 // (direct launches, CUDA events around the timed stage), in rotation, and once every candidate
 // has its samples the fastest is kept for that class on that device for the rest of the process.
+// The work of those ticks drifts (piles settle, contacts grow), so a solve sample is its time
+// per unit of the tick's work (bodies plus contact work items, the items read back with it).
 //
 // Tuned parameters:
 //   solve    schedule (tile queue / colour barriers), chunks per block and colour (the width of a
@@ -41,9 +43,27 @@ struct TuneCache {
   std::mutex m;
   std::map<TuneKey, SolveConfig> solve;
   std::map<TuneKey, int> radix;
+  // page-locked slots for the work items of timed ticks (read back in stream order)
+  static constexpr int ITEM_SLOTS = 256;
+  int* items = nullptr;
+  std::vector<int> freeItems;
   static TuneCache& get() {
     static TuneCache c;
     return c;
+  }
+  int takeItemSlot() {  // with m held; -1 when none is free
+    if (!items) {
+      if (cudaHostAlloc(reinterpret_cast<void**>(&items), ITEM_SLOTS * sizeof(int), cudaHostAllocPortable) != cudaSuccess) {
+        items = nullptr;
+        cudaGetLastError();
+        return -1;
+      }
+      for (int k = ITEM_SLOTS - 1; k >= 0; k--) freeItems.push_back(k);
+    }
+    if (freeItems.empty()) return -1;
+    const int k = freeItems.back();
+    freeItems.pop_back();
+    return k;
   }
 };
 
@@ -151,7 +171,27 @@ class Tuner {
     TuneKey key;
     int solveCand, radixCand;
     cudaEvent_t a, b, c, d;
+    int itemSlot, bodies;  // the tick's work: bodies, and its items in TuneCache::items[itemSlot] (-1: none)
   };
+
+  // The page-locked slot a timed tick copies its work-item count into (null when none is free).
+  int* itemSlot(int& slot) {
+    TuneCache& C = TuneCache::get();
+    std::lock_guard<std::mutex> lock(C.m);
+    slot = C.takeItemSlot();
+    return slot >= 0 ? C.items + slot : nullptr;
+  }
+  // Drop pending timings (held ticks), returning their events and item slots.
+  void discard(std::vector<cudaEvent_t>& freed) {
+    TuneCache& C = TuneCache::get();
+    std::lock_guard<std::mutex> lock(C.m);
+    for (auto& pt : pending) {
+      for (cudaEvent_t ev : {pt.a, pt.b, pt.c, pt.d})
+        if (ev) freed.push_back(ev);
+      if (pt.itemSlot >= 0) C.freeItems.push_back(pt.itemSlot);
+    }
+    pending.clear();
+  }
   std::vector<Pending> pending;
 
   // Harvest completed measurements (wait = true: wait for them); returns events to recycle.
@@ -170,9 +210,13 @@ class Tuner {
       auto& st = state(p.key);
       float ms = 0.f;
       if (p.solveCand >= 0 && cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess && size_t(p.solveCand) < st.solveBest.size()) {
-        st.solveBest[p.solveCand] = std::min(st.solveBest[p.solveCand], ms);
+        // time per unit of work (the item count was copied before event b in stream order)
+        const double work = double(p.bodies) + (p.itemSlot >= 0 ? double(C.items[p.itemSlot]) : 0.0);
+        const float score = work > 0.0 ? float(double(ms) * 1e6 / work) : ms;
+        st.solveBest[p.solveCand] = std::min(st.solveBest[p.solveCand], score);
         st.solveSeen[p.solveCand]++;
       }
+      if (p.itemSlot >= 0) C.freeItems.push_back(p.itemSlot);
       if (p.radixCand >= 0 && p.c && cudaEventElapsedTime(&ms, p.c, p.d) == cudaSuccess && size_t(p.radixCand) < st.radixBest.size()) {
         st.radixBest[p.radixCand] = std::min(st.radixBest[p.radixCand], ms);
         st.radixSeen[p.radixCand]++;
