@@ -385,7 +385,8 @@ class Arena {
     for (int w = nw - 1; w >= 0; w--) freeSlots.push_back(w);
     const size_t N = size_t(nb), NJ = size_t(nj);
     for (float4** p : {&B.pose, &B.pose0, &B.poseY}) *p = dalloc<float4>(2 * N);
-    for (float4** p : {&B.vel, &B.ang, &B.vprev, &B.size, &B.mass, &B.rot0i, &B.rotYi, &B.inert}) *p = dalloc<float4>(N);
+    for (float4** p : {&B.vel, &B.ang, &B.vprev, &B.size, &B.mass, &B.inert}) *p = dalloc<float4>(N);
+    for (float4** p : {&B.pose0i, &B.poseYi}) *p = dalloc<float4>(2 * N);
     B.meta = dalloc<int4>(N);
     B.restitution = dalloc<float>(N);
     B.sleep = dalloc<int>(N);
@@ -449,7 +450,7 @@ class Arena {
   }
 
   void release() {
-    void* ptrs[] = {B.pose, B.pose0, B.poseY, B.vel, B.ang, B.vprev, B.size, B.mass, B.rot0i, B.rotYi, B.inert, B.meta,
+    void* ptrs[] = {B.pose, B.pose0, B.poseY, B.vel, B.ang, B.vprev, B.size, B.mass, B.pose0i, B.poseYi, B.inert, B.meta,
                     B.restitution, B.sleep,
                     B.sleepTime, B.watch, B.watchPrev, EV.region, EV.count, EV.cap, EV.step, SB.parent, SB.flags,
                     SB.wake, SB.err, BB.inVel,
@@ -548,9 +549,9 @@ class Arena {
     const size_t o = size_t(bodyCap), N = size_t(nb);
     for (float4** p : {&B.pose, &B.pose0, &B.poseY}) regrow(*p, 2 * o, 2 * N);
     for (float4** p : {&B.vel, &B.ang, &B.vprev, &B.size, &B.mass}) regrow(*p, o, N);
-    for (float4** p : {&B.rot0i, &B.rotYi, &B.inert}) {  // rewritten by every step's warm start
+    for (float4** p : {&B.pose0i, &B.poseYi, &B.inert}) {  // rewritten by every step's warm start
       cudaFree(*p);
-      *p = dalloc<float4>(N);
+      *p = dalloc<float4>(p == &B.inert ? N : 2 * N);
     }
     regrow(B.meta, o, N);
     regrow(B.restitution, o, N);
@@ -634,7 +635,7 @@ class Arena {
   size_t scratchBytes() const { return itemCap * sizeof(int4); }
   static size_t scratchReserve(long long nb) { return size_t(nb) * 512; }
   size_t footprint(long long nb, long long nj, long long slots, long long nw) const {
-    const size_t perBody = 15 * 16 + 2 * 4 + 1 + 16 * 4 + 32 + 4 * PAIR_TMP + 1 + 8;
+    const size_t perBody = 17 * 16 + 2 * 4 + 1 + 16 * 4 + 32 + 4 * PAIR_TMP + 1 + 8;
     const size_t perJoint = 8 + 10 * 16 + 4 + 4 + 8;
     const size_t perSlot = 2 * (8 + 4 + 3 * 16 + MAX_CONTACTS * 64) + 16 + 4 * 4 + 8;
     const size_t perWorld = sizeof(WorldDev) + 4 * 4 + 16 + 4 + MAX_LARGE * 4;

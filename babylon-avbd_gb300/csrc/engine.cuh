@@ -89,8 +89,9 @@ struct BodyPtrs {
   float4 *pose, *pose0, *poseY;  // (pos, rot) at [2i], [2i + 1]: current, step start (x-), inertial
   float4 *vel, *ang, *vprev, *size, *mass;
   // set by each step's warm start for the solve and the velocity update (step-constant there):
-  // qinverse of the step-start and inertial rotations, and (mass, inertia) / dt^2
-  float4 *rot0i, *rotYi, *inert;
+  // (pos, qinverse(rot)) of the step-start and inertial poses at [2i], [2i + 1] (one 32-byte
+  // sector per body read), and (mass, inertia) / dt^2
+  float4 *pose0i, *poseYi, *inert;
   int4* meta;
   float* restitution;  // per body (0 for most)
   int* sleep;          // per body: SLEEP_ASLEEP | SLEEP_ALLOW | BODY_TRIGGER
