@@ -201,7 +201,7 @@ class Tuner {
     size_t keep = 0;
     for (size_t i = 0; i < pending.size(); i++) {
       Pending& p = pending[i];
-      cudaEvent_t last = p.d ? p.d : p.b;
+      cudaEvent_t last = p.b ? p.b : p.d;  // the solve (a, b) runs after the tree builds (c, d) in a tick
       if (!wait && cudaEventQuery(last) != cudaSuccess) {
         pending[keep++] = p;
         continue;
