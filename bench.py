@@ -547,6 +547,38 @@ def run_ours(args, dist):
                 "tick_ms": {"p50": pct(hticks, 50), "p99": pct(hticks, 99), "max": round(float(hticks.max()), 3)},
                 "note": "the first half of the worlds as one batch, steps 1..N, CUDA events per tick"}
         log(f"half batch done: {hel:.1f} ms")
+    # ---------------- the whole mix at that operating point: four quarter batches stepped in rotation
+    # (each tick steps one quarter of the worlds), every world's steps 1..N, per-tick p99
+    rot = None
+    if args.workload == "world_mix" and args.full_steps > 0 and len(worlds) >= 4:
+        parts = [worlds[k * len(worlds) // 4:(k + 1) * len(worlds) // 4] for k in range(4)]
+        for part in parts:  # the autotuner's ticks for each quarter's size class, untimed
+            tb = pipe.createBatch(part)
+            tb.step(24)
+            pipe.synchronize()
+            tb.destroy()
+        batches = [pipe.createBatch(part) for part in parts]
+        pipe.synchronize()
+        torch.cuda.synchronize()
+        n = 4 * args.full_steps
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(n + 1)]
+        ev[0].record(stream)
+        for k in range(n):
+            batches[k % 4].step(1)
+            ev[k + 1].record(stream)
+        pipe.synchronize()
+        torch.cuda.synchronize()
+        rticks = np.array([ev[k].elapsed_time(ev[k + 1]) for k in range(n)])
+        rel = float(ev[0].elapsed_time(ev[-1]))
+        rnb = sum(b.bodyCount for b in batches)
+        for b in batches:
+            b.destroy()
+        rot = {"batches": 4, "worlds": len(worlds), "bodies": int(rnb), "steps_per_world": args.full_steps, "ticks": n,
+               "value": rnb * args.full_steps / (rel / 1000.0), "unit": UNIT,
+               "tick_ms": {"p50": pct(rticks, 50), "p99": pct(rticks, 99), "max": round(float(rticks.max()), 3)},
+               "note": "all worlds as four quarter batches stepped in rotation (one quarter per tick), "
+                       "steps 1..N of every world, CUDA events per tick"}
+        log(f"rotation done: {rel:.1f} ms")
     # ---------------- e2e through the public API with host buffers
     e2e = None
     if not args.no_e2e:
@@ -641,7 +673,7 @@ def run_ours(args, dist):
             "autotuner": tuner,
             "graphs": {"on": bool(pclean["graphs_on"]), "replays_timed": pclean["graph_replays_timed"],
                        "captures_timed": pclean["graph_captures_timed"], "ticks_held": pclean["ticks_held"]},
-            "full_run": full, "half_batch": half, "instrumented": instrumented, "plain_gpu": plain, "stage_ms_per_step": breakdown,
+            "full_run": full, "half_batch": half, "rotation": rot, "instrumented": instrumented, "plain_gpu": plain, "stage_ms_per_step": breakdown,
             "roofline": roof, "cpu_baseline": cpu, "parity": parity, "e2e": e2e,
             "gpu_launches": int(pclean["launches_timed"]), "clocks": clk.summary(), "served": served}
     print(json.dumps(line), flush=True)
